@@ -1,0 +1,204 @@
+/*
+ * bkma_gb300 — C ABI of the GB300-native BKMA hot paths.
+ *
+ * One shared library (libbkma_gb300.so) with C linkage, plain pointers and
+ * sizes. Device pointers are CUDA device addresses on the current device;
+ * `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ * No call throws; every call returns a bkma_status and leaves a message for
+ * bkma_last_error() (thread-local) on failure.
+ *
+ * Reference interfaces replaced (Maison-de-la-Simulation/parallel-advection):
+ *   bkma_run<Solver, Impl>(queue, span3d data, solver, optim, global_scratch)
+ *       src/core/bkma_run.hpp:10-62                -> bkma_adv_step / bkma_conv_run
+ *   impl_selector<Solver>(name)   src/tools/impl_selector.hpp:31-49
+ *                                                  -> bkma_impl_from_name
+ *   AdvectionSolver(ADVParams)    src/solvers/AdvectionSolver.hpp:13-100
+ *                                                  -> bkma_adv_plan_create
+ *   ConvSolver{weight, bias, k, c_in, length}      src/solvers/ConvSolver.hpp:7-45
+ *                                                  -> bkma_conv_plan_create
+ *   create_optim_params / WorkItemDispatch / WorkGroupDispatch
+ *       src/tools/init.hpp:76-102, src/core/bkma_tools.hpp:25-107
+ *                                                  -> plan-time tile choice + bkma_adv_plan_autotune
+ *   fill_buffer_adv / validate_result_adv
+ *       src/tools/init.hpp:31-46, src/tools/validation.hpp:9-80
+ *                                                  -> bkma_adv_fill / bkma_adv_error_norms
+ */
+#ifndef BKMA_GB300_H
+#define BKMA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BKMA_ABI_VERSION 1
+
+typedef enum bkma_status {
+    BKMA_OK = 0,
+    BKMA_ERR_INVALID_ARG = 1, /* reference: std::invalid_argument (bkma_tools.hpp:38-51, bkma_run.hpp:53) */
+    BKMA_ERR_UNSUPPORTED = 2, /* reference: std::runtime_error (impl_selector.hpp:44-47) */
+    BKMA_ERR_CUDA = 3,        /* a CUDA runtime error (message holds cudaGetErrorString) */
+    BKMA_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    BKMA_ERR_NO_DEVICE = 5    /* no CUDA device visible */
+} bkma_status;
+
+typedef enum bkma_dtype { BKMA_F32 = 0, BKMA_F64 = 1, BKMA_BF16 = 2 } bkma_dtype;
+
+/* Strategy names accepted by bkma_impl_from_name (case-insensitive):
+ * "ndrange", "adaptivewg" (the reference's two live strategies), "basicrange"
+ * (out of place), "plain" (per-cell FP64 reference math), "staged" and
+ * "gb300"/"cuda" (the per-line staged kernel). */
+typedef enum bkma_adv_impl {
+    BKMA_ADV_AUTO = 0,   /* staged kernel, autotuned tile */
+    BKMA_ADV_STAGED = 1, /* per-line FP64 departure + weights, lines staged in shared memory */
+    BKMA_ADV_PLAIN = 2   /* per-cell FP64 reference math (AdvectionSolver.hpp:71-99); FP64 only */
+} bkma_adv_impl;
+
+typedef enum bkma_adv_weights {
+    BKMA_W_REFERENCE = 0, /* AdvectionSolver::lag_basis, degree 5 only (AdvectionSolver.hpp:31-51) */
+    BKMA_W_LAGRANGE = 1,  /* textbook Lagrange, degree 3 or 5 (no reference form) */
+    BKMA_W_TABLE = 2      /* caller-supplied per-line weights (bkma_adv_plan_set_weights) */
+} bkma_adv_weights;
+
+typedef struct bkma_adv_plan bkma_adv_plan;
+
+/* Mirrors ADVParams (src/config/AdvectionParams.hpp:10-57). dx, dvx, inv_dx
+ * and the width are derived exactly as ADVParams::update_deltas
+ * (AdvectionParams.cpp:96-103). The line velocity is coord(i0, minVx, dvx)
+ * (AdvectionSolver.hpp:60) unless `velocity` is given. */
+typedef struct bkma_adv_desc {
+    int64_t n0, n1, n2;      /* full field extents, layout_right (n2 fastest) */
+    int64_t i0_offset;       /* first global line of this shard */
+    int64_t i0_count;        /* lines in this shard; 0 = n0 - i0_offset */
+    int32_t dtype;           /* BKMA_F32 or BKMA_F64 */
+    int32_t degree;          /* 3 or 5 */
+    int32_t weights;         /* bkma_adv_weights */
+    int32_t impl;            /* bkma_adv_impl */
+    int32_t inplace;         /* 1: overwrite data (AdaptiveWg/NDRange); 0: write `out` (BasicRange) */
+    int32_t reserved;
+    double dt, minX, maxX, minVx, maxVx;
+    const double *velocity;  /* optional HOST array of i0_count line velocities */
+} bkma_adv_desc;
+
+typedef struct bkma_adv_plan_info {
+    int64_t lines;             /* i0_count */
+    int64_t exception_lines;   /* lines whose departure offset is not constant along n1 */
+    int32_t tile_cols;         /* n2 columns per tile (W) */
+    int32_t tile_slabs;        /* n0 lines per tile (R) */
+    int32_t threads;           /* threads per CTA */
+    int32_t smem_bytes;        /* dynamic shared memory per CTA */
+    int32_t npts;              /* stencil points (degree + 1) */
+    int32_t autotuned;         /* 1 once bkma_adv_plan_autotune picked the tile */
+    int64_t tiles;             /* CTAs per step */
+} bkma_adv_plan_info;
+
+int32_t bkma_abi_version(void);
+const char *bkma_last_error(void);
+
+/* impl_selector (src/tools/impl_selector.hpp:31-49): a strategy name to a
+ * bkma_adv_impl; unknown names give BKMA_ERR_UNSUPPORTED with the reference's
+ * message "<name> is not a valid implementation name.\nShould be: ...". */
+bkma_status bkma_impl_from_name(const char *name, int32_t *impl, int32_t *inplace);
+
+/* AdvectionSolver construction + create_optim_params: validates the
+ * descriptor, computes every line's departure offset and weights in FP64 on
+ * the host (bit-exact with AdvectionSolver::operator's leftNode), uploads the
+ * per-line tables and picks a tile. */
+bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan);
+bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info *info);
+/* Times the candidate tiles on `scratch_field` (a device field of the plan's
+ * shape, contents are overwritten) and keeps the fastest; cached per shape. */
+bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, void *stream);
+/* BKMA_W_TABLE: per-line weights, i0_count x (degree+1) floats (host or
+ * device pointer), applied on the plan's own departure offsets. */
+bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device);
+/* Per-line departure offsets (tap-0 node minus i1, modulo n1) and FP64
+ * fractional shifts d - 2 in [0,1) (host arrays of i0_count). */
+bkma_status bkma_adv_plan_line_table(const bkma_adv_plan *plan, int32_t *offsets, double *shifts);
+bkma_status bkma_adv_plan_destroy(bkma_adv_plan *plan);
+
+/* bkma_run for the advection solver: nsteps time steps of the device field
+ * `data` (i0_count x n1 x n2 elements of dtype). In place when out is NULL or
+ * equal to data. Out of place: the result lands in `out`; with nsteps > 1,
+ * `data` serves as the ping-pong buffer and is overwritten. Asynchronous on
+ * `stream`. */
+bkma_status bkma_adv_step(bkma_adv_plan *plan, void *data, void *out, int32_t nsteps, void *stream);
+/* The same on a HOST field: copies it to a plan-owned device buffer, runs
+ * nsteps, copies the result back and synchronizes `stream`. */
+bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nsteps, void *stream);
+
+/* Device init (fill_buffer_adv, init.hpp:31-46, generalised): mode 0 gives
+ * sin(4*pi*x) like the reference; mode 1 gives sin(2*pi*x) + amp*(2u-1) with
+ * u = bkma_uniform(seed, global cell index). */
+bkma_status bkma_adv_fill(const bkma_adv_plan *plan, void *data, int32_t mode, double amp,
+                          uint64_t seed, void *stream);
+/* Fused error norms of `data` against `ref` (same shape; ref may be FP64 while
+ * data is FP32): out[0] = max|data-ref|, out[1] = max|ref|, out[2] =
+ * sum (data-ref)^2, out[3] = sum ref^2. Host array out[4]; synchronizes. */
+bkma_status bkma_adv_error_norms(const bkma_adv_plan *plan, const void *data, int32_t data_dtype,
+                                 const void *ref, int32_t ref_dtype, double *out, void *stream);
+/* validate_result_adv (validation.hpp:9-80) on the device: max over i2 of
+ * the mean L1 error against sin(4*pi*(x - v*t)), t = max_iter*dt. */
+bkma_status bkma_adv_validate(const bkma_adv_plan *plan, const void *data, int64_t max_iter,
+                              double *highest_l1, double *lowest_l1, void *stream);
+
+/* ---------------------------------------------------------------- batches */
+/* Several independent fields advanced by ONE persistent launch per step over
+ * a device descriptor table (captured in a CUDA graph). */
+typedef struct bkma_adv_field {
+    void *data;              /* device field n0 x n1 x n2 of the batch dtype */
+    int64_t n0, n1, n2;
+    int32_t degree;          /* 3 or 5 */
+    int32_t weights;         /* BKMA_W_REFERENCE or BKMA_W_LAGRANGE */
+    double dt, minX, maxX, minVx, maxVx;
+    const double *velocity;  /* optional HOST array of n0 line velocities */
+} bkma_adv_field;
+
+typedef struct bkma_adv_batch bkma_adv_batch;
+bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields, int32_t dtype,
+                                  bkma_adv_batch **batch);
+bkma_status bkma_adv_batch_step(bkma_adv_batch *batch, int32_t nsteps, void *stream);
+/* Total cells over all fields, and kernel launches per step. */
+bkma_status bkma_adv_batch_info(const bkma_adv_batch *batch, int64_t *cells, int32_t *launches_per_step);
+bkma_status bkma_adv_batch_destroy(bkma_adv_batch *batch);
+
+/* ------------------------------------------------------------------ conv1d */
+typedef enum bkma_conv_semantics {
+    BKMA_CONV_TORCH = 0,     /* cross-correlation (B, C, L) like torch.nn.functional.conv1d */
+    BKMA_CONV_REFERENCE = 1  /* ConvSolver + AdaptiveWg packing (ConvSolver.hpp:20-44) */
+} bkma_conv_semantics;
+
+typedef enum bkma_conv_impl {
+    BKMA_CONV_AUTO = 0,
+    BKMA_CONV_TENSOR = 1,    /* BF16 tcgen05 implicit GEMM, FP32 accumulate in TMEM */
+    BKMA_CONV_PLAIN = 2      /* scalar FP64 / FP32 */
+} bkma_conv_impl;
+
+/* TORCH: data (batch, cin, length), weight (cout, cin, ksize), bias (cout).
+ * REFERENCE: data (n0, cin*length, n2), weight (ksize, cin, cin), bias (cin),
+ * matching Conv1dParams (src/config/Conv1dParams.cpp:44-76) with n0 =
+ * batch and n2 as given. In place the output (length - ksize + 1 per
+ * channel row, or the packed cin*length - ksize + 1 per line) overwrites the
+ * start of each row of `data`. */
+typedef struct bkma_conv_desc {
+    int64_t batch, cin, cout, length, ksize;
+    int64_t n2;              /* REFERENCE semantics only; 1 otherwise */
+    int32_t dtype;           /* BKMA_BF16 (TENSOR), BKMA_F32 or BKMA_F64 (PLAIN) */
+    int32_t semantics;       /* bkma_conv_semantics */
+    int32_t impl;            /* bkma_conv_impl */
+    int32_t inplace;
+} bkma_conv_desc;
+
+typedef struct bkma_conv_plan bkma_conv_plan;
+bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **plan);
+/* Device bytes of scratch the plan owns (halo snapshots, packed weights). */
+bkma_status bkma_conv_plan_scratch_bytes(const bkma_conv_plan *plan, int64_t *bytes);
+bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const void *weight,
+                          const void *bias, void *stream);
+bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,195 @@
+"""bkma_gb300: GB300-native BKMA hot paths (semi-Lagrangian advection and
+in-place conv1d) behind the C ABI of include/bkma_gb300.h.
+
+Python front-end over libbkma_gb300.so (ctypes). Device buffers are torch
+CUDA tensors (torch is the allocator and stream provider only); every
+computation runs in the library's CUDA kernels. There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import BkmaError, check, load  # noqa: F401
+
+_DT = {"f32": _lib.BKMA_F32, "f64": _lib.BKMA_F64, "bf16": _lib.BKMA_BF16}
+_IMPL = {"auto": _lib.BKMA_ADV_AUTO, "staged": _lib.BKMA_ADV_STAGED, "plain": _lib.BKMA_ADV_PLAIN}
+_W = {"reference": _lib.BKMA_W_REFERENCE, "lagrange": _lib.BKMA_W_LAGRANGE,
+      "table": _lib.BKMA_W_TABLE}
+
+
+def _ptr(t) -> int | None:
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    return t.data_ptr()
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def impl_from_name(name: str) -> tuple[int, bool]:
+    """impl_selector (src/tools/impl_selector.hpp:31-49) over the C ABI."""
+    impl, inplace = C.c_int32(), C.c_int32()
+    check(load().bkma_impl_from_name(name.encode(), C.byref(impl), C.byref(inplace)))
+    return impl.value, bool(inplace.value)
+
+
+class AdvectionPlan:
+    """AdvectionSolver + create_optim_params (src/solvers/AdvectionSolver.hpp,
+    src/tools/init.hpp:76-102): per-line FP64 departure and weights, tile
+    choice; `step` is bkma_run (src/core/bkma_run.hpp:10-62)."""
+
+    def __init__(self, n0: int, n1: int, n2: int, *, dtype: str = "f32", degree: int = 5,
+                 weights: str = "reference", impl: str = "auto", dt: float = 1e-4,
+                 minX: float = 0.0, maxX: float = 1.0, minVx: float = 0.0, maxVx: float = 1.0,
+                 velocity=None, i0_offset: int = 0, i0_count: int = 0, inplace: bool = True):
+        lib = load()
+        self.dtype = dtype
+        d = _lib.AdvDesc()
+        d.n0, d.n1, d.n2 = n0, n1, n2
+        d.i0_offset, d.i0_count = i0_offset, i0_count
+        d.dtype, d.degree, d.weights = _DT[dtype], degree, _W[weights]
+        d.impl, d.inplace = (_IMPL[impl] if isinstance(impl, str) else impl), int(inplace)
+        d.dt, d.minX, d.maxX, d.minVx, d.maxVx = dt, minX, maxX, minVx, maxVx
+        self._vel = None
+        if velocity is not None:
+            self._vel = np.ascontiguousarray(velocity, dtype=np.float64)
+            d.velocity = self._vel.ctypes.data_as(C.POINTER(C.c_double))
+        self.desc = d
+        self.n0, self.n1, self.n2 = n0, n1, n2
+        self.lines = i0_count or (n0 - i0_offset)
+        h = C.c_void_p()
+        check(lib.bkma_adv_plan_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    @property
+    def shape(self):
+        return (self.lines, self.n1, self.n2)
+
+    def info(self) -> dict:
+        i = _lib.AdvPlanInfo()
+        check(load().bkma_adv_plan_info_get(self._h, C.byref(i)))
+        return {n: getattr(i, n) for n, _ in i._fields_}
+
+    def step(self, data, out=None, nsteps: int = 1, stream=None):
+        check(load().bkma_adv_step(self._h, _ptr(data), _ptr(out), nsteps, _stream(stream)))
+        return data if out is None else out
+
+    def run_host(self, host: np.ndarray, nsteps: int = 1, stream=None) -> np.ndarray:
+        want = np.float32 if self.dtype == "f32" else np.float64
+        assert host.dtype == want and host.flags["C_CONTIGUOUS"] and host.shape == self.shape
+        check(load().bkma_adv_run_host(self._h, host.ctypes.data, nsteps, _stream(stream)))
+        return host
+
+    def autotune(self, field, stream=None):
+        check(load().bkma_adv_plan_autotune(self._h, _ptr(field), _stream(stream)))
+        return self.info()
+
+    def fill(self, data, mode: int = 0, amp: float = 0.0, seed: int = 0, stream=None):
+        check(load().bkma_adv_fill(self._h, _ptr(data), mode, amp, seed, _stream(stream)))
+        return data
+
+    def error_norms(self, data, ref, stream=None) -> dict:
+        out = (C.c_double * 4)()
+        dd = _DT[_dtype_name(data)]
+        rd = _DT[_dtype_name(ref)]
+        check(load().bkma_adv_error_norms(self._h, _ptr(data), dd, _ptr(ref), rd, out,
+                                          _stream(stream)))
+        maxabs, maxref, se, sr = list(out)
+        return {"max_abs": maxabs, "max_ref": maxref,
+                "max_rel": maxabs / maxref if maxref else 0.0,
+                "l2_rel": (se / sr) ** 0.5 if sr else 0.0}
+
+    def validate(self, data, max_iter: int, stream=None) -> tuple[float, float]:
+        hi, lo = C.c_double(), C.c_double()
+        check(load().bkma_adv_validate(self._h, _ptr(data), max_iter, C.byref(hi), C.byref(lo),
+                                       _stream(stream)))
+        return hi.value, lo.value
+
+    def line_table(self) -> tuple[np.ndarray, np.ndarray]:
+        off = np.zeros(self.lines, dtype=np.int32)
+        sh = np.zeros(self.lines, dtype=np.float64)
+        check(load().bkma_adv_plan_line_table(
+            self._h, off.ctypes.data_as(C.POINTER(C.c_int32)),
+            sh.ctypes.data_as(C.POINTER(C.c_double))))
+        return off, sh
+
+    def set_weights(self, weights, on_device: bool | None = None):
+        if isinstance(weights, np.ndarray):
+            w = np.ascontiguousarray(weights, dtype=np.float32)
+            check(load().bkma_adv_plan_set_weights(self._h, w.ctypes.data, 0))
+        else:
+            check(load().bkma_adv_plan_set_weights(self._h, _ptr(weights), 1))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bkma_adv_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _dtype_name(t) -> str:
+    s = str(t.dtype)
+    if "float32" in s:
+        return "f32"
+    if "float64" in s:
+        return "f64"
+    if "bfloat16" in s:
+        return "bf16"
+    raise ValueError(f"unsupported dtype {t.dtype}")
+
+
+class Conv1dPlan:
+    """ConvSolver + bkma_run for conv1d (src/solvers/ConvSolver.hpp,
+    src/conv1d.cpp:52-87)."""
+
+    def __init__(self, batch: int, cin: int, cout: int, length: int, ksize: int, *,
+                 dtype: str = "bf16", semantics: str = "torch", impl: str = "auto",
+                 inplace: bool = True, n2: int = 1):
+        d = _lib.ConvDesc()
+        d.batch, d.cin, d.cout, d.length, d.ksize, d.n2 = batch, cin, cout, length, ksize, n2
+        d.dtype = _DT[dtype]
+        d.semantics = {"torch": _lib.BKMA_CONV_TORCH, "reference": _lib.BKMA_CONV_REFERENCE}[semantics]
+        d.impl = {"auto": _lib.BKMA_CONV_AUTO, "tensor": _lib.BKMA_CONV_TENSOR,
+                  "plain": _lib.BKMA_CONV_PLAIN}[impl]
+        d.inplace = int(inplace)
+        self.desc = d
+        h = C.c_void_p()
+        check(load().bkma_conv_plan_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    def scratch_bytes(self) -> int:
+        b = C.c_int64()
+        check(load().bkma_conv_plan_scratch_bytes(self._h, C.byref(b)))
+        return b.value
+
+    def run(self, data, weight, bias=None, out=None, stream=None):
+        check(load().bkma_conv_run(self._h, _ptr(data), _ptr(out), _ptr(weight), _ptr(bias),
+                                   _stream(stream)))
+        return data if out is None else out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bkma_conv_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

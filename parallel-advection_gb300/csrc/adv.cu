@@ -1,0 +1,700 @@
+// Semi-Lagrangian advection along n1 (the reference's AdvectionSolver driven
+// by AdaptiveWg/NDRange/BasicRange: src/solvers/AdvectionSolver.hpp:71-99,
+// src/core/AdaptiveWg.hpp:57-140, src/core/NDRange.hpp:4-40,
+// src/core/BasicRange.hpp:27-69), rebuilt for sm_103a.
+//
+// Data layout in HBM: field[i0][i1][i2], n2 fastest (layout_right, as
+// src/types.hpp:12-30). A "line" is (i0, i2): n1 values at stride n2.
+//
+// Because the departure point depends on (i0, i1) only, every line of slab
+// i0 shares one integer tap offset and one set of weights. The plan computes
+// them once on the host in FP64 with the reference's exact formulas (leftNode
+// bit-identical), and lists any line whose offset is not constant along n1
+// (those get per-cell offsets and weights).
+//
+// Kernel `adv_staged`: one CTA per tile = a block of W columns (i2) of one
+// slab, or R whole slabs when n2 is small, spanning all n1 rows. The tile is
+// staged into shared memory with cp.async (16-byte chunks when aligned), with
+// the first npts-1 rows repeated after row n1-1 so the periodic wrap needs no
+// modulo per tap. After one barrier every output is computed from shared
+// memory with register-resident weights in the incremental form
+// f_c + sum_k w_k (f_k - f_c), and written straight to global memory: the
+// tile was read completely before the first write, so in place is legal
+// (the AdaptiveWg scratch/barrier/write-back pattern, with the scratch being
+// the input copy).
+//
+// Kernel `adv_plain`: the same staging, but each output recomputes the
+// reference's per-cell FP64 math (displ, floor, lag_basis) with
+// non-contracted operations: bit-identical to AdvectionSolver::operator().
+// It is the "plain FP64 form" speed baseline.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "adv.cuh"
+#include "adv_plan.cuh"
+#include "common.cuh"
+
+namespace bkma {
+
+// ----------------------------------------------------------------- device
+
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem, int bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if (bytes == 16) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+    } else if (bytes == 8) {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+    } else {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+    }
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Stage rows [0, n1) plus halo rows [n1, n1+H) (copies of rows 0..H-1) of
+// `nslab` slabs x `wc` columns into shared memory laid out
+// [slab (stride sstride elements)][row][col]. When a tile holds whole rows
+// (wc == n2) each slab is one contiguous block in HBM and is copied flat.
+// vec_ok: the global field allows 16-byte chunks for this tile.
+template <typename T>
+__device__ __forceinline__ void stage_tile(T *sm, const T *__restrict__ g, int64_t n1,
+                                           int64_t n2, int64_t line0, int nslab, int64_t c0,
+                                           int wc, int halo, int vec_ok, int sstride) {
+    constexpr int VEC = 16 / (int)sizeof(T);
+    if (wc == n2) {
+        const int body = (int)n1 * wc;
+        const int hal = halo * wc;
+        const bool v = vec_ok && (body % VEC) == 0;
+        const int chunks = v ? body / VEC : body;
+        const int per_slab = chunks + hal;
+        const int total = nslab * per_slab;
+        for (int i = threadIdx.x; i < total; i += blockDim.x) {
+            const int s = i / per_slab;
+            const int j = i - s * per_slab;
+            const T *gs = g + (line0 + s) * n1 * n2;
+            T *ss = sm + (int64_t)s * sstride;
+            if (j < chunks) {
+                if (v)
+                    cp_async(ss + j * VEC, gs + (int64_t)j * VEC, 16);
+                else
+                    cp_async(ss + j, gs + j, (int)sizeof(T));
+            } else {
+                const int h = j - chunks;
+                cp_async(ss + body + h, gs + h, (int)sizeof(T));
+            }
+        }
+    } else {
+        const int rows = (int)n1 + halo;
+        const int vec = (vec_ok && (wc % VEC) == 0) ? VEC : 1;
+        const int cpr = wc / vec;
+        const int per_slab = rows * cpr;
+        const int total = nslab * per_slab;
+        for (int i = threadIdx.x; i < total; i += blockDim.x) {
+            const int s = i / per_slab;
+            const int rem = i - s * per_slab;
+            const int r = rem / cpr;
+            const int ch = rem - r * cpr;
+            const int gr = r < n1 ? r : r - (int)n1;
+            const T *src = g + ((line0 + s) * n1 + gr) * n2 + c0 + (int64_t)ch * vec;
+            T *dst = sm + (int64_t)s * sstride + r * wc + ch * vec;
+            cp_async(dst, src, vec * (int)sizeof(T));
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+}
+
+// Tile coordinates of block `t`.
+struct TileCoord {
+    int64_t line0;
+    int nslab;
+    int64_t c0;
+    int wc;
+};
+
+__device__ __forceinline__ TileCoord tile_of(int64_t t, int64_t lines, int64_t n2, int R,
+                                             int W, int64_t ncb) {
+    TileCoord tc;
+    const int64_t lt = t / ncb;
+    const int64_t cb = t - lt * ncb;
+    tc.line0 = lt * R;
+    tc.nslab = (int)min((int64_t)R, lines - tc.line0);
+    tc.c0 = cb * W;
+    tc.wc = (int)min((int64_t)W, n2 - tc.c0);
+    return tc;
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(512) adv_staged(AdvStagedArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    constexpr int C = NT / 2 - 1;  // centre tap: the left node of the foot cell
+    const TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, a.R, a.W, a.ncb);
+    const int sstride = slab_stride(a.n1, NT - 1, tc.wc, (int)sizeof(T));
+    stage_tile<T>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, NT - 1, a.vec_ok,
+                  sstride);
+
+    const int n1 = (int)a.n1;
+    const int wc = tc.wc;
+    const int total = n1 * wc;
+    const int dr = blockDim.x / wc;
+    const int dc = blockDim.x - dr * wc;
+    const int r_init = threadIdx.x / wc;
+    const int c_init = threadIdx.x - r_init * wc;
+    for (int s = 0; s < tc.nslab; ++s) {
+        const int64_t line = tc.line0 + s;
+        const T *S = sm + (int64_t)s * sstride;
+        T *G = a.dst + line * a.n1 * a.n2 + tc.c0;
+        const int exc = a.exc_index[line];
+        if (exc < 0) {
+            const int base = a.base[line];
+            T w[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k) w[k] = a.w[line * NT + k];
+            int r = r_init, c = c_init;
+            for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+                int rr = r + base;
+                if (rr >= n1) rr -= n1;
+                const T *p = S + rr * wc + c;
+                const T fc = p[C * wc];
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < NT; ++k)
+                    if (k != C) acc = fma(w[k], p[k * wc] - fc, acc);
+                G[(int64_t)r * a.n2 + c] = fc + acc;
+                c += dc;
+                r += dr;
+                if (c >= wc) {
+                    c -= wc;
+                    r += 1;
+                }
+            }
+        } else {
+            // Line whose departure offset varies along n1: per-cell table.
+            const AdvExcCell<T> *cells = a.exc + (int64_t)exc * n1;
+            int r = r_init, c = c_init;
+            for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+                const AdvExcCell<T> &e = cells[r];
+                int rr = r + e.base;
+                if (rr >= n1) rr -= n1;
+                const T *p = S + rr * wc + c;
+                const T fc = p[C * wc];
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < NT; ++k)
+                    if (k != C) acc = fma(e.w[k], p[k * wc] - fc, acc);
+                G[(int64_t)r * a.n2 + c] = fc + acc;
+                c += dc;
+                r += dr;
+                if (c >= wc) {
+                    c -= wc;
+                    r += 1;
+                }
+            }
+        }
+    }
+}
+
+// Plain FP64 form: the reference's per-cell math, bit-identical.
+__global__ void __launch_bounds__(512) adv_plain(AdvPlainArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *sm = reinterpret_cast<double *>(smem_raw);
+    const TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, a.R, a.W, a.ncb);
+    const int sstride = slab_stride(a.n1, 0, tc.wc, 8);
+    stage_tile<double>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, 0, a.vec_ok,
+                       sstride);
+    const int n1 = (int)a.n1;
+    const int wc = tc.wc;
+    const int total = n1 * wc;
+    const uint64_t un1 = (uint64_t)a.n1;
+    for (int s = 0; s < tc.nslab; ++s) {
+        const int64_t line = tc.line0 + s;
+        const double *S = sm + (int64_t)s * sstride;
+        double *G = a.dst + line * a.n1 * a.n2 + tc.c0;
+        const double vx = a.vx[line];
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            const int r = idx / wc;
+            const int c = idx - r * wc;
+            double d;
+            const int left = adv_departure(a.phys, r, vx, &d);
+            double coef[6];
+            lag_basis_ref5(d, coef);
+            const int ipos1 = left - 2;
+            double value = 0.;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const uint64_t id = (un1 + (uint64_t)(int64_t)ipos1 + (uint64_t)k) % un1;
+                value = dadd(value, dmul(coef[k], S[(int64_t)id * wc + c]));
+            }
+            G[(int64_t)r * a.n2 + c] = value;
+        }
+    }
+}
+
+// ----------------------------------------------------------------- host
+
+namespace {
+
+// Textbook Lagrange basis on nodes 0..npts-1 at px.
+void lag_textbook(int npts, double px, double *c) {
+    for (int j = 0; j < npts; ++j) {
+        double num = 1.0, den = 1.0;
+        for (int m = 0; m < npts; ++m) {
+            if (m == j) continue;
+            num *= (px - (double)m);
+            den *= (double)(j - m);
+        }
+        c[j] = num / den;
+    }
+}
+
+// Weights of the stencil whose tap 0 sits at leftNode-(npts/2-1), for a foot
+// point with d = 2 + frac (frac in [0,1)).
+void stencil_weights(int weights_kind, int npts, double d, double *w) {
+    if (weights_kind == BKMA_W_REFERENCE) {
+        lag_basis_ref5(d, w);
+    } else {
+        lag_textbook(npts, (double)(npts / 2 - 1) + (d - 2.0), w);
+    }
+}
+
+struct TuneKey {
+    int dtype, npts, impl;
+    int64_t lines, n1, n2;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(dtype, npts, impl, lines, n1, n2) <
+               std::tie(o.dtype, o.npts, o.impl, o.lines, o.n1, o.n2);
+    }
+};
+struct TuneVal {
+    int W, R, threads;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune_cache;
+
+}  // namespace
+
+}  // namespace bkma
+
+namespace bkma {
+namespace {
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+// Default tile: columns of one slab when n2 is wide enough for 64-byte row
+// segments, otherwise whole slabs; about 32-64 KB of shared memory per CTA.
+void default_tile(AdvPlanImpl &p) {
+    const int64_t n2 = p.desc.n2;
+    const int min_cols = 64 / p.esize;  // 16 FP32 / 8 FP64 columns = 64 B rows
+    if (n2 >= min_cols) {
+        p.W = min_cols;
+        p.R = 1;
+    } else {
+        p.W = (int)n2;
+        const size_t per = p.smem_bytes(p.W, 1);
+        int r = (int)std::max<size_t>(1, (48 * 1024) / std::max<size_t>(per, 1));
+        r = (int)std::min<int64_t>(r, p.lines);
+        p.R = std::max(1, r);
+    }
+    while (p.R > 1 && p.smem_bytes(p.W, p.R) > kMaxSmem) p.R /= 2;
+    while (p.W > 1 && p.smem_bytes(p.W, p.R) > kMaxSmem) p.W /= 2;
+    p.threads = 256;
+}
+
+template <typename T>
+bkma_status upload_tables(AdvPlanImpl &p) {
+    const int64_t L = p.lines;
+    const int NT = p.npts;
+    std::vector<T> w((size_t)(L * NT));
+    for (int64_t i = 0; i < L * NT; ++i) w[(size_t)i] = (T)p.w64[(size_t)i];
+    BKMA_CUDA_TRY(cudaMalloc(&p.d_base, sizeof(int32_t) * (size_t)L));
+    BKMA_CUDA_TRY(cudaMalloc(&p.d_w, sizeof(T) * (size_t)(L * NT)));
+    BKMA_CUDA_TRY(cudaMalloc(&p.d_exc_index, sizeof(int32_t) * (size_t)L));
+    BKMA_CUDA_TRY(cudaMalloc(&p.d_vx, sizeof(double) * (size_t)L));
+    BKMA_CUDA_TRY(cudaMemcpy(p.d_base, p.base.data(), sizeof(int32_t) * L, cudaMemcpyHostToDevice));
+    BKMA_CUDA_TRY(cudaMemcpy(p.d_w, w.data(), sizeof(T) * L * NT, cudaMemcpyHostToDevice));
+    BKMA_CUDA_TRY(cudaMemcpy(p.d_exc_index, p.exc_index.data(), sizeof(int32_t) * L,
+                             cudaMemcpyHostToDevice));
+    BKMA_CUDA_TRY(cudaMemcpy(p.d_vx, p.vx.data(), sizeof(double) * L, cudaMemcpyHostToDevice));
+    if (p.n_exc > 0) {
+        // Per-cell tables for exception lines.
+        const int64_t n1 = p.desc.n1;
+        std::vector<AdvExcCell<T>> cells((size_t)(p.n_exc * n1));
+        for (int64_t l = 0; l < L; ++l) {
+            const int slot = p.exc_index[(size_t)l];
+            if (slot < 0) continue;
+            for (int64_t i1 = 0; i1 < n1; ++i1) {
+                double d;
+                const int left = adv_departure(p.phys, (int)i1, p.vx[(size_t)l], &d);
+                int64_t b = ((int64_t)left - (NT / 2 - 1) - i1) % n1;
+                if (b < 0) b += n1;
+                double wd[16];
+                stencil_weights(p.desc.weights, NT, d, wd);
+                AdvExcCell<T> &e = cells[(size_t)(slot * n1 + i1)];
+                e.base = (int32_t)b;
+                for (int k = 0; k < kMaxTaps; ++k) e.w[k] = k < NT ? (T)wd[k] : T(0);
+            }
+        }
+        BKMA_CUDA_TRY(cudaMalloc(&p.d_exc, sizeof(AdvExcCell<T>) * cells.size()));
+        BKMA_CUDA_TRY(cudaMemcpy(p.d_exc, cells.data(), sizeof(AdvExcCell<T>) * cells.size(),
+                                 cudaMemcpyHostToDevice));
+    }
+    return BKMA_OK;
+}
+
+// 16-byte chunks are legal when the field base is aligned and every row
+// (column tiles) or every slab (whole-row tiles) starts on 16 bytes.
+bool vec_ok(const AdvPlanImpl &p, const void *src, int W) {
+    const int64_t es = p.esize;
+    if ((uintptr_t)src % 16 != 0) return false;
+    if (W >= p.desc.n2) return (p.desc.n1 * p.desc.n2 * es) % 16 == 0;
+    return ((p.desc.n2 * es) % 16 == 0) && ((int64_t)W * es % 16 == 0);
+}
+
+template <typename T, int NT>
+cudaError_t launch_staged_t(const AdvPlanImpl &p, const T *src, T *dst, int W, int R,
+                            int threads, cudaStream_t st) {
+    AdvStagedArgs<T> a;
+    a.src = src;
+    a.dst = dst;
+    a.n1 = p.desc.n1;
+    a.n2 = p.desc.n2;
+    a.lines = p.lines;
+    a.W = W;
+    a.R = R;
+    a.ncb = p.ncb(W);
+    a.vec_ok = vec_ok(p, src, W) ? 1 : 0;
+    a.base = p.d_base;
+    a.w = (const T *)p.d_w;
+    a.exc_index = p.d_exc_index;
+    a.exc = (const AdvExcCell<T> *)p.d_exc;
+    const size_t smem = p.smem_bytes(W, R);
+    auto kern = adv_staged<T, NT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = p.tiles(W, R);
+    kern<<<(unsigned)grid, threads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_staged_npts(const AdvPlanImpl &p, const void *src, void *dst, int W, int R,
+                               int threads, cudaStream_t st) {
+    const T *s = (const T *)src;
+    T *d = (T *)dst;
+    switch (p.npts) {
+    case 4: return launch_staged_t<T, 4>(p, s, d, W, R, threads, st);
+    case 6: return launch_staged_t<T, 6>(p, s, d, W, R, threads, st);
+    case 10: return launch_staged_t<T, 10>(p, s, d, W, R, threads, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_plain(const AdvPlanImpl &p, const double *src, double *dst, int W, int R,
+                         int threads, cudaStream_t st) {
+    AdvPlainArgs a;
+    a.src = src;
+    a.dst = dst;
+    a.n1 = p.desc.n1;
+    a.n2 = p.desc.n2;
+    a.lines = p.lines;
+    a.W = W;
+    a.R = R;
+    a.ncb = p.ncb(W);
+    a.vec_ok = vec_ok(p, src, W) ? 1 : 0;
+    a.vx = p.d_vx;
+    a.phys = p.phys;
+    const size_t smem = p.smem_bytes(W, R);
+    cudaError_t e =
+        cudaFuncSetAttribute(adv_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    adv_plain<<<(unsigned)p.tiles(W, R), threads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_once(const AdvPlanImpl &p, const void *src, void *dst, int W, int R,
+                        int threads, cudaStream_t st) {
+    if (p.desc.impl == BKMA_ADV_PLAIN)
+        return launch_plain(p, (const double *)src, (double *)dst, W, R, threads, st);
+    if (p.desc.dtype == BKMA_F32) return launch_staged_npts<float>(p, src, dst, W, R, threads, st);
+    return launch_staged_npts<double>(p, src, dst, W, R, threads, st);
+}
+
+}  // namespace
+
+bkma_status adv_launch(AdvPlanImpl &p, void *data, void *out, int nsteps, cudaStream_t st) {
+    const bool inplace = (out == nullptr || out == data);
+    // Out of place: an odd number of steps alternates data->out->data...->out;
+    // an even number first steps `data` in place, then alternates.
+    int t0 = 0;
+    if (!inplace && nsteps > 0 && nsteps % 2 == 0) {
+        cudaError_t e = launch_once(p, data, data, p.W, p.R, p.threads, st);
+        if (e != cudaSuccess) return cuda_fail(e, "adv kernel launch");
+        t0 = 1;
+    }
+    for (int t = t0; t < nsteps; ++t) {
+        void *src = data, *dst = data;
+        if (!inplace) {
+            const bool to_out = ((t - t0) % 2) == 0;
+            src = to_out ? data : out;
+            dst = to_out ? out : data;
+        }
+        cudaError_t e = launch_once(p, src, dst, p.W, p.R, p.threads, st);
+        if (e != cudaSuccess) return cuda_fail(e, "adv kernel launch");
+    }
+    return BKMA_OK;
+}
+
+// Per-line precompute of a plan (bit-exact leftNode, FP64 weights).
+bkma_status adv_precompute(AdvPlanImpl &p) {
+    const bkma_adv_desc &d = p.desc;
+    const int NT = p.npts;
+    p.base.assign((size_t)p.lines, 0);
+    p.shift.assign((size_t)p.lines, 0.0);
+    p.vx.assign((size_t)p.lines, 0.0);
+    p.w64.assign((size_t)(p.lines * NT), 0.0);
+    p.exc_index.assign((size_t)p.lines, -1);
+    p.n_exc = 0;
+    const int64_t n1 = d.n1;
+    for (int64_t l = 0; l < p.lines; ++l) {
+        const int64_t g = d.i0_offset + l;
+        const double v = d.velocity ? d.velocity[l] : adv_coord((int)g, p.phys.minVx, p.phys.dvx);
+        p.vx[(size_t)l] = v;
+        double d0;
+        const int left0 = adv_departure(p.phys, 0, v, &d0);
+        int64_t b0 = ((int64_t)left0 - (NT / 2 - 1)) % n1;
+        if (b0 < 0) b0 += n1;
+        p.base[(size_t)l] = (int32_t)b0;
+        p.shift[(size_t)l] = d0 - 2.0;
+        stencil_weights(d.weights, NT, d0, &p.w64[(size_t)(l * NT)]);
+        if (d.impl == BKMA_ADV_PLAIN) continue;
+        for (int64_t i1 = 1; i1 < n1; ++i1) {
+            double di;
+            const int left = adv_departure(p.phys, (int)i1, v, &di);
+            int64_t b = ((int64_t)left - (NT / 2 - 1) - i1) % n1;
+            if (b < 0) b += n1;
+            if (b != b0) {
+                p.exc_index[(size_t)l] = (int32_t)p.n_exc++;
+                break;
+            }
+        }
+    }
+    if (d.impl == BKMA_ADV_PLAIN) return BKMA_OK;
+    if (d.dtype == BKMA_F32) return upload_tables<float>(p);
+    return upload_tables<double>(p);
+}
+
+bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
+    const TuneKey key{p.desc.dtype, p.npts, p.desc.impl, p.lines, p.desc.n1, p.desc.n2};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            p.W = it->second.W;
+            p.R = it->second.R;
+            p.threads = it->second.threads;
+            p.autotuned = true;
+            return BKMA_OK;
+        }
+    }
+    std::vector<TuneVal> cands;
+    const int64_t n2 = p.desc.n2;
+    const int ths[2] = {256, 512};
+    if (n2 >= 8) {
+        for (int W : {8, 16, 32, 64})
+            if (W <= n2 || W == 8)
+                for (int t : ths) cands.push_back({W, 1, t});
+    }
+    for (int R : {1, 2, 4, 8, 16})
+        if (n2 < 32 && R <= p.lines)
+            for (int t : ths) cands.push_back({(int)n2, R, t});
+    cudaEvent_t e0, e1;
+    BKMA_CUDA_TRY(cudaEventCreate(&e0));
+    BKMA_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    TuneVal bestv{p.W, p.R, p.threads};
+    for (const TuneVal &c : cands) {
+        if (p.smem_bytes(c.W, c.R) > kMaxSmem) continue;
+        cudaError_t err = launch_once(p, field, field, c.W, c.R, c.threads, st);  // warm-up
+        if (err != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        const int reps = 3;
+        cudaEventRecord(e0, st);
+        for (int i = 0; i < reps; ++i) launch_once(p, field, field, c.W, c.R, c.threads, st);
+        cudaEventRecord(e1, st);
+        BKMA_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            bestv = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p.W = bestv.W;
+    p.R = bestv.R;
+    p.threads = bestv.threads;
+    p.autotuned = true;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = bestv;
+    return BKMA_OK;
+}
+
+}  // namespace bkma
+
+// ================================================================= C ABI
+using namespace bkma;
+
+extern "C" {
+
+bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan) {
+    BKMA_CHECK_ARG(desc && plan, "bkma_adv_plan_create: null argument");
+    *plan = nullptr;
+    const bkma_adv_desc &d = *desc;
+    BKMA_CHECK_ARG(d.n0 > 0 && d.n1 > 0 && d.n2 > 0, "n0, n1, n2 must be positive");
+    BKMA_CHECK_ARG(d.n1 < (1 << 24) && d.n2 < (1 << 24), "n1 and n2 must be < 2^24");
+    BKMA_CHECK_ARG(d.i0_offset >= 0 && d.i0_offset < d.n0, "i0_offset out of range");
+    const int64_t count = d.i0_count == 0 ? d.n0 - d.i0_offset : d.i0_count;
+    BKMA_CHECK_ARG(count > 0 && d.i0_offset + count <= d.n0, "i0_count out of range");
+    BKMA_CHECK_ARG(d.dtype == BKMA_F32 || d.dtype == BKMA_F64, "dtype must be BKMA_F32 or BKMA_F64");
+    BKMA_CHECK_ARG(d.impl >= BKMA_ADV_AUTO && d.impl <= BKMA_ADV_PLAIN, "unknown impl");
+    BKMA_CHECK_ARG(d.weights >= BKMA_W_REFERENCE && d.weights <= BKMA_W_TABLE, "unknown weights");
+    if (d.weights == BKMA_W_REFERENCE)
+        BKMA_CHECK_ARG(d.degree == 5, "reference weights (lag_basis) exist for degree 5 only");
+    else
+        BKMA_CHECK_ARG(d.degree == 3 || d.degree == 5 || d.degree == 9, "degree must be 3, 5 or 9");
+    if (d.impl == BKMA_ADV_PLAIN) {
+        BKMA_CHECK_ARG(d.dtype == BKMA_F64 && d.weights == BKMA_W_REFERENCE,
+                       "the plain form is the reference's FP64 degree-5 operator");
+    }
+    BKMA_CHECK_ARG(d.maxX > d.minX, "maxX must exceed minX");
+    BKMA_CHECK_ARG(std::isfinite(d.dt), "dt must be finite");
+
+    auto *pl = new (std::nothrow) bkma_adv_plan;
+    if (!pl) return fail(BKMA_ERR_INVALID_ARG, "out of host memory");
+    AdvPlanImpl &p = pl->impl;
+    p.desc = d;
+    p.desc.i0_count = count;
+    p.desc.velocity = nullptr;
+    p.lines = count;
+    p.npts = d.degree + 1;
+    p.esize = d.dtype == BKMA_F32 ? 4 : 8;
+    p.phys.n0 = d.n0;
+    p.phys.n1 = d.n1;
+    p.phys.dt = d.dt;
+    p.phys.minX = d.minX;
+    p.phys.maxX = d.maxX;
+    p.phys.minVx = d.minVx;
+    p.phys.maxVx = d.maxVx;
+    adv_update_deltas(p.phys);
+    cudaGetDevice(&p.device);
+    // velocity pointer is only read during create
+    bkma_adv_desc dv = p.desc;
+    dv.velocity = d.velocity;
+    std::swap(p.desc, dv);
+    bkma_status s = adv_precompute(p);
+    std::swap(p.desc, dv);
+    p.desc.velocity = nullptr;
+    if (s == BKMA_OK && d.impl == BKMA_ADV_PLAIN) {
+        cudaError_t e = cudaMalloc(&p.d_vx, sizeof(double) * (size_t)p.lines);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(p.d_vx, p.vx.data(), sizeof(double) * p.lines, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) s = cuda_fail(e, "plan tables");
+    }
+    if (s != BKMA_OK) {
+        delete pl;
+        return s;
+    }
+    default_tile(p);
+    if (p.smem_bytes(p.W, p.R) > kMaxSmem) {
+        delete pl;
+        return fail(BKMA_ERR_UNSUPPORTED, "n1 too long for a shared-memory line tile");
+    }
+    *plan = pl;
+    return BKMA_OK;
+}
+
+bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info *info) {
+    BKMA_CHECK_ARG(plan && info, "null argument");
+    const AdvPlanImpl &p = plan->impl;
+    info->lines = p.lines;
+    info->exception_lines = p.n_exc;
+    info->tile_cols = (int32_t)std::min<int64_t>(p.W, p.desc.n2);
+    info->tile_slabs = p.R;
+    info->threads = p.threads;
+    info->smem_bytes = (int32_t)p.smem_bytes(p.W, p.R);
+    info->npts = p.npts;
+    info->autotuned = p.autotuned ? 1 : 0;
+    info->tiles = p.tiles(p.W, p.R);
+    return BKMA_OK;
+}
+
+bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *field, void *stream) {
+    BKMA_CHECK_ARG(plan && field, "null argument");
+    return adv_autotune(plan->impl, field, (cudaStream_t)stream);
+}
+
+bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device) {
+    BKMA_CHECK_ARG(plan && weights, "null argument");
+    AdvPlanImpl &p = plan->impl;
+    BKMA_CHECK_ARG(p.desc.weights == BKMA_W_TABLE, "plan was not created with BKMA_W_TABLE");
+    BKMA_CHECK_ARG(p.desc.dtype == BKMA_F32, "table weights are FP32");
+    const size_t bytes = sizeof(float) * (size_t)(p.lines * p.npts);
+    BKMA_CUDA_TRY(cudaMemcpy(p.d_w, weights, bytes,
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    return BKMA_OK;
+}
+
+bkma_status bkma_adv_plan_line_table(const bkma_adv_plan *plan, int32_t *offsets, double *shifts) {
+    BKMA_CHECK_ARG(plan, "null argument");
+    const AdvPlanImpl &p = plan->impl;
+    if (offsets) std::memcpy(offsets, p.base.data(), sizeof(int32_t) * (size_t)p.lines);
+    if (shifts) std::memcpy(shifts, p.shift.data(), sizeof(double) * (size_t)p.lines);
+    return BKMA_OK;
+}
+
+bkma_status bkma_adv_plan_destroy(bkma_adv_plan *plan) {
+    delete plan;
+    return BKMA_OK;
+}
+
+bkma_status bkma_adv_step(bkma_adv_plan *plan, void *data, void *out, int32_t nsteps, void *stream) {
+    BKMA_CHECK_ARG(plan && data, "bkma_adv_step: null argument");
+    BKMA_CHECK_ARG(nsteps >= 0, "nsteps must be >= 0");
+    AdvPlanImpl &p = plan->impl;
+    return adv_launch(p, data, out, nsteps, (cudaStream_t)stream);
+}
+
+bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nsteps, void *stream) {
+    BKMA_CHECK_ARG(plan && host_data, "bkma_adv_run_host: null argument");
+    AdvPlanImpl &p = plan->impl;
+    const size_t bytes = (size_t)(p.lines * p.desc.n1 * p.desc.n2) * (size_t)p.esize;
+    if (p.host_buf_bytes < bytes) {
+        cudaFree(p.d_host_buf);
+        p.d_host_buf = nullptr;
+        p.host_buf_bytes = 0;
+        BKMA_CUDA_TRY(cudaMalloc(&p.d_host_buf, bytes));
+        p.host_buf_bytes = bytes;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    BKMA_CUDA_TRY(cudaMemcpyAsync(p.d_host_buf, host_data, bytes, cudaMemcpyHostToDevice, st));
+    bkma_status s = adv_launch(p, p.d_host_buf, nullptr, nsteps, st);
+    if (s != BKMA_OK) return s;
+    BKMA_CUDA_TRY(cudaMemcpyAsync(host_data, p.d_host_buf, bytes, cudaMemcpyDeviceToHost, st));
+    BKMA_CUDA_TRY(cudaStreamSynchronize(st));
+    return BKMA_OK;
+}
+
+}  // extern "C"

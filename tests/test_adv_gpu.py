@@ -1,0 +1,259 @@
+"""Advection parity on the GPU, through the C ABI, against the CPU oracle
+(which tests/test_oracle_golden.py pins to the reference's own code).
+
+Tolerances:
+  - plain FP64 kernel: bit-exact (same operation order, no FMA contraction);
+  - staged FP64 kernel: |err| <= 1e-11 * max|f| (per-line weights use the
+    line's i1 = 0 fractional shift, which differs from the per-cell one by
+    at most ~1e-12);
+  - staged FP32 kernel: max |err| <= (3e-7 * steps + 2e-7) * max|f| against the
+    FP64 oracle (FP32 storage rounding accumulates per step).
+"""
+import numpy as np
+import pytest
+
+from oracle import AdvParams
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # n0, n1, n2, dt, minX, maxX, minVx, maxVx
+    (8, 64, 3, 0.0010000000474974513, 0.0, 1.0, -1.0, 1.0),
+    (5, 999, 2, 0.37, -0.5, 2.5, -3.0, 3.3),
+    (16, 1024, 1, 1e-4, 0.0, 1.0, 0.0, 1.0),
+    (4, 128, 17, 0.5, 0.0, 1.0, -4.0, 4.0),
+    (3, 256, 64, 0.003, 0.0, 1.0, -1.0, 1.0),
+    (2, 1000, 33, 0.0011, 0.0, 1.0, -1.0, 1.0),
+]
+
+
+def _init(p, seed=0):
+    rng = np.random.default_rng(seed)
+    x = p.minX + np.arange(p.n1) * ((p.maxX - p.minX) / p.n1)
+    f = np.sin(2 * np.pi * (x - p.minX) / (p.maxX - p.minX))[None, :, None]
+    f = f + 0.01 * rng.uniform(-1, 1, (p.n0, p.n1, p.n2))
+    return np.ascontiguousarray(f)
+
+
+def _plan(bkma, p, **kw):
+    return bkma.AdvectionPlan(p.n0, p.n1, p.n2, dt=p.dt, minX=p.minX, maxX=p.maxX,
+                              minVx=p.minVx, maxVx=p.maxVx, **kw)
+
+
+def _to(cuda, a, dtype):
+    import torch
+    return torch.tensor(a, dtype=dtype, device=cuda)
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("steps", [1, 3])
+def test_plain_fp64_bitexact(bkma, cuda, oracle, case, steps):
+    import torch
+    p = AdvParams(*case)
+    f0 = _init(p)
+    plan = _plan(bkma, p, dtype="f64", impl="plain")
+    d = _to(cuda, f0, torch.float64)
+    plan.step(d, nsteps=steps)
+    got = d.cpu().numpy()
+    want = oracle.adv_step(p, f0.copy(), steps)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("name", ["small", "odd", "default"])
+def test_plain_fp64_matches_reference_vectors(bkma, cuda, golden, name):
+    import torch
+    n0, n1, n2, dt, mnx, mxx, mnv, mxv = golden[f"adv_{name}_params"]
+    p = AdvParams(int(n0), int(n1), int(n2), dt, mnx, mxx, mnv, mxv)
+    plan = _plan(bkma, p, dtype="f64", impl="plain")
+    d = _to(cuda, golden[f"adv_{name}_init"], torch.float64)
+    done = 0
+    for s in sorted(int(k.rsplit("step", 1)[1]) for k in golden if k.startswith(f"adv_{name}_step")):
+        plan.step(d, nsteps=s - done)
+        done = s
+        assert np.array_equal(d.cpu().numpy(), golden[f"adv_{name}_step{s}"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_staged_fp64_close(bkma, cuda, oracle, case):
+    import torch
+    p = AdvParams(*case)
+    f0 = _init(p, 1)
+    plan = _plan(bkma, p, dtype="f64")
+    d = _to(cuda, f0, torch.float64)
+    plan.step(d, nsteps=3)
+    want = oracle.adv_step(p, f0.copy(), 3)
+    err = np.abs(d.cpu().numpy() - want).max() / np.abs(want).max()
+    assert err <= 1e-11, err
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("steps", [1, 10])
+def test_staged_fp32_vs_fp64_oracle(bkma, cuda, oracle, case, steps):
+    import torch
+    p = AdvParams(*case)
+    f0 = _init(p, 2).astype(np.float32).astype(np.float64)
+    plan = _plan(bkma, p, dtype="f32")
+    d = _to(cuda, f0, torch.float32)
+    plan.step(d, nsteps=steps)
+    want = oracle.adv_step(p, f0.copy(), steps)
+    err = np.abs(d.cpu().numpy().astype(np.float64) - want).max() / np.abs(want).max()
+    assert err <= 3e-7 * steps + 2e-7, err
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_departure_offsets_bitexact(bkma, cuda, oracle, case):
+    p = AdvParams(*case)
+    plan = _plan(bkma, p, dtype="f32")
+    offs, shifts = plan.line_table()
+    n_exc = 0
+    for i0 in range(p.n0):
+        vx = oracle.line_velocity(p, i0)
+        left0, d0 = oracle.departure(p, 0, vx)
+        assert offs[i0] == (left0 - 2) % p.n1
+        assert shifts[i0] == d0 - 2.0
+        varying = any(((oracle.departure(p, i1, vx)[0] - 2 - i1) % p.n1) != offs[i0]
+                      for i1 in range(p.n1))
+        n_exc += int(varying)
+    assert plan.info()["exception_lines"] == n_exc
+
+
+def test_exception_lines_use_per_cell_stencils(bkma, cuda, oracle):
+    """A shape whose departure offset changes along n1 (n1 = 1000, dt chosen so
+    v*dt/dx sits on a half-integer boundary): the per-cell table must give the
+    oracle's results."""
+    import torch
+    found = None
+    for dt in (0.0005, 0.0015, 0.0025, 0.00025, 0.0035):
+        p = AdvParams(16, 1000, 2, dt, 0.0, 1.0, -1.0, 1.0)
+        plan = _plan(bkma, p, dtype="f64")
+        if plan.info()["exception_lines"] > 0:
+            found = (p, plan)
+            break
+    if found is None:
+        pytest.skip("no shape with exception lines found")
+    p, plan = found
+    f0 = _init(p, 3)
+    d = _to(cuda, f0, torch.float64)
+    plan.step(d, nsteps=2)
+    want = oracle.adv_step(p, f0.copy(), 2)
+    assert np.abs(d.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+@pytest.mark.parametrize("steps", [1, 2, 3])
+def test_inplace_equals_out_of_place(bkma, cuda, dtype, steps):
+    import torch
+    p = AdvParams(*CASES[4])
+    f0 = _init(p, 4)
+    tdt = torch.float32 if dtype == "f32" else torch.float64
+    plan = _plan(bkma, p, dtype=dtype)
+    a = _to(cuda, f0, tdt)
+    plan.step(a, nsteps=steps)
+    src = _to(cuda, f0, tdt)
+    out = torch.empty_like(src)
+    plan.step(src, out=out, nsteps=steps)
+    assert torch.equal(a, out)
+    if steps == 1:
+        assert torch.equal(src, _to(cuda, f0, tdt))
+
+
+def test_sharded_equals_full(bkma, cuda):
+    import torch
+    p = AdvParams(*CASES[0])
+    f0 = _init(p, 5)
+    full = _plan(bkma, p, dtype="f32")
+    a = _to(cuda, f0, torch.float32)
+    full.step(a, nsteps=4)
+    h = p.n0 // 2
+    parts = []
+    for off, cnt in ((0, h), (h, p.n0 - h)):
+        sp = _plan(bkma, p, dtype="f32", i0_offset=off, i0_count=cnt)
+        b = _to(cuda, f0[off:off + cnt], torch.float32)
+        sp.step(b, nsteps=4)
+        parts.append(b)
+    assert torch.equal(a, torch.cat(parts, 0))
+
+
+def test_velocity_array_and_degree3(bkma, cuda, oracle):
+    import torch
+    p = AdvParams(12, 256, 5, 0.001, 0.0, 1.0, -1.0, 1.0)
+    vel = np.random.default_rng(6).uniform(-2, 2, p.n0)
+    f0 = _init(p, 6)
+    for degree, weights in ((5, "reference"), (3, "lagrange"), (5, "lagrange")):
+        plan = _plan(bkma, p, dtype="f64", velocity=vel, degree=degree, weights=weights)
+        d = _to(cuda, f0, torch.float64)
+        plan.step(d, nsteps=2)
+        want = oracle.adv_step(p, f0.copy(), 2, velocity=vel, degree=degree,
+                               ref_weights=(weights == "reference"))
+        assert np.abs(d.cpu().numpy() - want).max() <= 1e-11, (degree, weights)
+
+
+def test_analytic_validation_on_device(bkma, cuda, oracle):
+    """The reference's unit tests: fill sin(4 pi x), exact 0 at maxIter = 0,
+    mean L1 < 1e-6 after each of 10 steps (validation_unittests.cpp:11-94)."""
+    import torch
+    p = AdvParams(16, 512, 4, 1e-4, 0.0, 1.0, 0.0, 1.0)
+    plan = _plan(bkma, p, dtype="f64")
+    d = torch.empty(p.n0, p.n1, p.n2, dtype=torch.float64, device=cuda)
+    plan.fill(d, mode=0)
+    hi, lo = plan.validate(d, 0)
+    assert hi == 0.0 and lo == 0.0
+    for it in range(1, 11):
+        plan.step(d)
+        hi, lo = plan.validate(d, it)
+        assert hi < 1e-6
+    # the device analytic check agrees with the oracle's
+    ref = oracle.fill_adv(p)
+    oracle.adv_step(p, ref, 10)
+    assert abs(oracle.validate_adv(p, ref, 10) - hi) < 1e-9
+
+
+def test_run_host_matches_device_path(bkma, cuda):
+    import torch
+    p = AdvParams(*CASES[3])
+    f0 = _init(p, 7).astype(np.float32)
+    plan = _plan(bkma, p, dtype="f32")
+    d = _to(cuda, f0, torch.float32)
+    plan.step(d, nsteps=3)
+    h = f0.copy()
+    plan.run_host(h, nsteps=3)
+    assert np.array_equal(h, d.cpu().numpy())
+
+
+def test_autotune_is_result_neutral(bkma, cuda):
+    import torch
+    p = AdvParams(6, 512, 48, 0.001, 0.0, 1.0, -1.0, 1.0)
+    f0 = _init(p, 8)
+    plan = _plan(bkma, p, dtype="f32")
+    a = _to(cuda, f0, torch.float32)
+    plan.step(a, nsteps=2)
+    scratch = torch.empty_like(a)
+    info = plan.autotune(scratch)
+    assert info["autotuned"] == 1
+    b = _to(cuda, f0, torch.float32)
+    plan.step(b, nsteps=2)
+    assert torch.equal(a, b)
+
+
+def test_error_norms(bkma, cuda):
+    import torch
+    p = AdvParams(4, 64, 8, 0.001, 0.0, 1.0, -1.0, 1.0)
+    plan = _plan(bkma, p, dtype="f32")
+    rng = np.random.default_rng(9)
+    ref = rng.standard_normal(plan.shape)
+    x = (ref + 1e-3 * rng.standard_normal(plan.shape)).astype(np.float32)
+    n = plan.error_norms(_to(cuda, x, torch.float32), _to(cuda, ref, torch.float64))
+    d = x.astype(np.float64) - ref
+    assert abs(n["max_abs"] - np.abs(d).max()) < 1e-12
+    assert abs(n["max_ref"] - np.abs(ref).max()) < 1e-12
+    assert abs(n["l2_rel"] - np.sqrt((d ** 2).sum() / (ref ** 2).sum())) < 1e-9
+
+
+def test_zero_steps_is_identity(bkma, cuda):
+    import torch
+    p = AdvParams(*CASES[0])
+    plan = _plan(bkma, p, dtype="f32")
+    a = _to(cuda, _init(p), torch.float32)
+    b = a.clone()
+    plan.step(a, nsteps=0)
+    assert torch.equal(a, b)
