@@ -266,6 +266,17 @@ void stencil_weights(int weights_kind, int npts, double d, double *w) {
     }
 }
 
+// Row of tap 0 for point i1, as an offset from i1 modulo n1. The tap index
+// is formed like the reference's (n1 + ipos1 + k) % n1 in size_t arithmetic
+// (AdvectionSolver.hpp:94), so even a negative foot (a displacement beyond a
+// full period) selects the same rows.
+int64_t tap0_offset(int left, int NT, int64_t i1, int64_t n1) {
+    const uint64_t un1 = (uint64_t)n1;
+    const int64_t first = (int64_t)left - (NT / 2 - 1);
+    const uint64_t id0 = (un1 + (uint64_t)first) % un1;
+    return (int64_t)((id0 + un1 - (uint64_t)i1 % un1) % un1);
+}
+
 struct TuneKey {
     int dtype, npts, impl;
     int64_t lines, n1, n2;
@@ -334,8 +345,7 @@ bkma_status upload_tables(AdvPlanImpl &p) {
             for (int64_t i1 = 0; i1 < n1; ++i1) {
                 double d;
                 const int left = adv_departure(p.phys, (int)i1, p.vx[(size_t)l], &d);
-                int64_t b = ((int64_t)left - (NT / 2 - 1) - i1) % n1;
-                if (b < 0) b += n1;
+                const int64_t b = tap0_offset(left, NT, i1, n1);
                 double wd[16];
                 stencil_weights(p.desc.weights, NT, d, wd);
                 AdvExcCell<T> &e = cells[(size_t)(slot * n1 + i1)];
@@ -471,8 +481,7 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
         p.vx[(size_t)l] = v;
         double d0;
         const int left0 = adv_departure(p.phys, 0, v, &d0);
-        int64_t b0 = ((int64_t)left0 - (NT / 2 - 1)) % n1;
-        if (b0 < 0) b0 += n1;
+        const int64_t b0 = tap0_offset(left0, NT, 0, n1);
         p.base[(size_t)l] = (int32_t)b0;
         p.shift[(size_t)l] = d0 - 2.0;
         stencil_weights(d.weights, NT, d0, &p.w64[(size_t)(l * NT)]);
@@ -480,9 +489,7 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
         for (int64_t i1 = 1; i1 < n1; ++i1) {
             double di;
             const int left = adv_departure(p.phys, (int)i1, v, &di);
-            int64_t b = ((int64_t)left - (NT / 2 - 1) - i1) % n1;
-            if (b < 0) b += n1;
-            if (b != b0) {
+            if (tap0_offset(left, NT, i1, n1) != b0) {
                 p.exc_index[(size_t)l] = (int32_t)p.n_exc++;
                 break;
             }
@@ -578,6 +585,8 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
     if (d.impl == BKMA_ADV_PLAIN) {
         BKMA_CHECK_ARG(d.dtype == BKMA_F64 && d.weights == BKMA_W_REFERENCE,
                        "the plain form is the reference's FP64 degree-5 operator");
+    } else {
+        BKMA_CHECK_ARG(d.n1 >= d.degree + 1, "the staged kernel needs n1 >= degree + 1");
     }
     BKMA_CHECK_ARG(d.maxX > d.minX, "maxX must exceed minX");
     BKMA_CHECK_ARG(std::isfinite(d.dt), "dt must be finite");
