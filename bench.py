@@ -29,7 +29,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "parallel-advection_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-N0, N1, N2 = 2048, 1024, 512
+N0, N1, N2 = 2048, 1024, 512  # --n0 shrinks N0 for profiling captures only
 DT, MINX, MAXX = 0.001, 0.0, 1.0
 NOISE, SEED = 0.01, 12345
 CFG_STEPS = 50
@@ -177,7 +177,7 @@ def cpu_baseline_sample(cores: int):
     t0 = time.perf_counter()
     orc.adv_step(p, f, 1, velocity=vel[:S], nthreads=cores)
     one = time.perf_counter() - t0
-    S = int(max(1, min(256, S * 3.0 / max(one, 1e-3))))
+    S = int(max(1, min(N0, S * 3.0 / max(one, 1e-3))))
     f = np.ascontiguousarray(np.sin(2 * np.pi * x)[None, :, None] +
                              NOISE * rng.uniform(-1, 1, (S, N1, N2)))
     steps = 4
@@ -217,8 +217,9 @@ def run_gpu(args):
     cells = N0 * N1 * N2
     f = torch.empty((N0, N1, N2), dtype=torch.float32, device=dev)
     plan.fill(f, mode=1, amp=NOISE, seed=SEED)
-    plan.autotune(f)
-    plan.fill(f, mode=1, amp=NOISE, seed=SEED)
+    if not args.no_autotune:
+        plan.autotune(f)
+        plan.fill(f, mode=1, amp=NOISE, seed=SEED)
     st = torch.cuda.current_stream()
     for _ in range(args.warmup):
         plan.step(f)
@@ -281,6 +282,7 @@ def run_gpu(args):
         result.update(extras(plan, bkma_gb300, dev, vel, kw, cells))
         result["e2e"] = e2e(plan, dev, cells)
         result["cpu_baseline"] = cpu_baseline_sample(os.cpu_count() or 1)
+        result["conv1d"] = conv_block(bkma_gb300, dev)
     if rank == 0:
         print(json.dumps(result))
     if dist is not None:
@@ -342,6 +344,74 @@ def extras(plan, bkma_gb300, dev, vel, kw, cells):
     return out
 
 
+def conv_block(bkma_gb300, dev):
+    """In-place conv1d, BF16 with FP32 accumulation (tcgen05): B=256,
+    Cin=Cout=128, L=8192, K=7, inputs and weights U[-1,1]/sqrt(Cin*K), bias 0.
+    TFLOP/s = 2*B*Cout*Cin*K*(L-K+1) / kernel time; error against the plain
+    FP64 kernel (bit-identical to the oracle) on the same BF16-rounded inputs,
+    which is also the plain-FP64-form speed baseline."""
+    import torch
+    B, C, L, K = 256, 128, 8192, 7
+    flops = 2.0 * B * C * C * K * (L - K + 1)
+    out = {"workload": f"in-place conv1d BF16 B={B} Cin=Cout={C} L={L} K={K}",
+           "metric": "conv1d TFLOP/s", "unit": "TFLOP/s"}
+    try:
+        g = torch.Generator(device=dev).manual_seed(SEED)
+        s = 1.0 / (C * K) ** 0.5
+        x0 = ((torch.rand((B, C, L), generator=g, device=dev) * 2 - 1) * s).to(torch.bfloat16)
+        w = ((torch.rand((C, C, K), generator=g, device=dev) * 2 - 1) * s).to(torch.bfloat16)
+        bias = torch.zeros(C, dtype=torch.bfloat16, device=dev)
+        plan = bkma_gb300.Conv1dPlan(B, C, C, L, K, dtype="bf16", impl="tensor")
+        x = x0.clone()
+        plan.run(x, w, bias)
+        plan.status()
+        st = torch.cuda.current_stream()
+        reps = 20
+        bufs = [x0.clone() for _ in range(2)]
+        times = []
+        for r in range(reps + 3):
+            xb = bufs[r % 2]
+            xb.copy_(x0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            plan.run(xb, w, bias)
+            b.record(st)
+            torch.cuda.synchronize()
+            if r >= 3:
+                times.append(a.elapsed_time(b))
+        plan.status()
+        ms = statistics.median(times)
+        _, bf16_peak, kind = peaks()
+        tflops = flops / (ms / 1e3) / 1e12
+        out.update({"value": tflops, "ms": ms, "launches_per_call": 2,
+                    "roofline": {"bound": "tensor", "achieved": tflops, "peak": bf16_peak,
+                                 "unit": "TFLOP/s", "frac": tflops / bf16_peak,
+                                 "peak_kind": f"{kind} cuBLAS bf16 burst",
+                                 "algorithmic_flops": flops,
+                                 "note": "time includes the halo pre-pass kernel"}})
+        # FP64 plain form on the same BF16 inputs: error reference and speed baseline
+        p64 = bkma_gb300.Conv1dPlan(B, C, C, L, K, dtype="f64", impl="plain")
+        x64 = x0.double()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        p64.run(x64, w.double(), bias.double())
+        b.record(st)
+        torch.cuda.synchronize()
+        ms64 = a.elapsed_time(b)
+        got = x[:, :, :L - K + 1].double()
+        ref = x64[:, :, :L - K + 1]
+        d = (got - ref).abs()
+        out["error_vs_fp64"] = {"max_rel": float(d.max() / ref.abs().max()),
+                                "l2_rel": float((d.pow(2).sum() / ref.pow(2).sum()).sqrt())}
+        out["plain_fp64"] = {"tflops": flops / (ms64 / 1e3) / 1e12, "ms": ms64,
+                             "speedup": ms64 / ms}
+        del x64, ref, got, d
+    except Exception as e:  # reported, not hidden
+        out["error"] = repr(e)
+    torch.cuda.empty_cache()
+    return out
+
+
 def e2e(plan, dev, cells):
     """The same metric through the C ABI with a HOST field: every e2e step
     copies the field host->device, runs the 50 time steps and copies it back
@@ -375,8 +445,13 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--quick", action="store_true", help="skip error/e2e/cpu blocks")
+    ap.add_argument("--quick", action="store_true", help="skip error/e2e/cpu/conv blocks")
+    ap.add_argument("--n0", type=int, default=None, help="smaller field for profiling captures")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
+    if args.n0:
+        global N0
+        N0 = args.n0
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

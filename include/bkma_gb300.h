@@ -196,6 +196,10 @@ bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **p
 bkma_status bkma_conv_plan_scratch_bytes(const bkma_conv_plan *plan, int64_t *bytes);
 bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const void *weight,
                           const void *bias, void *stream);
+/* Synchronizes `stream` and returns the device status of the tensor-core
+ * kernel's bounded waits since the last query (BKMA_OK or BKMA_ERR_TIMEOUT),
+ * then clears it. */
+bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream);
 bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan);
 
 #ifdef __cplusplus

@@ -183,6 +183,10 @@ class Conv1dPlan:
                                    _stream(stream)))
         return data if out is None else out
 
+    def status(self, stream=None):
+        """Raise if a bounded device wait of the tensor kernel timed out."""
+        check(load().bkma_conv_plan_status(self._h, _stream(stream)))
+
     def close(self):
         if getattr(self, "_h", None):
             load().bkma_conv_plan_destroy(self._h)

@@ -84,6 +84,7 @@ SIGNATURES = {
     "bkma_conv_plan_create": (_st, [C.POINTER(ConvDesc), C.POINTER(_vp)]),
     "bkma_conv_plan_scratch_bytes": (_st, [_vp, _i64p]),
     "bkma_conv_run": (_st, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "bkma_conv_plan_status": (_st, [_vp, _vp]),
     "bkma_conv_plan_destroy": (_st, [_vp]),
 }
 

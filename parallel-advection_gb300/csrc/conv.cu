@@ -312,6 +312,18 @@ bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const voi
     return run_torch_plain<float>(p, data, out, weight, bias, st);
 }
 
+bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream) {
+    BKMA_CHECK_ARG(plan, "null argument");
+    ConvPlanImpl &p = plan->impl;
+    BKMA_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    if (!p.d_status) return BKMA_OK;
+    int st = 0;
+    BKMA_CUDA_TRY(cudaMemcpy(&st, p.d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    BKMA_CUDA_TRY(cudaMemset(p.d_status, 0, sizeof(int)));
+    if (st != 0) return fail((bkma_status)st, "tensor-core conv1d: a bounded device wait timed out");
+    return BKMA_OK;
+}
+
 bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan) {
     delete plan;
     return BKMA_OK;

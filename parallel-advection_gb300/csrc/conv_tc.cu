@@ -464,6 +464,9 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
         bkma_status s = conv_halo_prepass(p, data, st);
         if (s != BKMA_OK) return s;
     }
+    const auto misaligned = [](const void *q) { return q && ((uintptr_t)q % 16) != 0; };
+    if (misaligned(data) || misaligned(out) || misaligned(w))
+        return fail(BKMA_ERR_INVALID_ARG, "tensor path: data, out and weight must be 16-byte aligned");
     tc::Args a;
     a.x = (const __nv_bfloat16 *)data;
     a.out = (__nv_bfloat16 *)(inplace ? data : out);
@@ -488,7 +491,9 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
     if (smem > 220 * 1024) return fail(BKMA_ERR_UNSUPPORTED, "tensor path: stage too large for shared memory");
     BKMA_CUDA_TRY(cudaFuncSetAttribute(tc::conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
-    tc::conv_tc_kernel<<<p.grid, tc::THREADS, smem, st>>>(a);
+    const int64_t items = (int64_t)a.B * a.ntiles;
+    const int grid = (int)std::min<int64_t>(p.grid, items);
+    tc::conv_tc_kernel<<<grid, tc::THREADS, smem, st>>>(a);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
 }

@@ -1,0 +1,118 @@
+"""BF16 tensor-core conv1d (tcgen05, FP32 accumulate in TMEM) against the
+FP64 oracle evaluated on the same BF16-rounded inputs.
+
+Tolerance: max |out - ref| <= 1e-2 * max |ref| (the BF16 output rounding alone
+is 2^-9 relative); the tests also bound the mean error far tighter, at
+3e-3 * max|ref|, to catch layout mistakes that only touch some elements.
+Shapes run smallest first.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [
+    # B, C, L, K
+    (1, 16, 256, 3),
+    (1, 16, 136, 1),
+    (2, 32, 512, 7),
+    (3, 64, 1000, 5),
+    (2, 128, 1024, 7),
+    (1, 128, 8192, 7),
+]
+
+
+def _case(shape, seed):
+    B, C, L, K = shape
+    rng = np.random.default_rng(seed)
+    s = 1.0 / np.sqrt(C * K)
+    x = rng.uniform(-1, 1, (B, C, L))
+    w = rng.uniform(-1, 1, (C, C, K)) * s
+    b = rng.uniform(-1, 1, C) * s
+    return x, w, b
+
+
+def _bf(cuda, a):
+    import torch
+    return torch.tensor(a, dtype=torch.float64, device=cuda).to(torch.bfloat16)
+
+
+def _check(got, want):
+    err = np.abs(got - want)
+    scale = np.abs(want).max()
+    assert err.max() <= 1e-2 * scale, (err.max(), scale)
+    assert err.mean() <= 3e-3 * scale, (err.mean(), scale)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_tensor_conv_inplace(bkma, cuda, oracle, shape):
+    B, C, L, K = shape
+    x, w, b = _case(shape, 100 + L)
+    xd, wd, bd = _bf(cuda, x), _bf(cuda, w), _bf(cuda, b)
+    want = oracle.conv_torch(xd.double().cpu().numpy(), wd.double().cpu().numpy(),
+                             bd.double().cpu().numpy())
+    orig = xd.clone()
+    plan = bkma.Conv1dPlan(B, C, C, L, K, dtype="bf16", impl="tensor")
+    plan.run(xd, wd, bd)
+    plan.status()
+    got = xd.double().cpu().numpy()
+    _check(got[:, :, :L - K + 1], want)
+    # the tail keeps its input values
+    assert np.array_equal(got[:, :, L - K + 1:], orig.double().cpu().numpy()[:, :, L - K + 1:])
+
+
+@pytest.mark.parametrize("shape", [(2, 32, 512, 7), (2, 128, 1024, 7)])
+def test_tensor_conv_out_of_place_and_bias_none(bkma, cuda, oracle, shape):
+    import torch
+    B, C, L, K = shape
+    x, w, _ = _case(shape, 7)
+    xd, wd = _bf(cuda, x), _bf(cuda, w)
+    want = oracle.conv_torch(xd.double().cpu().numpy(), wd.double().cpu().numpy(), None)
+    plan = bkma.Conv1dPlan(B, C, C, L, K, dtype="bf16", impl="tensor", inplace=False)
+    out = torch.empty(B, C, L - K + 1, dtype=torch.bfloat16, device=cuda)
+    before = xd.clone()
+    plan.run(xd, wd, None, out=out)
+    plan.status()
+    _check(out.double().cpu().numpy(), want)
+    assert torch.equal(xd, before)
+
+
+def test_tensor_conv_fewer_out_channels(bkma, cuda, oracle):
+    import torch
+    B, cin, cout, L, K = 2, 64, 48, 512, 3
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, (B, cin, L))
+    w = rng.uniform(-1, 1, (cout, cin, K)) / np.sqrt(cin * K)
+    b = rng.uniform(-1, 1, cout)
+    xd, wd, bd = _bf(cuda, x), _bf(cuda, w), _bf(cuda, b)
+    want = oracle.conv_torch(xd.double().cpu().numpy(), wd.double().cpu().numpy(),
+                             bd.double().cpu().numpy())
+    plan = bkma.Conv1dPlan(B, cin, cout, L, K, dtype="bf16", impl="tensor", inplace=False)
+    out = torch.empty(B, cout, L - K + 1, dtype=torch.bfloat16, device=cuda)
+    plan.run(xd, wd, bd, out=out)
+    plan.status()
+    _check(out.double().cpu().numpy(), want)
+
+
+def test_tensor_conv_repeatable(bkma, cuda):
+    """Two runs on the same input give identical bits (no race in the
+    in-place halo handling)."""
+    B, C, L, K = 4, 128, 4096, 7
+    x, w, b = _case((B, C, L, K), 9)
+    plan = bkma.Conv1dPlan(B, C, C, L, K, dtype="bf16", impl="tensor")
+    outs = []
+    for _ in range(2):
+        xd = _bf(cuda, x)
+        plan.run(xd, _bf(cuda, w), _bf(cuda, b))
+        plan.status()
+        outs.append(xd)
+    import torch
+    assert torch.equal(outs[0], outs[1])
+
+
+def test_tensor_conv_rejects_unsupported(bkma, cuda):
+    with pytest.raises(bkma.BkmaError) as e:
+        bkma.Conv1dPlan(2, 24, 24, 256, 3, dtype="bf16", impl="tensor")
+    assert e.value.status == 2
+    with pytest.raises(bkma.BkmaError):
+        bkma.Conv1dPlan(2, 128, 128, 256, 9, dtype="bf16", impl="tensor")
