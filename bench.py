@@ -344,14 +344,14 @@ def extras(plan, bkma_gb300, dev, vel, kw, cells):
     return out
 
 
-def conv_block(bkma_gb300, dev):
+def conv_block(bkma_gb300, dev, batch: int = 256, with_fp64: bool = True):
     """In-place conv1d, BF16 with FP32 accumulation (tcgen05): B=256,
     Cin=Cout=128, L=8192, K=7, inputs and weights U[-1,1]/sqrt(Cin*K), bias 0.
     TFLOP/s = 2*B*Cout*Cin*K*(L-K+1) / kernel time; error against the plain
     FP64 kernel (bit-identical to the oracle) on the same BF16-rounded inputs,
     which is also the plain-FP64-form speed baseline."""
     import torch
-    B, C, L, K = 256, 128, 8192, 7
+    B, C, L, K = batch, 128, 8192, 7
     flops = 2.0 * B * C * C * K * (L - K + 1)
     out = {"workload": f"in-place conv1d BF16 B={B} Cin=Cout={C} L={L} K={K}",
            "metric": "conv1d TFLOP/s", "unit": "TFLOP/s"}
@@ -389,6 +389,8 @@ def conv_block(bkma_gb300, dev):
                                  "peak_kind": f"{kind} cuBLAS bf16 burst",
                                  "algorithmic_flops": flops,
                                  "note": "time includes the halo pre-pass kernel"}})
+        if not with_fp64:
+            raise StopIteration
         # FP64 plain form on the same BF16 inputs: error reference and speed baseline
         p64 = bkma_gb300.Conv1dPlan(B, C, C, L, K, dtype="f64", impl="plain")
         x64 = x0.double()
@@ -406,6 +408,8 @@ def conv_block(bkma_gb300, dev):
         out["plain_fp64"] = {"tflops": flops / (ms64 / 1e3) / 1e12, "ms": ms64,
                              "speedup": ms64 / ms}
         del x64, ref, got, d
+    except StopIteration:
+        pass
     except Exception as e:  # reported, not hidden
         out["error"] = repr(e)
     torch.cuda.empty_cache()
@@ -448,12 +452,22 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip error/e2e/cpu/conv blocks")
     ap.add_argument("--n0", type=int, default=None, help="smaller field for profiling captures")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--workload", default="advection", choices=["advection", "conv"],
+                    help="conv: only the conv1d block, as its own JSON line")
+    ap.add_argument("--conv-batch", type=int, default=256, help="smaller batch for captures")
     args = ap.parse_args()
     if args.n0:
         global N0
         N0 = args.n0
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "conv" and args.impl != "reference":
+        import torch
+        import bkma_gb300
+        r = conv_block(bkma_gb300, torch.device("cuda", 0), batch=args.conv_batch,
+                       with_fp64=not args.quick)
+        print(json.dumps(r))
+        return 0 if "error" not in r else 1
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

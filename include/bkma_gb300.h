@@ -91,6 +91,8 @@ typedef struct bkma_adv_plan_info {
     int32_t npts;              /* stencil points (degree + 1) */
     int32_t autotuned;         /* 1 once bkma_adv_plan_autotune picked the tile */
     int64_t tiles;             /* CTAs per step */
+    int32_t path;              /* 0: cp.async staging, 1: TMA (cp.async.bulk.tensor) staging */
+    int32_t reserved;
 } bkma_adv_plan_info;
 
 int32_t bkma_abi_version(void);
@@ -110,12 +112,20 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
 /* Times the candidate tiles on `scratch_field` (a device field of the plan's
  * shape, contents are overwritten) and keeps the fastest; cached per shape. */
 bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, void *stream);
+/* Explicit tile choice (the reference's pref_wg_size / seq_size knobs):
+ * W columns x R slabs per CTA, `threads` per CTA (128, 256 or 512), staging
+ * path 0 (cp.async) or 1 (TMA; FP32, n2 % 4 == 0, W in {8,16,32}, R == 1). */
+bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
+                                   int32_t path);
 /* BKMA_W_TABLE: per-line weights, i0_count x (degree+1) floats (host or
  * device pointer), applied on the plan's own departure offsets. */
 bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device);
 /* Per-line departure offsets (tap-0 node minus i1, modulo n1) and FP64
  * fractional shifts d - 2 in [0,1) (host arrays of i0_count). */
 bkma_status bkma_adv_plan_line_table(const bkma_adv_plan *plan, int32_t *offsets, double *shifts);
+/* Synchronizes `stream`, returns the device status of the kernels' bounded
+ * waits since the last query (BKMA_OK or BKMA_ERR_TIMEOUT) and clears it. */
+bkma_status bkma_adv_plan_status(bkma_adv_plan *plan, void *stream);
 bkma_status bkma_adv_plan_destroy(bkma_adv_plan *plan);
 
 /* bkma_run for the advection solver: nsteps time steps of the device field

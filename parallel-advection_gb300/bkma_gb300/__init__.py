@@ -91,6 +91,14 @@ class AdvectionPlan:
         check(load().bkma_adv_run_host(self._h, host.ctypes.data, nsteps, _stream(stream)))
         return host
 
+    def set_tile(self, W: int, R: int = 1, threads: int = 256, path: int = 0):
+        check(load().bkma_adv_plan_set_tile(self._h, W, R, threads, path))
+        return self.info()
+
+    def status(self, stream=None):
+        """Raise if a bounded device wait timed out since the last query."""
+        check(load().bkma_adv_plan_status(self._h, _stream(stream)))
+
     def autotune(self, field, stream=None):
         check(load().bkma_adv_plan_autotune(self._h, _ptr(field), _stream(stream)))
         return self.info()

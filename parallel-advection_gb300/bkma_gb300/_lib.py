@@ -37,7 +37,7 @@ class AdvPlanInfo(C.Structure):
     _fields_ = [("lines", C.c_int64), ("exception_lines", C.c_int64),
                 ("tile_cols", C.c_int32), ("tile_slabs", C.c_int32), ("threads", C.c_int32),
                 ("smem_bytes", C.c_int32), ("npts", C.c_int32), ("autotuned", C.c_int32),
-                ("tiles", C.c_int64)]
+                ("tiles", C.c_int64), ("path", C.c_int32), ("reserved", C.c_int32)]
 
 
 class AdvField(C.Structure):
@@ -69,8 +69,10 @@ SIGNATURES = {
     "bkma_adv_plan_create": (_st, [C.POINTER(AdvDesc), C.POINTER(_vp)]),
     "bkma_adv_plan_info_get": (_st, [_vp, C.POINTER(AdvPlanInfo)]),
     "bkma_adv_plan_autotune": (_st, [_vp, _vp, _vp]),
+    "bkma_adv_plan_set_tile": (_st, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "bkma_adv_plan_set_weights": (_st, [_vp, _vp, C.c_int32]),
     "bkma_adv_plan_line_table": (_st, [_vp, _i32p, _dp]),
+    "bkma_adv_plan_status": (_st, [_vp, _vp]),
     "bkma_adv_plan_destroy": (_st, [_vp]),
     "bkma_adv_step": (_st, [_vp, _vp, _vp, C.c_int32, _vp]),
     "bkma_adv_run_host": (_st, [_vp, _vp, C.c_int32, _vp]),

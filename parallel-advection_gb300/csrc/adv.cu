@@ -286,7 +286,7 @@ struct TuneKey {
     }
 };
 struct TuneVal {
-    int W, R, threads;
+    int W, R, threads, path;
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneVal> g_tune_cache;
@@ -318,6 +318,11 @@ void default_tile(AdvPlanImpl &p) {
     while (p.R > 1 && p.smem_bytes(p.W, p.R) > kMaxSmem) p.R /= 2;
     while (p.W > 1 && p.smem_bytes(p.W, p.R) > kMaxSmem) p.W /= 2;
     p.threads = 256;
+    // TMA staging for FP32 column tiles; launch_once falls back per call when
+    // a field pointer is not 16-byte aligned.
+    const void *aligned_probe = reinterpret_cast<const void *>(uintptr_t(256));
+    p.path = (p.R == 1 && adv_tma_eligible(p, aligned_probe, p.W) &&
+              adv_tma_smem(p, p.W) <= kMaxSmem) ? 1 : 0;
 }
 
 template <typename T>
@@ -431,8 +436,10 @@ cudaError_t launch_plain(const AdvPlanImpl &p, const double *src, double *dst, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_once(const AdvPlanImpl &p, const void *src, void *dst, int W, int R,
-                        int threads, cudaStream_t st) {
+cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R, int threads,
+                        int path, cudaStream_t st) {
+    if (path == 1 && R == 1 && adv_tma_eligible(p, src, W))
+        return adv_tma_launch(p, src, dst, W, threads, st);
     if (p.desc.impl == BKMA_ADV_PLAIN)
         return launch_plain(p, (const double *)src, (double *)dst, W, R, threads, st);
     if (p.desc.dtype == BKMA_F32) return launch_staged_npts<float>(p, src, dst, W, R, threads, st);
@@ -447,7 +454,7 @@ bkma_status adv_launch(AdvPlanImpl &p, void *data, void *out, int nsteps, cudaSt
     // an even number first steps `data` in place, then alternates.
     int t0 = 0;
     if (!inplace && nsteps > 0 && nsteps % 2 == 0) {
-        cudaError_t e = launch_once(p, data, data, p.W, p.R, p.threads, st);
+        cudaError_t e = launch_once(p, data, data, p.W, p.R, p.threads, p.path, st);
         if (e != cudaSuccess) return cuda_fail(e, "adv kernel launch");
         t0 = 1;
     }
@@ -458,7 +465,7 @@ bkma_status adv_launch(AdvPlanImpl &p, void *data, void *out, int nsteps, cudaSt
             src = to_out ? data : out;
             dst = to_out ? out : data;
         }
-        cudaError_t e = launch_once(p, src, dst, p.W, p.R, p.threads, st);
+        cudaError_t e = launch_once(p, src, dst, p.W, p.R, p.threads, p.path, st);
         if (e != cudaSuccess) return cuda_fail(e, "adv kernel launch");
     }
     return BKMA_OK;
@@ -509,6 +516,7 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
             p.W = it->second.W;
             p.R = it->second.R;
             p.threads = it->second.threads;
+            p.path = it->second.path;
             p.autotuned = true;
             return BKMA_OK;
         }
@@ -519,26 +527,31 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     if (n2 >= 8) {
         for (int W : {8, 16, 32, 64})
             if (W <= n2 || W == 8)
-                for (int t : ths) cands.push_back({W, 1, t});
+                for (int t : ths) {
+                    cands.push_back({W, 1, t, 0});
+                    if (adv_tma_eligible(p, field, W)) cands.push_back({W, 1, t, 1});
+                }
     }
     for (int R : {1, 2, 4, 8, 16})
         if (n2 < 32 && R <= p.lines)
-            for (int t : ths) cands.push_back({(int)n2, R, t});
+            for (int t : ths) cands.push_back({(int)n2, R, t, 0});
     cudaEvent_t e0, e1;
     BKMA_CUDA_TRY(cudaEventCreate(&e0));
     BKMA_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
-    TuneVal bestv{p.W, p.R, p.threads};
+    TuneVal bestv{p.W, p.R, p.threads, p.path};
     for (const TuneVal &c : cands) {
-        if (p.smem_bytes(c.W, c.R) > kMaxSmem) continue;
-        cudaError_t err = launch_once(p, field, field, c.W, c.R, c.threads, st);  // warm-up
+        const size_t need = c.path == 1 ? adv_tma_smem(p, c.W) : p.smem_bytes(c.W, c.R);
+        if (need > kMaxSmem) continue;
+        cudaError_t err = launch_once(p, field, field, c.W, c.R, c.threads, c.path, st);  // warm-up
         if (err != cudaSuccess) {
             cudaGetLastError();
             continue;
         }
         const int reps = 3;
         cudaEventRecord(e0, st);
-        for (int i = 0; i < reps; ++i) launch_once(p, field, field, c.W, c.R, c.threads, st);
+        for (int i = 0; i < reps; ++i)
+            launch_once(p, field, field, c.W, c.R, c.threads, c.path, st);
         cudaEventRecord(e1, st);
         BKMA_CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;
@@ -553,6 +566,7 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     p.W = bestv.W;
     p.R = bestv.R;
     p.threads = bestv.threads;
+    p.path = bestv.path;
     p.autotuned = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_cache[key] = bestv;
@@ -626,6 +640,14 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
         delete pl;
         return s;
     }
+    {
+        cudaError_t e = cudaMalloc(&p.d_status, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(p.d_status, 0, sizeof(int));
+        if (e != cudaSuccess) {
+            delete pl;
+            return cuda_fail(e, "plan status word");
+        }
+    }
     default_tile(p);
     if (p.smem_bytes(p.W, p.R) > kMaxSmem) {
         delete pl;
@@ -643,16 +665,50 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
     info->tile_cols = (int32_t)std::min<int64_t>(p.W, p.desc.n2);
     info->tile_slabs = p.R;
     info->threads = p.threads;
-    info->smem_bytes = (int32_t)p.smem_bytes(p.W, p.R);
+    info->smem_bytes = (int32_t)(p.path == 1 ? adv_tma_smem(p, p.W) : p.smem_bytes(p.W, p.R));
     info->npts = p.npts;
     info->autotuned = p.autotuned ? 1 : 0;
     info->tiles = p.tiles(p.W, p.R);
+    info->path = p.path;
+    return BKMA_OK;
+}
+
+bkma_status bkma_adv_plan_status(bkma_adv_plan *plan, void *stream) {
+    BKMA_CHECK_ARG(plan, "null argument");
+    AdvPlanImpl &p = plan->impl;
+    BKMA_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    int st = 0;
+    BKMA_CUDA_TRY(cudaMemcpy(&st, p.d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    BKMA_CUDA_TRY(cudaMemset(p.d_status, 0, sizeof(int)));
+    if (st != 0) return fail((bkma_status)st, "advection: a bounded device wait timed out");
     return BKMA_OK;
 }
 
 bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *field, void *stream) {
     BKMA_CHECK_ARG(plan && field, "null argument");
     return adv_autotune(plan->impl, field, (cudaStream_t)stream);
+}
+
+bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
+                                   int32_t path) {
+    BKMA_CHECK_ARG(plan, "null argument");
+    AdvPlanImpl &p = plan->impl;
+    BKMA_CHECK_ARG(W >= 1 && W <= 64 && R >= 1 && R <= 64, "W must be in [1,64], R in [1,64]");
+    BKMA_CHECK_ARG(threads == 128 || threads == 256 || threads == 512, "threads must be 128, 256 or 512");
+    BKMA_CHECK_ARG(path == 0 || path == 1, "path must be 0 or 1");
+    BKMA_CHECK_ARG(R == 1 || W >= p.desc.n2, "R > 1 needs whole-row tiles (W >= n2)");
+    if (path == 1) {
+        const void *probe = reinterpret_cast<const void *>(uintptr_t(256));
+        BKMA_CHECK_ARG(R == 1 && adv_tma_eligible(p, probe, W), "TMA staging not available for this tile");
+        BKMA_CHECK_ARG(adv_tma_smem(p, W) <= kMaxSmem, "tile does not fit shared memory");
+    } else {
+        BKMA_CHECK_ARG(p.smem_bytes(W, R) <= kMaxSmem, "tile does not fit shared memory");
+    }
+    p.W = W;
+    p.R = R;
+    p.threads = threads;
+    p.path = path;
+    return BKMA_OK;
 }
 
 bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device) {

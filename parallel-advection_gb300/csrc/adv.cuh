@@ -29,6 +29,18 @@ struct AdvStagedArgs {
     const AdvExcCell<T> *exc;  // [exception lines][n1]
 };
 
+struct AdvTmaArgs {
+    float *dst;
+    int64_t n1, n2;
+    int64_t ncb;               // column blocks per slab
+    int box_rows, nbox;        // TMA boxes of box_rows rows cover n1
+    const int32_t *base;       // [lines]
+    const float *w;            // [lines][NT]
+    const int32_t *exc_index;  // [lines]
+    const AdvExcCell<float> *exc;
+    int *status;               // device status word (BKMA_ERR_TIMEOUT on a stuck copy)
+};
+
 struct AdvPlainArgs {
     const double *src;
     double *dst;

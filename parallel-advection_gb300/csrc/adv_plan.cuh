@@ -1,5 +1,6 @@
 // Host-side advection plan (shared by adv.cu and adv_util.cu).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,9 +30,16 @@ struct AdvPlanImpl {
     int32_t *d_exc_index = nullptr;
     void *d_exc = nullptr;
     double *d_vx = nullptr;
-    // launch shape
-    int W = 16, R = 1, threads = 256;
+    // launch shape: path 0 = cp.async staging (any shape), 1 = TMA staging
+    int W = 16, R = 1, threads = 256, path = 0;
     bool autotuned = false;
+    struct TmapCache {
+        const void *ptr;
+        int W;
+        CUtensorMap map;
+    };
+    std::vector<TmapCache> tmaps;  // TMA descriptors of recently used fields
+    int *d_status = nullptr;       // device status word of the bounded waits
     // host-run buffer
     void *d_host_buf = nullptr;
     size_t host_buf_bytes = 0;
@@ -46,6 +54,7 @@ struct AdvPlanImpl {
         cudaFree(d_vx);
         cudaFree(d_host_buf);
         cudaFree(d_partials);
+        cudaFree(d_status);
     }
 
     int halo() const { return desc.impl == BKMA_ADV_PLAIN ? 0 : npts - 1; }
@@ -56,6 +65,11 @@ struct AdvPlanImpl {
     }
     int64_t tiles(int w, int r) const { return ((lines + r - 1) / r) * ncb(w); }
 };
+
+bool adv_tma_eligible(const AdvPlanImpl &p, const void *src, int W);
+size_t adv_tma_smem(const AdvPlanImpl &p, int W);
+cudaError_t adv_tma_launch(AdvPlanImpl &p, const void *src, void *dst, int W, int threads,
+                           cudaStream_t st);
 
 }  // namespace bkma
 

@@ -257,3 +257,52 @@ def test_zero_steps_is_identity(bkma, cuda):
     b = a.clone()
     plan.step(a, nsteps=0)
     assert torch.equal(a, b)
+
+
+TMA_CASES = [
+    (3, 256, 64, 0.003, 0.0, 1.0, -1.0, 1.0),
+    (4, 1000, 48, 0.0011, 0.0, 1.0, -1.0, 1.0),   # last TMA box partly past n1
+    (2, 300, 20, 0.002, 0.0, 1.0, -2.0, 2.0),     # ragged column block (16 + 4)
+    (3, 64, 16, 0.01, 0.0, 1.0, -1.0, 1.0),
+    (2, 2048, 32, 0.0007, 0.0, 1.0, -1.0, 1.0),
+]
+
+
+@pytest.mark.parametrize("case", TMA_CASES)
+@pytest.mark.parametrize("degree,weights", [(5, "reference"), (3, "lagrange")])
+def test_tma_and_cp_async_paths_bit_identical(bkma, cuda, oracle, case, degree, weights):
+    """The TMA-staged kernel and the cp.async-staged kernel compute the same
+    FP32 operations in the same order: identical bits, and both within the
+    FP32 tolerance of the FP64 oracle."""
+    import torch
+    p = AdvParams(*case)
+    f0 = _init(p, 10).astype(np.float32).astype(np.float64)
+    outs = {}
+    for path, W in ((0, 16), (1, 16), (1, 8)):
+        if path == 1 and p.n2 < W:
+            continue
+        plan = _plan(bkma, p, dtype="f32", degree=degree, weights=weights)
+        info = plan.set_tile(W, 1, 256, path)
+        assert info["path"] == path
+        d = _to(cuda, f0, torch.float32)
+        plan.step(d, nsteps=3)
+        plan.status()
+        outs[(path, W)] = d
+    ref = outs[(0, 16)]
+    for k, v in outs.items():
+        assert torch.equal(v, ref), k
+    want = oracle.adv_step(p, f0.copy(), 3, degree=degree, ref_weights=(weights == "reference"))
+    err = np.abs(ref.cpu().numpy().astype(np.float64) - want).max() / np.abs(want).max()
+    assert err <= 3e-7 * 3 + 2e-7, err
+
+
+def test_set_tile_validation(bkma, cuda):
+    p = AdvParams(*TMA_CASES[0])
+    plan = _plan(bkma, p, dtype="f32")
+    with pytest.raises(bkma.BkmaError):
+        plan.set_tile(16, 1, 100, 0)
+    with pytest.raises(bkma.BkmaError):
+        plan.set_tile(16, 2, 256, 0)
+    f64 = _plan(bkma, p, dtype="f64")
+    with pytest.raises(bkma.BkmaError):
+        f64.set_tile(16, 1, 256, 1)
