@@ -180,7 +180,7 @@ def cpu_baseline_sample(cores: int):
     S = int(max(1, min(N0, S * 3.0 / max(one, 1e-3))))
     f = np.ascontiguousarray(np.sin(2 * np.pi * x)[None, :, None] +
                              NOISE * rng.uniform(-1, 1, (S, N1, N2)))
-    steps = 4
+    steps = 6
     t0 = time.perf_counter()
     orc.adv_step(p, f, steps, velocity=vel[:S], nthreads=cores)
     el = time.perf_counter() - t0
@@ -268,11 +268,13 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD, "n0": N0, "n1": N1, "n2": N2, "degree": 5,
                    "dt": DT, "parallelism": f"replicas x{world} (n0 sharded, no exchange)",
                    "l2": "field 4 GiB > L2 129 MB, no flush",
-                   "tile": {k: info[k] for k in ("tile_cols", "tile_slabs", "threads",
+                   "tile": {k: info[k] for k in ("tile_cols", "tile_slabs", "threads", "path",
                                                   "smem_bytes", "tiles", "exception_lines")}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
-                     "kernel": "adv_staged<float,6>", "peak_kind": f"{peak_kind} copy bandwidth",
+                     "kernel": (f"adv_tma_f32<6,{info['tile_cols']}>" if info["path"] == 1
+                                else "adv_staged<float,6>"),
+                     "peak_kind": f"{peak_kind} copy bandwidth",
                      "algorithmic_bytes_per_launch": cells * 8},
         "gpu_launches": args.steps,
         "clocks": clocks,

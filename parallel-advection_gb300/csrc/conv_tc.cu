@@ -129,6 +129,16 @@ __device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_
         : "memory");
 }
 
+// Same MMA with the B descriptor given as its two 32-bit words.
+__device__ __forceinline__ void mma_ts2(uint32_t d_tmem, uint32_t a_tmem, uint32_t b_lo,
+                                        uint32_t b_hi, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n .reg .b64 bd;\n setp.ne.u32 p, %5, 0;\n mov.b64 bd, {%2, %3};\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], bd, %4, p;\n}" ::"r"(d_tmem),
+        "r"(a_tmem), "r"(b_lo), "r"(b_hi), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile(
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -213,6 +223,7 @@ __device__ __forceinline__ void load_block(const Args &a, int b, int tile, int c
     }
 }
 
+template <int KC>  // K16 steps per tap: Cin / 16
 __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
@@ -251,7 +262,6 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_base_sh;
-    const int kc = a.cin / 16;           // K16 steps per tap
     const int wcols = a.K * a.cin / 2;   // TMEM columns of A
     const uint32_t acc_col0 = (uint32_t)W_COLS_MAX;
 
@@ -298,23 +308,32 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
             unsigned char *stage = smem + (size_t)s * a.stage_bytes;
-            for (int p = pt; p < pairs; p += 32 * NUM_PROD_WARPS) {
-                const int c = p % nchunks;
-                const int q = p / nchunks;
-                uint4 v[8];
-                load_block(a, b, tile, c, q, v);
-                const uint32_t *w = reinterpret_cast<const uint32_t *>(v);
-                unsigned char *dst = stage + ((size_t)c * a.chunk_rows + 8 * q) * 16;
+            constexpr int PT = 32 * NUM_PROD_WARPS;
+            for (int p = pt; p < pairs; p += 2 * PT) {
+                // two 8x8 blocks in flight before either is transposed
+                uint4 v[2][8];
+                const bool second = p + PT < pairs;
+                load_block(a, b, tile, p % nchunks, p / nchunks, v[0]);
+                if (second) load_block(a, b, tile, (p + PT) % nchunks, (p + PT) / nchunks, v[1]);
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int wsel = i / 2;
-                    const uint32_t sel = (i & 1) ? 0x7632u : 0x5410u;
-                    uint4 o;
-                    o.x = __byte_perm(w[0 * 4 + wsel], w[1 * 4 + wsel], sel);
-                    o.y = __byte_perm(w[2 * 4 + wsel], w[3 * 4 + wsel], sel);
-                    o.z = __byte_perm(w[4 * 4 + wsel], w[5 * 4 + wsel], sel);
-                    o.w = __byte_perm(w[6 * 4 + wsel], w[7 * 4 + wsel], sel);
-                    *reinterpret_cast<uint4 *>(dst + (size_t)i * 16) = o;
+                for (int h = 0; h < 2; ++h) {
+                    if (h == 1 && !second) break;
+                    const int ph2 = p + h * PT;
+                    const int c = ph2 % nchunks;
+                    const int q = ph2 / nchunks;
+                    const uint32_t *w = reinterpret_cast<const uint32_t *>(v[h]);
+                    unsigned char *dst = stage + ((size_t)c * a.chunk_rows + 8 * q) * 16;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int wsel = i / 2;
+                        const uint32_t sel = (i & 1) ? 0x7632u : 0x5410u;
+                        uint4 o;
+                        o.x = __byte_perm(w[0 * 4 + wsel], w[1 * 4 + wsel], sel);
+                        o.y = __byte_perm(w[2 * 4 + wsel], w[3 * 4 + wsel], sel);
+                        o.z = __byte_perm(w[4 * 4 + wsel], w[5 * 4 + wsel], sel);
+                        o.w = __byte_perm(w[6 * 4 + wsel], w[7 * 4 + wsel], sel);
+                        *reinterpret_cast<uint4 *>(dst + (size_t)i * 16) = o;
+                    }
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -323,7 +342,10 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     } else if (is_mma) {
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(128, NSUB);
-            const uint32_t lbo = (uint32_t)a.chunk_rows * 16;
+            const uint32_t lbo16 = (uint32_t)a.chunk_rows;  // LBO >> 4
+            // high word: SBO = 128 B (>> 4 = 8) in bits 32-45, version 1 at bit 46
+            const uint32_t desc_hi = (128u >> 4) | (1u << 14);
+            const uint32_t a_step = (uint32_t)(a.cin / 2);  // TMEM columns per tap
             int it = 0;
             int n = 0;  // sub-tile counter
             for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
@@ -342,13 +364,17 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
                     }
                     fence_after();
                     const uint32_t d_tmem = tmem + acc_col0 + (uint32_t)(acc * NSUB);
-                    for (int k = 0; k < a.K; ++k) {
-                        for (int j = 0; j < kc; ++j) {
-                            const uint32_t a_tmem = tmem + (uint32_t)((k * a.cin + 16 * j) / 2);
-                            const uint32_t baddr = stage_addr + (uint32_t)(2 * j) * lbo +
-                                                   (uint32_t)(NSUB * sub + k) * 16u;
-                            const uint64_t bdesc = desc_kmajor_noswizzle(baddr, lbo, 128);
-                            mma_ts(d_tmem, a_tmem, bdesc, idesc, (k | j) != 0 ? 1u : 0u);
+                    // Descriptor low word: start address >> 4 in bits 0-13
+                    // (below 256 KB, so adding row / chunk offsets never
+                    // carries into the LBO field in bits 16-29).
+                    const uint32_t lo0 = ((stage_addr + (uint32_t)(NSUB * sub) * 16u) >> 4) |
+                                         (lbo16 << 16);
+                    uint32_t a_k = tmem;
+                    for (int k = 0; k < a.K; ++k, a_k += a_step) {
+#pragma unroll
+                        for (int j = 0; j < KC; ++j) {
+                            mma_ts2(d_tmem, a_k + 8u * j, lo0 + (uint32_t)k + 2u * j * lbo16, desc_hi,
+                                    idesc, (k | j) != 0 ? 1u : 0u);
                         }
                     }
                     mma_commit(&accf_bar[acc]);
@@ -434,8 +460,8 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
 
 bkma_status conv_tc_plan_init(ConvPlanImpl &p) {
     const bkma_conv_desc &d = p.desc;
-    if (d.cout > 128)
-        return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cout must be <= 128");
+    if (d.cout > 128 || d.cin > 128)
+        return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin and cout must be <= 128");
     if (d.cin % 16 != 0)
         return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be a multiple of 16");
     if (d.ksize * d.cin > 2 * tc::W_COLS_MAX)
@@ -489,11 +515,22 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
     a.status = (int *)p.d_status;
     const size_t smem = (size_t)tc::STAGES * a.stage_bytes;
     if (smem > 220 * 1024) return fail(BKMA_ERR_UNSUPPORTED, "tensor path: stage too large for shared memory");
-    BKMA_CUDA_TRY(cudaFuncSetAttribute(tc::conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+    void (*kern)(tc::Args) = nullptr;
+    switch (a.cin / 16) {
+    case 1: kern = tc::conv_tc_kernel<1>; break;
+    case 2: kern = tc::conv_tc_kernel<2>; break;
+    case 3: kern = tc::conv_tc_kernel<3>; break;
+    case 4: kern = tc::conv_tc_kernel<4>; break;
+    case 5: kern = tc::conv_tc_kernel<5>; break;
+    case 6: kern = tc::conv_tc_kernel<6>; break;
+    case 7: kern = tc::conv_tc_kernel<7>; break;
+    case 8: kern = tc::conv_tc_kernel<8>; break;
+    default: return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be 16..128");
+    }
+    BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t items = (int64_t)a.B * a.ntiles;
     const int grid = (int)std::min<int64_t>(p.grid, items);
-    tc::conv_tc_kernel<<<grid, tc::THREADS, smem, st>>>(a);
+    kern<<<grid, tc::THREADS, smem, st>>>(a);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
 }
