@@ -5,9 +5,12 @@
 // (W_k = weight[:, :, k]). GEMM view per tap: M = Cout (<= 128, zero-padded
 // rows), N = output positions, K = Cin.
 //
-//  * A (weights) lives in TMEM for the whole kernel: lane m = output channel,
-//    column (k*Cin + ci)/2 holds the BF16 pair (ci, ci+1) of tap k. One MMA
-//    reads only B from shared memory.
+//  * A (weights) stays on chip for the whole kernel. Every MMA has N = 128
+//    (a tcgen05.mma costs at least ~51 cycles, so N = 32 or 64 cannot reach
+//    the tensor peak; N >= 128 does). Two 128-column FP32 accumulators leave
+//    256 TMEM columns for weights: taps 0..3 (Cin = 128) sit in TMEM (lane m
+//    = output channel, column (k*Cin + ci)/2 holds the BF16 pair (ci, ci+1)),
+//    the remaining taps sit in shared memory as K-major no-swizzle A tiles.
 //  * B (activations) is staged K-major without swizzle: 16-byte rows of 8
 //    input channels, one row per position l, rows contiguous (SBO = 128 B),
 //    ci-chunks at a padded stride (LBO). Tap k is then the same staging
@@ -18,10 +21,9 @@
 //    odd row count of a chunk spreads the 8 stores of a phase over all
 //    banks). Rows past the tile come from the halo snapshot (conv.cu), so
 //    tiles of one row can be overwritten in place concurrently.
-//  * One thread issues the MMAs (N = 32 per instruction, 4 sub-tiles per
-//    128-position stage) into two alternating TMEM accumulators; four
-//    epilogue warps drain one accumulator (tcgen05.ld) while the other fills,
-//    add the bias, round to BF16 and store.
+//  * One thread issues the MMAs of a 128-position item (K taps x Cin/16
+//    K-steps) into one of two alternating TMEM accumulators; four epilogue
+//    warps drain the other (tcgen05.ld), add the bias, round to BF16 and store.
 //  * Every mbarrier wait is bounded; on timeout the CTA raises a status word,
 //    stops, drains its MMAs with a bounded wait and frees TMEM.
 #include <cuda_bf16.h>
@@ -33,13 +35,12 @@
 namespace bkma {
 namespace tc {
 
-constexpr int TILE = 128;          // output positions per stage
-constexpr int NSUB = 32;           // positions per MMA (N)
-constexpr int SUBS = TILE / NSUB;  // sub-tiles per stage
-constexpr int STAGES = 4;
-constexpr int ACC_COLS = 2 * NSUB;  // two accumulators
+constexpr int TILE = 128;   // output positions per item = N of every MMA
+constexpr int STAGES_MAX = 4;
 constexpr int TMEM_COLS = 512;
-constexpr int W_COLS_MAX = TMEM_COLS - ACC_COLS;  // 448: K*Cin <= 896
+constexpr int ACC_COL0 = 256;     // two FP32 accumulators of 128 columns: 256, 384
+constexpr int W_TMEM_COLS = 256;  // TMEM columns for weights (taps 0 .. taps_tmem-1)
+constexpr int SMEM_LIMIT = 232448 - 1024;
 constexpr int NUM_EPI_WARPS = 4;
 constexpr int NUM_PROD_WARPS = 4;
 constexpr int THREADS = 32 * (NUM_EPI_WARPS + NUM_PROD_WARPS + 1);
@@ -57,6 +58,9 @@ struct Args {
     int halo_rows;   // rows after the tile: round_up(K-1, 8)
     int chunk_rows;  // TILE + halo_rows + 1 (odd, spreads banks)
     int stage_bytes;
+    int stages;      // activation stages (2..STAGES_MAX)
+    int taps_tmem;   // taps whose weights live in TMEM; the rest live in shared memory
+    int wsmem_bytes; // shared-memory weights, placed before the stages
     int *status;     // device status word (0 ok, 4 timeout)
 };
 
@@ -103,30 +107,10 @@ __device__ __forceinline__ void fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, no swizzle.
-__device__ __forceinline__ uint64_t desc_kmajor_noswizzle(uint32_t addr, uint32_t lbo,
-                                                          uint32_t sbo) {
-    uint64_t d = 0;
-    d |= (uint64_t)((addr & 0x3FFFF) >> 4);
-    d |= (uint64_t)((lbo & 0x3FFFF) >> 4) << 16;
-    d |= (uint64_t)((sbo & 0x3FFFF) >> 4) << 32;
-    d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-    return d;                // base offset 0, swizzle mode 0 (none)
-}
-
 // Instruction descriptor: kind::f16, BF16 A and B, FP32 D, both K-major.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
            ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc,
-                                       uint32_t idesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}" ::"r"(d_tmem),
-        "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
-        : "memory");
 }
 
 // Same MMA with the B descriptor given as its two 32-bit words.
@@ -136,6 +120,17 @@ __device__ __forceinline__ void mma_ts2(uint32_t d_tmem, uint32_t a_tmem, uint32
         "{\n .reg .pred p;\n .reg .b64 bd;\n setp.ne.u32 p, %5, 0;\n mov.b64 bd, {%2, %3};\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], bd, %4, p;\n}" ::"r"(d_tmem),
         "r"(a_tmem), "r"(b_lo), "r"(b_hi), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// MMA with both operands in shared memory (descriptor words lo/hi).
+__device__ __forceinline__ void mma_ss2(uint32_t d_tmem, uint32_t a_lo, uint32_t a_hi, uint32_t b_lo,
+                                        uint32_t b_hi, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.u32 p, %6, 0;\n mov.b64 ad, {%1, %2};\n"
+        " mov.b64 bd, {%3, %4};\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p;\n}" ::"r"(d_tmem),
+        "r"(a_lo), "r"(a_hi), "r"(b_lo), "r"(b_hi), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 
@@ -226,7 +221,7 @@ __device__ __forceinline__ void load_block(const Args &a, int b, int tile, int c
 template <int KC>  // K16 steps per tap: Cin / 16
 __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
+    __shared__ __align__(8) uint64_t full_bar[STAGES_MAX], empty_bar[STAGES_MAX];
     __shared__ __align__(8) uint64_t accf_bar[2], acce_bar[2];
     __shared__ __align__(8) uint64_t drain_bar;
     __shared__ uint32_t tmem_base_sh;
@@ -237,10 +232,11 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     const bool is_epi = warp < NUM_EPI_WARPS;
     const bool is_prod = warp >= NUM_EPI_WARPS && warp < NUM_EPI_WARPS + NUM_PROD_WARPS;
     const bool is_mma = warp == NUM_EPI_WARPS + NUM_PROD_WARPS;
+    const int stages = a.stages;
 
     if (threadIdx.x == 0) {
         abort_flag = 0;
-        for (int s = 0; s < STAGES; ++s) {
+        for (int s = 0; s < stages; ++s) {
             mbar_init(&full_bar[s], 32 * NUM_PROD_WARPS);
             mbar_init(&empty_bar[s], 1);
         }
@@ -262,12 +258,17 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_base_sh;
-    const int wcols = a.K * a.cin / 2;   // TMEM columns of A
-    const uint32_t acc_col0 = (uint32_t)W_COLS_MAX;
+    const int cin = KC * 16;
+    unsigned char *wsm = smem;                      // shared-memory weights
+    unsigned char *stages_sm = smem + a.wsmem_bytes;  // activation stages
 
-    // ---- weights -> TMEM (epilogue warps: thread = output channel lane)
+    // ---- weights on chip (epilogue warps: thread = output channel)
     if (is_epi) {
         const int co = threadIdx.x;  // 0..127
+        const __nv_bfloat16 *wr = a.w + (int64_t)co * cin * a.K;
+        const bool live = co < a.cout;
+        // taps 0 .. taps_tmem-1 -> TMEM columns (k*cin + ci)/2
+        const int wcols = a.taps_tmem * cin / 2;
         const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
         for (int c0 = 0; c0 < wcols; c0 += 32) {
             uint32_t v[32];
@@ -275,10 +276,9 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
             for (int j = 0; j < 32; ++j) {
                 const int col = c0 + j;
                 uint32_t pair = 0;
-                if (col < wcols && co < a.cout) {
-                    const int k = (2 * col) / a.cin;
-                    const int ci = (2 * col) % a.cin;
-                    const __nv_bfloat16 *wr = a.w + (int64_t)co * a.cin * a.K;
+                if (col < wcols && live) {
+                    const int k = (2 * col) / cin;
+                    const int ci = (2 * col) % cin;
                     pair = bf16_bits(wr[(int64_t)ci * a.K + k]) |
                            (bf16_bits(wr[(int64_t)(ci + 1) * a.K + k]) << 16);
                 }
@@ -287,6 +287,23 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
             tmem_st32(lane_addr + (uint32_t)c0, v);
         }
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        // taps taps_tmem .. K-1 -> shared memory [tap][ci-chunk][co][8 ci]
+        for (int t = 0; t < a.K - a.taps_tmem; ++t) {
+            const int k = a.taps_tmem + t;
+            for (int c = 0; c < KC * 2; ++c) {
+                uint32_t wv[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int ci = 8 * c + 2 * e;
+                    wv[e] = live ? (bf16_bits(wr[(int64_t)ci * a.K + k]) |
+                                    (bf16_bits(wr[(int64_t)(ci + 1) * a.K + k]) << 16))
+                                 : 0u;
+                }
+                *reinterpret_cast<uint4 *>(wsm + (size_t)t * cin * 256 + (size_t)c * 2048 +
+                                           (size_t)co * 16) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     fence_before();
     __syncthreads();
@@ -297,17 +314,17 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
 
     if (is_prod) {
         const int pt = threadIdx.x - 32 * NUM_EPI_WARPS;  // 0..127
-        const int nchunks = a.cin / 8;
+        const int nchunks = cin / 8;
         const int qblocks = (TILE + a.halo_rows) / 8;
         const int pairs = nchunks * qblocks;
         int it = 0;
         for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
-            const int s = it % STAGES;
-            const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+            const int s = it % stages;
+            const uint32_t ph = (uint32_t)(it / stages) & 1u;
             if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_flag, a.status)) break;
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
-            unsigned char *stage = smem + (size_t)s * a.stage_bytes;
+            unsigned char *stage = stages_sm + (size_t)s * a.stage_bytes;
             constexpr int PT = 32 * NUM_PROD_WARPS;
             for (int p = pt; p < pairs; p += 2 * PT) {
                 // two 8x8 blocks in flight before either is transposed
@@ -341,46 +358,45 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
         }
     } else if (is_mma) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(128, NSUB);
-            const uint32_t lbo16 = (uint32_t)a.chunk_rows;  // LBO >> 4
-            // high word: SBO = 128 B (>> 4 = 8) in bits 32-45, version 1 at bit 46
+            const uint32_t idesc = idesc_bf16(128, TILE);
+            const uint32_t lbo16 = (uint32_t)a.chunk_rows;  // B: LBO >> 4 (ci-chunk stride)
+            // high word of both descriptors: SBO = 128 B (>> 4 = 8), version 1 (bit 46)
             const uint32_t desc_hi = (128u >> 4) | (1u << 14);
-            const uint32_t a_step = (uint32_t)(a.cin / 2);  // TMEM columns per tap
+            const uint32_t a_step = (uint32_t)(cin / 2);  // TMEM columns per tap
+            // A in shared memory: LBO = 2048 B (chunk of 128 rows x 16 B)
+            const uint32_t wlo0 = (smem_base >> 4) | ((2048u >> 4) << 16);
+            const uint32_t tap16 = (uint32_t)(cin * 256) >> 4;
+            const uint32_t stage0 = smem_base + (uint32_t)a.wsmem_bytes;
             int it = 0;
-            int n = 0;  // sub-tile counter
             for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
-                const int s = it % STAGES;
-                const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                const int s = it % stages;
+                const uint32_t ph = (uint32_t)(it / stages) & 1u;
                 if (!mbar_wait(&full_bar[s], ph, &abort_flag, a.status)) break;
+                const int acc = it & 1;
+                const uint32_t aph = (uint32_t)(it >> 1) & 1u;
+                if (!mbar_wait(&acce_bar[acc], aph ^ 1u, &abort_flag, a.status)) break;
                 fence_after();
-                const uint32_t stage_addr = smem_base + (uint32_t)(s * a.stage_bytes);
-                bool ok = true;
-                for (int sub = 0; sub < SUBS; ++sub, ++n) {
-                    const int acc = n & 1;
-                    const uint32_t aph = (uint32_t)(n >> 1) & 1u;
-                    if (!mbar_wait(&acce_bar[acc], aph ^ 1u, &abort_flag, a.status)) {
-                        ok = false;
-                        break;
-                    }
-                    fence_after();
-                    const uint32_t d_tmem = tmem + acc_col0 + (uint32_t)(acc * NSUB);
-                    // Descriptor low word: start address >> 4 in bits 0-13
-                    // (below 256 KB, so adding row / chunk offsets never
-                    // carries into the LBO field in bits 16-29).
-                    const uint32_t lo0 = ((stage_addr + (uint32_t)(NSUB * sub) * 16u) >> 4) |
-                                         (lbo16 << 16);
-                    uint32_t a_k = tmem;
-                    for (int k = 0; k < a.K; ++k, a_k += a_step) {
+                const uint32_t d_tmem = tmem + (uint32_t)(ACC_COL0 + acc * TILE);
+                // descriptor low word: start address >> 4 (bits 0-13, < 256 KB so
+                // row / chunk offsets never carry into the LBO field at bit 16)
+                const uint32_t lo0 = ((stage0 + (uint32_t)(s * a.stage_bytes)) >> 4) | (lbo16 << 16);
+                uint32_t a_k = tmem;
+                int k = 0;
+                for (; k < a.taps_tmem; ++k, a_k += a_step) {
 #pragma unroll
-                        for (int j = 0; j < KC; ++j) {
-                            mma_ts2(d_tmem, a_k + 8u * j, lo0 + (uint32_t)k + 2u * j * lbo16, desc_hi,
-                                    idesc, (k | j) != 0 ? 1u : 0u);
-                        }
-                    }
-                    mma_commit(&accf_bar[acc]);
+                    for (int j = 0; j < KC; ++j)
+                        mma_ts2(d_tmem, a_k + 8u * j, lo0 + (uint32_t)k + 2u * j * lbo16, desc_hi,
+                                idesc, (k | j) != 0 ? 1u : 0u);
                 }
+                for (; k < a.K; ++k) {
+                    const uint32_t wk = wlo0 + (uint32_t)(k - a.taps_tmem) * tap16;
+#pragma unroll
+                    for (int j = 0; j < KC; ++j)
+                        mma_ss2(d_tmem, wk + 2u * j * 128u, desc_hi, lo0 + (uint32_t)k + 2u * j * lbo16,
+                                desc_hi, idesc, (k | j) != 0 ? 1u : 0u);
+                }
+                mma_commit(&accf_bar[acc]);
                 mma_commit(&empty_bar[s]);
-                if (!ok) break;
             }
             // all MMAs issued by this thread are complete once this arrives
             mma_commit(&drain_bar);
@@ -388,45 +404,47 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     } else if (is_epi) {
         const int co = threadIdx.x;
         const float bias = (a.bias && co < a.cout) ? __bfloat162float(a.bias[co]) : 0.0f;
-        const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16) + acc_col0;
-        int n = 0;
-        for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
+        const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)ACC_COL0;
+        int it = 0;
+        for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
-            bool ok = true;
-            for (int sub = 0; sub < SUBS; ++sub, ++n) {
-                const int acc = n & 1;
-                const uint32_t aph = (uint32_t)(n >> 1) & 1u;
-                if (!mbar_wait(&accf_bar[acc], aph, &abort_flag, a.status)) {
-                    ok = false;
-                    break;
-                }
-                fence_after();
-                uint32_t v[32];
-                tmem_ld32(lane_addr + (uint32_t)(acc * NSUB), v);
+            const int acc = it & 1;
+            const uint32_t aph = (uint32_t)(it >> 1) & 1u;
+            if (!mbar_wait(&accf_bar[acc], aph, &abort_flag, a.status)) break;
+            fence_after();
+            const int64_t l0 = (int64_t)tile * TILE;
+            __nv_bfloat16 *row = a.out + ((int64_t)b * a.cout + co) * a.out_stride;
+#pragma unroll 1
+            for (int half = 0; half < 2; ++half) {
+                uint32_t v[2][32];
+                const uint32_t col = lane_addr + (uint32_t)(acc * TILE + 64 * half);
+                tmem_ld32(col, v[0]);
+                tmem_ld32(col + 32u, v[1]);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                fence_before();
-                mbar_arrive(&acce_bar[acc]);
+                if (half == 1) {
+                    fence_before();
+                    mbar_arrive(&acce_bar[acc]);
+                }
                 if (co < a.cout) {
-                    const int64_t l0 = (int64_t)tile * TILE + NSUB * sub;
-                    __nv_bfloat16 *dst = a.out + ((int64_t)b * a.cout + co) * a.out_stride + l0;
-                    uint32_t pk[16];
+                    const int64_t lh = l0 + 64 * half;
+                    uint32_t pk[32];
 #pragma unroll
-                    for (int e = 0; e < 16; ++e) {
-                        const float f0 = __uint_as_float(v[2 * e]) + bias;
-                        const float f1 = __uint_as_float(v[2 * e + 1]) + bias;
+                    for (int e = 0; e < 32; ++e) {
+                        const float f0 = __uint_as_float(v[e / 16][(2 * e) % 32]) + bias;
+                        const float f1 = __uint_as_float(v[e / 16][(2 * e + 1) % 32]) + bias;
                         const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
                         pk[e] = *reinterpret_cast<const uint32_t *>(&h);
                     }
-                    const bool full = (l0 + NSUB <= a.lout) && ((a.out_stride % 8) == 0);
-                    if (full) {
+                    __nv_bfloat16 *dst = row + lh;
+                    if (lh + 64 <= a.lout && (a.out_stride % 8) == 0) {
                         uint4 *d4 = reinterpret_cast<uint4 *>(dst);
 #pragma unroll
-                        for (int e = 0; e < 4; ++e)
+                        for (int e = 0; e < 8; ++e)
                             d4[e] = make_uint4(pk[4 * e], pk[4 * e + 1], pk[4 * e + 2], pk[4 * e + 3]);
                     } else {
-                        for (int e = 0; e < NSUB; ++e) {
-                            if (l0 + e < a.lout) {
+                        for (int e = 0; e < 64; ++e) {
+                            if (lh + e < a.lout) {
                                 const uint16_t bits =
                                     (uint16_t)((pk[e / 2] >> (16 * (e & 1))) & 0xFFFFu);
                                 dst[e] = __ushort_as_bfloat16(bits);
@@ -435,7 +453,6 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
                     }
                 }
             }
-            if (!ok) break;
         }
     }
 
@@ -458,16 +475,37 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
 
 }  // namespace tc
 
+namespace {
+struct TcLayout {
+    int taps_tmem, wsmem_bytes, halo_rows, chunk_rows, stage_bytes, stages;
+};
+
+TcLayout tc_layout(const bkma_conv_desc &d) {
+    TcLayout t;
+    const int cin = (int)d.cin, K = (int)d.ksize;
+    t.taps_tmem = std::min(K, tc::W_TMEM_COLS / (cin / 2));
+    t.wsmem_bytes = (K - t.taps_tmem) * cin * 256;
+    t.wsmem_bytes = (t.wsmem_bytes + 1023) / 1024 * 1024;
+    t.halo_rows = std::max(8, (K - 1 + 7) / 8 * 8);
+    t.chunk_rows = tc::TILE + t.halo_rows + 1;
+    t.stage_bytes = ((cin / 8) * t.chunk_rows * 16 + 1023) / 1024 * 1024;
+    t.stages = std::min(tc::STAGES_MAX, (tc::SMEM_LIMIT - t.wsmem_bytes) / t.stage_bytes);
+    return t;
+}
+}  // namespace
+
 bkma_status conv_tc_plan_init(ConvPlanImpl &p) {
     const bkma_conv_desc &d = p.desc;
     if (d.cout > 128 || d.cin > 128)
         return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin and cout must be <= 128");
     if (d.cin % 16 != 0)
         return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be a multiple of 16");
-    if (d.ksize * d.cin > 2 * tc::W_COLS_MAX)
-        return fail(BKMA_ERR_UNSUPPORTED, "tensor path: ksize*cin must be <= 896 (TMEM-resident weights)");
     if (d.length % 8 != 0)
         return fail(BKMA_ERR_UNSUPPORTED, "tensor path: length must be a multiple of 8");
+    const TcLayout t = tc_layout(d);
+    if (t.stages < 2)
+        return fail(BKMA_ERR_UNSUPPORTED,
+                    "tensor path: ksize*cin too large for on-chip weights (TMEM + shared memory)");
     p.tensor = true;
     p.TL = tc::TILE;
     p.ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
@@ -486,13 +524,14 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
                         cudaStream_t st) {
     const bkma_conv_desc &d = p.desc;
     const bool inplace = (out == nullptr || out == data);
+    const auto misaligned = [](const void *q) { return q && ((uintptr_t)q % 16) != 0; };
+    if (misaligned(data) || misaligned(out) || misaligned(w))
+        return fail(BKMA_ERR_INVALID_ARG, "tensor path: data, out and weight must be 16-byte aligned");
     if (inplace && d.ksize > 1) {
         bkma_status s = conv_halo_prepass(p, data, st);
         if (s != BKMA_OK) return s;
     }
-    const auto misaligned = [](const void *q) { return q && ((uintptr_t)q % 16) != 0; };
-    if (misaligned(data) || misaligned(out) || misaligned(w))
-        return fail(BKMA_ERR_INVALID_ARG, "tensor path: data, out and weight must be 16-byte aligned");
+    const TcLayout t = tc_layout(d);
     tc::Args a;
     a.x = (const __nv_bfloat16 *)data;
     a.out = (__nv_bfloat16 *)(inplace ? data : out);
@@ -507,14 +546,14 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
     a.lout = d.length - d.ksize + 1;
     a.out_stride = inplace ? d.length : a.lout;
     a.ntiles = (int)p.ntiles;
-    a.halo_rows = (int)((d.ksize - 1 + 7) / 8 * 8);
-    if (a.halo_rows == 0) a.halo_rows = 8;
-    a.chunk_rows = tc::TILE + a.halo_rows + 1;
-    a.stage_bytes = (a.cin / 8) * a.chunk_rows * 16;
-    a.stage_bytes = (a.stage_bytes + 1023) / 1024 * 1024;
+    a.halo_rows = t.halo_rows;
+    a.chunk_rows = t.chunk_rows;
+    a.stage_bytes = t.stage_bytes;
+    a.stages = t.stages;
+    a.taps_tmem = t.taps_tmem;
+    a.wsmem_bytes = t.wsmem_bytes;
     a.status = (int *)p.d_status;
-    const size_t smem = (size_t)tc::STAGES * a.stage_bytes;
-    if (smem > 220 * 1024) return fail(BKMA_ERR_UNSUPPORTED, "tensor path: stage too large for shared memory");
+    const size_t smem = (size_t)t.wsmem_bytes + (size_t)t.stages * t.stage_bytes;
     void (*kern)(tc::Args) = nullptr;
     switch (a.cin / 16) {
     case 1: kern = tc::conv_tc_kernel<1>; break;
