@@ -69,11 +69,12 @@ __global__ void __launch_bounds__(256) conv_ref_kernel(ConvRefArgs a) {
 // ---------------------------------------------------------------- torch
 
 // Copy the right halo of every tile: halo[b][t][ci][j] = x[b][ci][(t+1)*TL + j]
-// for j < K-1 (columns past L are never read).
+// for j < K-1, zero for K-1 <= j < hw (hw >= K-1 pads rows to a vector width;
+// columns past L are zero and never used).
 template <typename T>
 __global__ void conv_halo_kernel(const T *x, T *halo, int64_t B, int64_t cin, int64_t L,
-                                 int K, int TL, int64_t ntiles) {
-    const int hk = K - 1;
+                                 int K, int TL, int64_t ntiles, int hw) {
+    const int hk = hw;
     const int64_t total = B * ntiles * cin * hk;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -85,7 +86,7 @@ __global__ void conv_halo_kernel(const T *x, T *halo, int64_t B, int64_t cin, in
         const int64_t t = r % ntiles;
         const int64_t b = r / ntiles;
         const int64_t col = (t + 1) * TL + j;
-        halo[i] = col < L ? x[(b * cin + ci) * L + col] : T(0);
+        halo[i] = (col < L && j < K - 1) ? x[(b * cin + ci) * L + col] : T(0);
     }
 }
 
@@ -151,15 +152,15 @@ bkma_status conv_halo_prepass(ConvPlanImpl &p, const void *x, cudaStream_t st) {
     if (d.dtype == BKMA_F64)
         conv_halo_kernel<double><<<blocks, 256, 0, st>>>((const double *)x, (double *)p.d_halo,
                                                         d.batch, d.cin, d.length, (int)d.ksize,
-                                                        p.TL, p.ntiles);
+                                                        p.TL, p.ntiles, p.halo_width);
     else if (d.dtype == BKMA_F32)
         conv_halo_kernel<float><<<blocks, 256, 0, st>>>((const float *)x, (float *)p.d_halo,
                                                        d.batch, d.cin, d.length, (int)d.ksize,
-                                                       p.TL, p.ntiles);
+                                                       p.TL, p.ntiles, p.halo_width);
     else
         conv_halo_kernel<uint16_t><<<blocks, 256, 0, st>>>((const uint16_t *)x, (uint16_t *)p.d_halo,
                                                           d.batch, d.cin, d.length, (int)d.ksize,
-                                                          p.TL, p.ntiles);
+                                                          p.TL, p.ntiles, p.halo_width);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
 }
@@ -273,7 +274,8 @@ bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **p
             const size_t es = d.dtype == BKMA_F64 ? 8 : 4;
             const size_t smem = es * (size_t)(d.cin * (p.TL + d.ksize - 1));
             if (smem > 227 * 1024) s = fail(BKMA_ERR_UNSUPPORTED, "cin too large for the plain tile");
-            p.halo_bytes = es * (size_t)(d.batch * p.ntiles * d.cin * (d.ksize - 1));
+            p.halo_width = (int)(d.ksize - 1);
+            p.halo_bytes = es * (size_t)(d.batch * p.ntiles * d.cin * p.halo_width);
         }
         if (s == BKMA_OK && d.inplace && p.halo_bytes > 0) {
             cudaError_t e = cudaMalloc(&p.d_halo, p.halo_bytes);

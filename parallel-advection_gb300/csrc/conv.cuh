@@ -42,6 +42,7 @@ struct ConvPlanImpl {
     int64_t ntiles = 0;   // tiles per row
     void *d_halo = nullptr;
     size_t halo_bytes = 0;
+    int halo_width = 0;       // halo values kept per (row, tile, channel) >= K-1
     void *d_wpack = nullptr;  // weights packed for the tensor path
     size_t wpack_bytes = 0;
     void *d_status = nullptr; // device status word of the tensor kernel

@@ -42,7 +42,8 @@ constexpr int ACC_COL0 = 256;     // two FP32 accumulators of 128 columns: 256, 
 constexpr int W_TMEM_COLS = 256;  // TMEM columns for weights (taps 0 .. taps_tmem-1)
 constexpr int SMEM_LIMIT = 232448 - 1024;
 constexpr int NUM_EPI_WARPS = 4;
-constexpr int NUM_PROD_WARPS = 4;
+constexpr int NUM_PROD_WARPS = 8;  // two groups of 4 warps, alternate items
+constexpr int PROD_GROUP = 128;    // threads per producer group
 constexpr int THREADS = 32 * (NUM_EPI_WARPS + NUM_PROD_WARPS + 1);
 constexpr uint32_t kSpinLimit = 1u << 22;  // x ~ 0.25 us backoff: ~1 s
 
@@ -51,7 +52,9 @@ struct Args {
     __nv_bfloat16 *out;       // (B, Cout, out_stride)
     const __nv_bfloat16 *w;   // (Cout, Cin, K)
     const __nv_bfloat16 *bias;  // (Cout) or null
-    const __nv_bfloat16 *halo;  // [B][ntiles][Cin][K-1] or null
+    const __nv_bfloat16 *halo;  // [B][ntiles][Cin][halo_rows] or null (out of place)
+    const uint32_t *wpack_tmem;  // [128][256] BF16 pairs: TMEM image of taps 0..taps_tmem-1
+    const uint4 *wpack_smem;     // shared-memory image of taps taps_tmem..K-1
     int B, cin, cout, K;
     int64_t L, lout, out_stride;
     int ntiles;
@@ -174,14 +177,21 @@ __device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat16 h) {
 }
 
 // Load the 8x8 block (ci = 8c..8c+7) x (rows 8q..8q+7 of the tile) into v[j]
-// (row j = ci 8c+j, 8 positions).
+// (row j = ci 8c+j, 8 positions). Rows past the tile come from the halo
+// snapshot when running in place (16-byte rows, halo_rows values per channel).
 __device__ __forceinline__ void load_block(const Args &a, int b, int tile, int c, int q,
                                            uint4 (&v)[8]) {
     const int64_t l0 = (int64_t)tile * TILE;
     const int r0 = 8 * q;
     const int64_t col = l0 + r0;
-    const bool from_halo = a.halo != nullptr && r0 >= TILE;
-    if (!from_halo && col + 8 <= a.L && (a.L % 8) == 0) {
+    if (a.halo != nullptr && r0 >= TILE) {
+        const __nv_bfloat16 *h =
+            a.halo + (((int64_t)b * a.ntiles + tile) * a.cin + 8 * c) * a.halo_rows + (r0 - TILE);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = *reinterpret_cast<const uint4 *>(h + (int64_t)j * a.halo_rows);
+        return;
+    }
+    if (col + 8 <= a.L) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int64_t ci = 8 * c + j;
@@ -189,32 +199,69 @@ __device__ __forceinline__ void load_block(const Args &a, int b, int tile, int c
         }
         return;
     }
-    // ragged end or halo rows: element-wise
+    // past the end of the row: zeros (L is a multiple of 8, so a block is
+    // either fully inside or fully outside)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const int64_t ci = 8 * c + j;
-        uint32_t wv[4];
+    for (int j = 0; j < 8; ++j) v[j] = make_uint4(0, 0, 0, 0);
+}
+
+// Transpose an 8x8 BF16 block (v[j] = channel j, 8 positions) into 8 rows of
+// 8 channels and store them at dst + 16*i.
+__device__ __forceinline__ void store_block(unsigned char *dst, const uint4 (&v)[8]) {
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(v);
 #pragma unroll
-        for (int e2 = 0; e2 < 4; ++e2) {
-            uint32_t pair = 0;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int r = r0 + 2 * e2 + h;
-                const int64_t l = l0 + r;
-                uint32_t bits = 0;
-                if (from_halo) {
-                    const int hk = r - TILE;
-                    if (hk < a.K - 1)
-                        bits = bf16_bits(a.halo[(((int64_t)b * a.ntiles + tile) * a.cin + ci) *
-                                                    (a.K - 1) + hk]);
-                } else if (l < a.L) {
-                    bits = bf16_bits(a.x[((int64_t)b * a.cin + ci) * a.L + l]);
-                }
-                pair |= bits << (16 * h);
+    for (int i = 0; i < 8; ++i) {
+        const int wsel = i / 2;
+        const uint32_t sel = (i & 1) ? 0x7632u : 0x5410u;
+        uint4 o;
+        o.x = __byte_perm(w[0 * 4 + wsel], w[1 * 4 + wsel], sel);
+        o.y = __byte_perm(w[2 * 4 + wsel], w[3 * 4 + wsel], sel);
+        o.z = __byte_perm(w[4 * 4 + wsel], w[5 * 4 + wsel], sel);
+        o.w = __byte_perm(w[6 * 4 + wsel], w[7 * 4 + wsel], sel);
+        *reinterpret_cast<uint4 *>(dst + (size_t)i * 16) = o;
+    }
+}
+
+// Weight pre-pack: the TMEM image (taps 0..taps_tmem-1 as BF16 pairs per
+// output channel) and the shared-memory image of the other taps
+// ([tap][ci-chunk][co][8 ci], K-major no-swizzle A tiles of 128 rows).
+__global__ void conv_tc_pack_weights(const __nv_bfloat16 *w, int cin, int cout, int K,
+                                     int taps_tmem, uint32_t *tm_img, uint32_t *sm_img) {
+    const int wcols = taps_tmem * cin / 2;
+    const int nA = 128 * 256;
+    const int nB = (K - taps_tmem) * (cin / 8) * 128 * 4;  // 32-bit words
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA + nB; i += gridDim.x * blockDim.x) {
+        int co, k, ci;
+        if (i < nA) {
+            co = i / 256;
+            const int col = i % 256;
+            if (col >= wcols || co >= cout) {
+                tm_img[i] = 0;
+                continue;
             }
-            wv[e2] = pair;
+            k = (2 * col) / cin;
+            ci = (2 * col) % cin;
+        } else {
+            int r = i - nA;
+            const int e = r % 4;
+            r /= 4;
+            co = r % 128;
+            r /= 128;
+            const int c = r % (cin / 8);
+            k = taps_tmem + r / (cin / 8);
+            ci = 8 * c + 2 * e;
+            if (co >= cout) {
+                sm_img[i - nA] = 0;
+                continue;
+            }
         }
-        v[j] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+        const __nv_bfloat16 *wr = w + (int64_t)co * cin * K;
+        const uint32_t pair = (uint32_t)__bfloat16_as_ushort(wr[(int64_t)ci * K + k]) |
+                              ((uint32_t)__bfloat16_as_ushort(wr[(int64_t)(ci + 1) * K + k]) << 16);
+        if (i < nA)
+            tm_img[i] = pair;
+        else
+            sm_img[i - nA] = pair;
     }
 }
 
@@ -237,7 +284,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     if (threadIdx.x == 0) {
         abort_flag = 0;
         for (int s = 0; s < stages; ++s) {
-            mbar_init(&full_bar[s], 32 * NUM_PROD_WARPS);
+            mbar_init(&full_bar[s], PROD_GROUP);
             mbar_init(&empty_bar[s], 1);
         }
         for (int i = 0; i < 2; ++i) {
@@ -262,47 +309,30 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     unsigned char *wsm = smem;                      // shared-memory weights
     unsigned char *stages_sm = smem + a.wsmem_bytes;  // activation stages
 
-    // ---- weights on chip (epilogue warps: thread = output channel)
-    if (is_epi) {
-        const int co = threadIdx.x;  // 0..127
-        const __nv_bfloat16 *wr = a.w + (int64_t)co * cin * a.K;
-        const bool live = co < a.cout;
-        // taps 0 .. taps_tmem-1 -> TMEM columns (k*cin + ci)/2
+    // ---- weights on chip from the pre-packed images
+    if (is_epi) {  // TMEM part: thread = output channel = TMEM lane
+        const int co = threadIdx.x;
         const int wcols = a.taps_tmem * cin / 2;
         const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.wpack_tmem + (size_t)co * 256);
         for (int c0 = 0; c0 < wcols; c0 += 32) {
             uint32_t v[32];
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const int col = c0 + j;
-                uint32_t pair = 0;
-                if (col < wcols && live) {
-                    const int k = (2 * col) / cin;
-                    const int ci = (2 * col) % cin;
-                    pair = bf16_bits(wr[(int64_t)ci * a.K + k]) |
-                           (bf16_bits(wr[(int64_t)(ci + 1) * a.K + k]) << 16);
-                }
-                v[j] = pair;
+            for (int j = 0; j < 8; ++j) {
+                const uint4 q4 = src[c0 / 4 + j];
+                v[4 * j] = q4.x;
+                v[4 * j + 1] = q4.y;
+                v[4 * j + 2] = q4.z;
+                v[4 * j + 3] = q4.w;
             }
             tmem_st32(lane_addr + (uint32_t)c0, v);
         }
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-        // taps taps_tmem .. K-1 -> shared memory [tap][ci-chunk][co][8 ci]
-        for (int t = 0; t < a.K - a.taps_tmem; ++t) {
-            const int k = a.taps_tmem + t;
-            for (int c = 0; c < KC * 2; ++c) {
-                uint32_t wv[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int ci = 8 * c + 2 * e;
-                    wv[e] = live ? (bf16_bits(wr[(int64_t)ci * a.K + k]) |
-                                    (bf16_bits(wr[(int64_t)(ci + 1) * a.K + k]) << 16))
-                                 : 0u;
-                }
-                *reinterpret_cast<uint4 *>(wsm + (size_t)t * cin * 256 + (size_t)c * 2048 +
-                                           (size_t)co * 16) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
-            }
-        }
+    }
+    {  // shared-memory part: every thread copies 16-byte chunks
+        const int n16 = (a.K - a.taps_tmem) * cin * 256 / 16;
+        for (int i = threadIdx.x; i < n16; i += blockDim.x)
+            reinterpret_cast<uint4 *>(wsm)[i] = a.wpack_smem[i];
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     fence_before();
@@ -313,44 +343,37 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     const uint32_t smem_base = smem_u32(smem);
 
     if (is_prod) {
-        const int pt = threadIdx.x - 32 * NUM_EPI_WARPS;  // 0..127
+        const int pidx = threadIdx.x - 32 * NUM_EPI_WARPS;  // 0..255
+        const int grp = pidx / PROD_GROUP;                 // items it with it % 2 == grp
+        const int pt = pidx % PROD_GROUP;
         const int nchunks = cin / 8;
         const int qblocks = (TILE + a.halo_rows) / 8;
         const int pairs = nchunks * qblocks;
         int it = 0;
         for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
+            if ((it & 1) != grp) continue;
             const int s = it % stages;
             const uint32_t ph = (uint32_t)(it / stages) & 1u;
             if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_flag, a.status)) break;
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
             unsigned char *stage = stages_sm + (size_t)s * a.stage_bytes;
-            constexpr int PT = 32 * NUM_PROD_WARPS;
-            for (int p = pt; p < pairs; p += 2 * PT) {
-                // two 8x8 blocks in flight before either is transposed
-                uint4 v[2][8];
-                const bool second = p + PT < pairs;
-                load_block(a, b, tile, p % nchunks, p / nchunks, v[0]);
-                if (second) load_block(a, b, tile, (p + PT) % nchunks, (p + PT) / nchunks, v[1]);
+            // up to three 8x8 blocks per thread in flight at once (one round trip
+            // for Cin = 128: 16 chunks x 17 row blocks = 272 blocks / 128 threads)
+            for (int p = pt; p < pairs; p += 3 * PROD_GROUP) {
+                uint4 v[3][8];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (h == 1 && !second) break;
-                    const int ph2 = p + h * PT;
-                    const int c = ph2 % nchunks;
-                    const int q = ph2 / nchunks;
-                    const uint32_t *w = reinterpret_cast<const uint32_t *>(v[h]);
-                    unsigned char *dst = stage + ((size_t)c * a.chunk_rows + 8 * q) * 16;
+                for (int h = 0; h < 3; ++h) {
+                    const int ph2 = p + h * PROD_GROUP;
+                    if (ph2 < pairs) load_block(a, b, tile, ph2 % nchunks, ph2 / nchunks, v[h]);
+                }
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const int wsel = i / 2;
-                        const uint32_t sel = (i & 1) ? 0x7632u : 0x5410u;
-                        uint4 o;
-                        o.x = __byte_perm(w[0 * 4 + wsel], w[1 * 4 + wsel], sel);
-                        o.y = __byte_perm(w[2 * 4 + wsel], w[3 * 4 + wsel], sel);
-                        o.z = __byte_perm(w[4 * 4 + wsel], w[5 * 4 + wsel], sel);
-                        o.w = __byte_perm(w[6 * 4 + wsel], w[7 * 4 + wsel], sel);
-                        *reinterpret_cast<uint4 *>(dst + (size_t)i * 16) = o;
-                    }
+                for (int h = 0; h < 3; ++h) {
+                    const int ph2 = p + h * PROD_GROUP;
+                    if (ph2 < pairs)
+                        store_block(stage + ((size_t)(ph2 % nchunks) * a.chunk_rows +
+                                             8 * (ph2 / nchunks)) * 16,
+                                    v[h]);
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -509,7 +532,10 @@ bkma_status conv_tc_plan_init(ConvPlanImpl &p) {
     p.tensor = true;
     p.TL = tc::TILE;
     p.ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
-    p.halo_bytes = 2 * (size_t)(d.batch * p.ntiles * d.cin * (d.ksize - 1));
+    p.halo_width = t.halo_rows;
+    p.halo_bytes = 2 * (size_t)(d.batch * p.ntiles * d.cin * p.halo_width);
+    p.wpack_bytes = (size_t)128 * 256 * 4 + (size_t)t.wsmem_bytes;
+    BKMA_CUDA_TRY(cudaMalloc(&p.d_wpack, p.wpack_bytes));
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
@@ -532,6 +558,11 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
         if (s != BKMA_OK) return s;
     }
     const TcLayout t = tc_layout(d);
+    uint32_t *tm_img = (uint32_t *)p.d_wpack;
+    uint32_t *sm_img = tm_img + 128 * 256;
+    tc::conv_tc_pack_weights<<<64, 256, 0, st>>>((const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout,
+                                                 (int)d.ksize, t.taps_tmem, tm_img, sm_img);
+    BKMA_CUDA_TRY(cudaGetLastError());
     tc::Args a;
     a.x = (const __nv_bfloat16 *)data;
     a.out = (__nv_bfloat16 *)(inplace ? data : out);
@@ -552,6 +583,8 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
     a.stages = t.stages;
     a.taps_tmem = t.taps_tmem;
     a.wsmem_bytes = t.wsmem_bytes;
+    a.wpack_tmem = tm_img;
+    a.wpack_smem = reinterpret_cast<const uint4 *>(sm_img);
     a.status = (int *)p.d_status;
     const size_t smem = (size_t)t.wsmem_bytes + (size_t)t.stages * t.stage_bytes;
     void (*kern)(tc::Args) = nullptr;
