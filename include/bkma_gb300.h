@@ -169,6 +169,14 @@ typedef struct bkma_adv_batch bkma_adv_batch;
 bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields, int32_t dtype,
                                   bkma_adv_batch **batch);
 bkma_status bkma_adv_batch_step(bkma_adv_batch *batch, int32_t nsteps, void *stream);
+/* Times the tile-model candidates (shared-memory cap per tile, threads per
+ * CTA) on the live fields - their contents advance by the timed steps - and
+ * keeps the fastest. */
+bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream);
+/* Chosen tiles: per field W (columns) and R (slabs) (arrays of nfields), the
+ * total tile count, threads per CTA and shared memory per CTA. */
+bkma_status bkma_adv_batch_tiles(const bkma_adv_batch *batch, int32_t *W, int32_t *R, int64_t *tiles,
+                                 int32_t *threads, int64_t *smem_bytes);
 /* Total cells over all fields, and kernel launches per step. */
 bkma_status bkma_adv_batch_info(const bkma_adv_batch *batch, int64_t *cells, int32_t *launches_per_step);
 bkma_status bkma_adv_batch_destroy(bkma_adv_batch *batch);

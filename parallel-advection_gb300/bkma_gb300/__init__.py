@@ -151,6 +151,66 @@ class AdvectionPlan:
             pass
 
 
+class AdvectionBatch:
+    """Many independent fields advanced by one persistent, graph-captured
+    launch per step. `fields`: dicts with keys data (CUDA tensor n0 x n1 x n2),
+    degree (3 or 5), weights ("reference" for degree 5, "lagrange"), dt, minX,
+    maxX, minVx, maxVx, velocity (optional array of n0)."""
+
+    def __init__(self, fields, dtype: str = "f32"):
+        arr = (_lib.AdvField * len(fields))()
+        self._keep = []
+        self.cells = 0
+        for i, f in enumerate(fields):
+            t = f["data"]
+            n0, n1, n2 = t.shape
+            a = arr[i]
+            a.data = t.data_ptr()
+            a.n0, a.n1, a.n2 = n0, n1, n2
+            a.degree = f.get("degree", 5)
+            a.weights = _W[f.get("weights", "reference" if a.degree == 5 else "lagrange")]
+            a.dt = f.get("dt", 1e-3)
+            a.minX, a.maxX = f.get("minX", 0.0), f.get("maxX", 1.0)
+            a.minVx, a.maxVx = f.get("minVx", -1.0), f.get("maxVx", 1.0)
+            v = f.get("velocity")
+            if v is not None:
+                v = np.ascontiguousarray(v, dtype=np.float64)
+                self._keep.append(v)
+                a.velocity = v.ctypes.data_as(C.POINTER(C.c_double))
+            self._keep.append(t)
+            self.cells += n0 * n1 * n2
+        self.nfields = len(fields)
+        h = C.c_void_p()
+        check(load().bkma_adv_batch_create(arr, len(fields), _DT[dtype], C.byref(h)))
+        self._h = h
+
+    def step(self, nsteps: int = 1, stream=None):
+        check(load().bkma_adv_batch_step(self._h, nsteps, _stream(stream)))
+
+    def autotune(self, stream=None):
+        check(load().bkma_adv_batch_autotune(self._h, _stream(stream)))
+        return self.tiles()
+
+    def tiles(self) -> dict:
+        W = (C.c_int32 * self.nfields)()
+        R = (C.c_int32 * self.nfields)()
+        nt, th, sm = C.c_int64(), C.c_int32(), C.c_int64()
+        check(load().bkma_adv_batch_tiles(self._h, W, R, C.byref(nt), C.byref(th), C.byref(sm)))
+        return {"W": list(W), "R": list(R), "tiles": nt.value, "threads": th.value,
+                "smem_bytes": sm.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bkma_adv_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _dtype_name(t) -> str:
     s = str(t.dtype)
     if "float32" in s:

@@ -82,6 +82,8 @@ SIGNATURES = {
     "bkma_adv_batch_create": (_st, [C.POINTER(AdvField), C.c_int32, C.c_int32, C.POINTER(_vp)]),
     "bkma_adv_batch_step": (_st, [_vp, C.c_int32, _vp]),
     "bkma_adv_batch_info": (_st, [_vp, _i64p, _i32p]),
+    "bkma_adv_batch_autotune": (_st, [_vp, _vp]),
+    "bkma_adv_batch_tiles": (_st, [_vp, _i32p, _i32p, _i64p, _i32p, _i64p]),
     "bkma_adv_batch_destroy": (_st, [_vp]),
     "bkma_conv_plan_create": (_st, [C.POINTER(ConvDesc), C.POINTER(_vp)]),
     "bkma_conv_plan_scratch_bytes": (_st, [_vp, _i64p]),

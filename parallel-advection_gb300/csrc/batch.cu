@@ -1,16 +1,320 @@
-// Batched uneven advection. Placeholder until the persistent kernel lands.
+// Batched uneven advection: many fields of different (n0, n1, n2), degree and
+// line velocities advanced by ONE persistent kernel launch per time step.
+//
+// Each field gets its own per-line tables (the same host precompute as a
+// single-field plan, so departure cells are bit-identical to the reference)
+// and a tile shape from a cost model: column tiles of W = 32/16/8/4 columns
+// when n2 allows, otherwise R whole slabs, each kept under a shared-memory cap
+// so several CTAs stay resident per SM. All tiles of all fields form one
+// work list; persistent CTAs pull tiles from a global counter (atomicAdd, no
+// waiting on other CTAs) and run the same staged-tile device code as the
+// single-field kernel. The counter reset and the launch are captured once in
+// a CUDA graph; a step is one graph launch. bkma_adv_batch_autotune times the
+// candidate caps and CTA sizes on the live fields (this stands in for the
+// reference's WorkItemDispatch / adjust_sizes_mem_limit sizing,
+// src/core/bkma_tools.hpp:74-107).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "adv_device.cuh"
 #include "adv_plan.cuh"
+#include "common.cuh"
+
+namespace bkma {
+
+template <typename T>
+struct BatchFieldDev {
+    AdvStagedArgs<T> args;
+    int npts;
+    int64_t tile0;  // first tile of this field in the work list
+};
+
+template <typename T>
+__global__ void __launch_bounds__(512) adv_batch_kernel(const BatchFieldDev<T> *__restrict__ fields,
+                                                        int nfields, int64_t ntiles,
+                                                        unsigned long long *counter) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ long long t_sh;
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    for (;;) {
+        if (threadIdx.x == 0) t_sh = (long long)atomicAdd(counter, 1ull);
+        __syncthreads();
+        const long long t = t_sh;
+        if (t >= ntiles) break;
+        int lo = 0, hi = nfields - 1;  // last field with tile0 <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (fields[mid].tile0 <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchFieldDev<T> &F = fields[lo];
+        const TileCoord tc = tile_of(t - F.tile0, F.args.lines, F.args.n2, F.args.R, F.args.W,
+                                     F.args.ncb);
+        if (F.npts == 6)
+            staged_tile<T, 6>(F.args, tc, sm);
+        else
+            staged_tile<T, 4>(F.args, tc, sm);
+        __syncthreads();  // shared memory is restaged by the next tile
+    }
+}
+
+namespace {
+
+struct BatchImpl {
+    int dtype = BKMA_F32;
+    int esize = 4;
+    std::vector<bkma_adv_plan *> plans;
+    std::vector<void *> data;
+    std::vector<int> W, R;
+    void *d_fields = nullptr;
+    unsigned long long *d_counter = nullptr;
+    int nfields = 0;
+    int64_t ntiles = 0, cells = 0;
+    size_t smem = 0;
+    int threads = 256, grid = 0;
+    size_t cap = 48 * 1024;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cs = nullptr;
+
+    ~BatchImpl() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (cs) cudaStreamDestroy(cs);
+        cudaFree(d_fields);
+        cudaFree(d_counter);
+        for (auto *p : plans) bkma_adv_plan_destroy(p);
+    }
+};
+
+// Tile of one field under a shared-memory cap.
+void choose_tile(const AdvPlanImpl &p, size_t cap, int &W, int &R) {
+    const int64_t n2 = p.desc.n2;
+    W = (int)n2;
+    R = 1;
+    if (n2 >= 8) {
+        for (int w : {32, 16, 8, 4}) {
+            if (w <= n2 && p.smem_bytes(w, 1) <= cap) {
+                W = w;
+                return;
+            }
+        }
+        W = 4;
+        return;
+    }
+    const size_t per = p.smem_bytes((int)n2, 1);
+    R = (int)std::max<size_t>(1, cap / std::max<size_t>(per, 1));
+    R = (int)std::min<int64_t>(R, p.lines);
+}
+
+template <typename T>
+bkma_status build_batch(BatchImpl &b, cudaStream_t st) {
+    std::vector<BatchFieldDev<T>> f((size_t)b.nfields);
+    b.ntiles = 0;
+    b.smem = 0;
+    for (int i = 0; i < b.nfields; ++i) {
+        AdvPlanImpl &p = plan_impl(b.plans[(size_t)i]);
+        int W, R;
+        choose_tile(p, b.cap, W, R);
+        b.W[(size_t)i] = W;
+        b.R[(size_t)i] = R;
+        AdvStagedArgs<T> &a = f[(size_t)i].args;
+        a.src = (const T *)b.data[(size_t)i];
+        a.dst = (T *)b.data[(size_t)i];
+        a.n1 = p.desc.n1;
+        a.n2 = p.desc.n2;
+        a.lines = p.lines;
+        a.W = W;
+        a.R = R;
+        a.ncb = p.ncb(W);
+        const int64_t es = b.esize;
+        const bool al = (uintptr_t)b.data[(size_t)i] % 16 == 0;
+        a.vec_ok = (W >= p.desc.n2) ? (al && (p.desc.n1 * p.desc.n2 * es) % 16 == 0)
+                                    : (al && (p.desc.n2 * es) % 16 == 0 && (W * es) % 16 == 0);
+        a.base = p.d_base;
+        a.w = (const T *)p.d_w;
+        a.exc_index = p.d_exc_index;
+        a.exc = (const AdvExcCell<T> *)p.d_exc;
+        f[(size_t)i].npts = p.npts;
+        f[(size_t)i].tile0 = b.ntiles;
+        b.ntiles += p.tiles(W, R);
+        b.smem = std::max(b.smem, p.smem_bytes(W, R));
+    }
+    if (!b.d_fields) BKMA_CUDA_TRY(cudaMalloc(&b.d_fields, sizeof(BatchFieldDev<T>) * f.size()));
+    BKMA_CUDA_TRY(cudaMemcpy(b.d_fields, f.data(), sizeof(BatchFieldDev<T>) * f.size(),
+                             cudaMemcpyHostToDevice));
+    auto kern = adv_batch_kernel<T>;
+    BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b.smem));
+    int per_sm = 0, dev = 0, sms = 0;
+    BKMA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, b.threads, b.smem));
+    cudaGetDevice(&dev);
+    BKMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (per_sm < 1) return fail(BKMA_ERR_UNSUPPORTED, "batched tile does not fit an SM");
+    b.grid = (int)std::min<int64_t>((int64_t)per_sm * sms, b.ntiles);
+    // capture: counter reset + persistent launch
+    if (b.exec) {
+        cudaGraphExecDestroy(b.exec);
+        b.exec = nullptr;
+    }
+    if (!b.cs) BKMA_CUDA_TRY(cudaStreamCreateWithFlags(&b.cs, cudaStreamNonBlocking));
+    (void)st;
+    cudaGraph_t g = nullptr;
+    BKMA_CUDA_TRY(cudaStreamBeginCapture(b.cs, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), b.cs);
+    kern<<<b.grid, b.threads, b.smem, b.cs>>>((const BatchFieldDev<T> *)b.d_fields, b.nfields,
+                                             b.ntiles, b.d_counter);
+    cudaError_t e = cudaStreamEndCapture(b.cs, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
+    e = cudaGraphInstantiate(&b.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "batch graph instantiate");
+    return BKMA_OK;
+}
+
+bkma_status rebuild(BatchImpl &b, cudaStream_t st) {
+    return b.dtype == BKMA_F32 ? build_batch<float>(b, st) : build_batch<double>(b, st);
+}
+
+}  // namespace
+}  // namespace bkma
+
+struct bkma_adv_batch {
+    bkma::BatchImpl impl;
+};
+
+using namespace bkma;
 
 extern "C" {
-bkma_status bkma_adv_batch_create(const bkma_adv_field *, int32_t, int32_t, bkma_adv_batch **b) {
-    if (b) *b = nullptr;
-    return bkma::fail(BKMA_ERR_UNSUPPORTED, "batched advection not built yet");
+
+bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields, int32_t dtype,
+                                  bkma_adv_batch **batch) {
+    BKMA_CHECK_ARG(fields && batch && nfields > 0, "bkma_adv_batch_create: bad arguments");
+    BKMA_CHECK_ARG(dtype == BKMA_F32 || dtype == BKMA_F64, "dtype must be BKMA_F32 or BKMA_F64");
+    *batch = nullptr;
+    auto *bb = new (std::nothrow) bkma_adv_batch;
+    if (!bb) return fail(BKMA_ERR_INVALID_ARG, "out of host memory");
+    BatchImpl &b = bb->impl;
+    b.dtype = dtype;
+    b.esize = dtype == BKMA_F32 ? 4 : 8;
+    b.nfields = nfields;
+    b.W.assign((size_t)nfields, 0);
+    b.R.assign((size_t)nfields, 1);
+    for (int i = 0; i < nfields; ++i) {
+        const bkma_adv_field &f = fields[i];
+        if (!f.data) {
+            delete bb;
+            return fail(BKMA_ERR_INVALID_ARG, "field " + std::to_string(i) + ": null data");
+        }
+        if (f.degree != 3 && f.degree != 5) {
+            delete bb;
+            return fail(BKMA_ERR_INVALID_ARG, "field " + std::to_string(i) + ": degree must be 3 or 5");
+        }
+        bkma_adv_desc d{};
+        d.n0 = f.n0;
+        d.n1 = f.n1;
+        d.n2 = f.n2;
+        d.dtype = dtype;
+        d.degree = f.degree;
+        d.weights = f.weights;
+        d.impl = BKMA_ADV_STAGED;
+        d.inplace = 1;
+        d.dt = f.dt;
+        d.minX = f.minX;
+        d.maxX = f.maxX;
+        d.minVx = f.minVx;
+        d.maxVx = f.maxVx;
+        d.velocity = f.velocity;
+        bkma_adv_plan *p = nullptr;
+        bkma_status s = bkma_adv_plan_create(&d, &p);
+        if (s != BKMA_OK) {
+            const std::string m = bkma_last_error();
+            delete bb;
+            return fail(s, "field " + std::to_string(i) + ": " + m);
+        }
+        b.plans.push_back(p);
+        b.data.push_back(f.data);
+        b.cells += f.n0 * f.n1 * f.n2;
+    }
+    cudaError_t e = cudaMalloc(&b.d_counter, sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        delete bb;
+        return cuda_fail(e, "batch counter");
+    }
+    bkma_status s = rebuild(b, nullptr);
+    if (s != BKMA_OK) {
+        delete bb;
+        return s;
+    }
+    *batch = bb;
+    return BKMA_OK;
 }
-bkma_status bkma_adv_batch_step(bkma_adv_batch *, int32_t, void *) {
-    return bkma::fail(BKMA_ERR_UNSUPPORTED, "batched advection not built yet");
+
+bkma_status bkma_adv_batch_step(bkma_adv_batch *batch, int32_t nsteps, void *stream) {
+    BKMA_CHECK_ARG(batch && nsteps >= 0, "bkma_adv_batch_step: bad arguments");
+    BatchImpl &b = batch->impl;
+    for (int i = 0; i < nsteps; ++i) BKMA_CUDA_TRY(cudaGraphLaunch(b.exec, (cudaStream_t)stream));
+    return BKMA_OK;
 }
-bkma_status bkma_adv_batch_info(const bkma_adv_batch *, int64_t *, int32_t *) {
-    return bkma::fail(BKMA_ERR_UNSUPPORTED, "batched advection not built yet");
+
+bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream) {
+    BKMA_CHECK_ARG(batch, "null argument");
+    BatchImpl &b = batch->impl;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    BKMA_CUDA_TRY(cudaEventCreate(&e0));
+    BKMA_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    size_t best_cap = b.cap;
+    int best_thr = b.threads;
+    for (size_t cap : {24 * 1024, 32 * 1024, 48 * 1024, 64 * 1024, 96 * 1024}) {
+        for (int thr : {256, 512}) {
+            b.cap = cap;
+            b.threads = thr;
+            if (rebuild(b, st) != BKMA_OK) continue;
+            cudaGraphLaunch(b.exec, st);  // warm-up
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < 2; ++r) cudaGraphLaunch(b.exec, st);
+            cudaEventRecord(e1, st);
+            BKMA_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                best_cap = cap;
+                best_thr = thr;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b.cap = best_cap;
+    b.threads = best_thr;
+    return rebuild(b, st);
 }
-bkma_status bkma_adv_batch_destroy(bkma_adv_batch *) { return BKMA_OK; }
+
+bkma_status bkma_adv_batch_info(const bkma_adv_batch *batch, int64_t *cells, int32_t *launches_per_step) {
+    BKMA_CHECK_ARG(batch, "null argument");
+    if (cells) *cells = batch->impl.cells;
+    if (launches_per_step) *launches_per_step = 1;
+    return BKMA_OK;
 }
+
+bkma_status bkma_adv_batch_tiles(const bkma_adv_batch *batch, int32_t *W, int32_t *R, int64_t *tiles,
+                                 int32_t *threads, int64_t *smem_bytes) {
+    BKMA_CHECK_ARG(batch, "null argument");
+    const BatchImpl &b = batch->impl;
+    for (int i = 0; i < b.nfields; ++i) {
+        if (W) W[i] = b.W[(size_t)i];
+        if (R) R[i] = b.R[(size_t)i];
+    }
+    if (tiles) *tiles = b.ntiles;
+    if (threads) *threads = b.threads;
+    if (smem_bytes) *smem_bytes = (int64_t)b.smem;
+    return BKMA_OK;
+}
+
+bkma_status bkma_adv_batch_destroy(bkma_adv_batch *batch) {
+    delete batch;
+    return BKMA_OK;
+}
+
+}  // extern "C"
