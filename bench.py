@@ -36,7 +36,7 @@ CFG_STEPS = 50
 METRIC = "advection GCells/s (FP32 storage, FP64 foot-point, degree 5)"
 UNIT = "GCells/s"
 WORKLOAD = "large single advection FP32 2048x1024x512, degree 5, 50 steps"
-PROFILE_JSON = os.path.join(ROOT, "profiles", "adv_staged_f32_2048x1024x512.json")
+PROFILE_JSON = os.path.join(ROOT, "profiles", "adv_tma_f32_2048x1024x512.json")
 
 
 def velocities(n0: int):
