@@ -220,6 +220,24 @@ bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const voi
 bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream);
 bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan);
 
+/* In-place BF16 tensor-core conv1d (torch semantics, cin = cout = channels,
+ * data (batch, channels, length), weight (channels, channels, ksize), bias
+ * (channels) or NULL) that allocates nothing. No counterpart in the
+ * reference: it exists for callers that must not call cudaMalloc while they
+ * run - code recorded into a replayable stream capture, runtimes that give all
+ * device memory to their own pool at start-up, and loops that cannot afford
+ * an allocation's implicit synchronization. Its scratch is one 16 MiB device
+ * array inside the library (held by every GPU that loads it until exit):
+ * 512 KiB for packed weights and 15.5 MiB for the halo snapshot, so
+ * batch * ceil((length-ksize+1)/128) * channels * 2 * max(8, round_up(ksize-1, 8))
+ * bytes must stay within 16252672; larger shapes get BKMA_ERR_INVALID_ARG
+ * (split the batch, or use bkma_conv_run). The first call on a device looks the array's address up,
+ * so make it before any stream capture. Calls share the array: calls that
+ * overlap on the GPU race, and a device-side wait timeout is not reported. */
+bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *weight, const void *bias,
+                                             int64_t batch, int64_t channels, int64_t length,
+                                             int64_t ksize, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

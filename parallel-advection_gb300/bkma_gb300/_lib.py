@@ -90,6 +90,8 @@ SIGNATURES = {
     "bkma_conv_run": (_st, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "bkma_conv_plan_status": (_st, [_vp, _vp]),
     "bkma_conv_plan_destroy": (_st, [_vp]),
+    "bkma_conv1d_bf16_inplace_noalloc": (_st, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64,
+                                               C.c_int64, _vp]),
 }
 
 _LIB = None

@@ -172,6 +172,23 @@ using namespace bkma;
 
 namespace bkma {
 
+// 16-bit halo snapshot into caller-provided memory (no plan): the same
+// kernels as conv_halo_prepass, for the allocation-free conv1d entry point.
+bkma_status conv_halo_bf16_into(const bkma_conv_desc &d, const void *x, void *halo, int TL,
+                                int64_t ntiles, int hw, cudaStream_t st) {
+    const int blocks = 152 * 4;
+    if (hw % 8 == 0 && TL % 8 == 0 && d.length % 8 == 0 && (uintptr_t)x % 16 == 0 &&
+        (uintptr_t)halo % 16 == 0)
+        conv_halo_kernel_v8<<<blocks, 256, 0, st>>>((const uint16_t *)x, (uint16_t *)halo, d.batch,
+                                                    d.cin, d.length, (int)d.ksize, TL, ntiles, hw);
+    else
+        conv_halo_kernel<uint16_t><<<blocks, 256, 0, st>>>((const uint16_t *)x, (uint16_t *)halo,
+                                                          d.batch, d.cin, d.length, (int)d.ksize,
+                                                          TL, ntiles, hw);
+    BKMA_CUDA_TRY(cudaGetLastError());
+    return BKMA_OK;
+}
+
 bkma_status conv_halo_prepass(ConvPlanImpl &p, const void *x, cudaStream_t st) {
     const bkma_conv_desc &d = p.desc;
     const int blocks = 152 * 4;

@@ -55,6 +55,11 @@ struct ConvPlanImpl {
 };
 
 bkma_status conv_halo_prepass(ConvPlanImpl &p, const void *x, cudaStream_t st);
+bkma_status conv_halo_bf16_into(const bkma_conv_desc &d, const void *x, void *halo, int TL,
+                                int64_t ntiles, int hw, cudaStream_t st);
+bkma_status conv_tc_scratch_need(const bkma_conv_desc &d, size_t *halo_bytes, size_t *wpack_bytes);
+bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w, const void *bias,
+                             void *halo, void *wpack, int *status, cudaStream_t st);
 bkma_status conv_tc_plan_init(ConvPlanImpl &p);
 bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, const void *bias,
                         cudaStream_t st);

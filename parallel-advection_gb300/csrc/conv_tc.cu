@@ -608,3 +608,89 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
 }
 
 }  // namespace bkma
+
+namespace bkma {
+
+// Scratch needs of the tensor path for one in-place call: the halo snapshot
+// and the packed weights (bytes, each rounded to 256).
+bkma_status conv_tc_scratch_need(const bkma_conv_desc &d, size_t *halo_bytes, size_t *wpack_bytes) {
+    if (d.cout > 128 || d.cin > 128 || d.cin % 16 != 0 || d.length % 8 != 0)
+        return fail(BKMA_ERR_UNSUPPORTED,
+                    "tensor path: cin = cout <= 128, cin a multiple of 16, length a multiple of 8");
+    const TcLayout t = tc_layout(d);
+    if (t.stages < 2)
+        return fail(BKMA_ERR_UNSUPPORTED,
+                    "tensor path: ksize*cin too large for on-chip weights (TMEM + shared memory)");
+    const int64_t ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
+    *halo_bytes = ((size_t)2 * (size_t)(d.batch * ntiles * d.cin * t.halo_rows) + 255) / 256 * 256;
+    *wpack_bytes = ((size_t)128 * 256 * 4 + (size_t)t.wsmem_bytes + 255) / 256 * 256;
+    return BKMA_OK;
+}
+
+// In-place BF16 tensor-core conv1d with caller-provided scratch (halo
+// snapshot, packed weights, status word): the same three kernels as
+// conv_tc_run, launched without a plan and without allocating.
+bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w, const void *bias,
+                             void *halo, void *wpack, int *status, cudaStream_t st) {
+    const auto misaligned = [](const void *q) { return q && ((uintptr_t)q % 16) != 0; };
+    if (misaligned(data) || misaligned(w) || misaligned(halo) || misaligned(wpack))
+        return fail(BKMA_ERR_INVALID_ARG, "tensor path: data, weight and scratch must be 16-byte aligned");
+    const TcLayout t = tc_layout(d);
+    const int64_t ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
+    if (d.ksize > 1) {
+        bkma_status s = conv_halo_bf16_into(d, data, halo, tc::TILE, ntiles, t.halo_rows, st);
+        if (s != BKMA_OK) return s;
+    }
+    uint32_t *tm_img = (uint32_t *)wpack;
+    uint32_t *sm_img = tm_img + 128 * 256;
+    tc::conv_tc_pack_weights<<<64, 256, 0, st>>>((const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout,
+                                                 (int)d.ksize, t.taps_tmem, tm_img, sm_img);
+    BKMA_CUDA_TRY(cudaGetLastError());
+    tc::Args a;
+    a.x = (const __nv_bfloat16 *)data;
+    a.out = (__nv_bfloat16 *)data;
+    a.w = (const __nv_bfloat16 *)w;
+    a.bias = (const __nv_bfloat16 *)bias;
+    a.halo = d.ksize > 1 ? (const __nv_bfloat16 *)halo : nullptr;
+    a.B = (int)d.batch;
+    a.cin = (int)d.cin;
+    a.cout = (int)d.cout;
+    a.K = (int)d.ksize;
+    a.L = d.length;
+    a.lout = d.length - d.ksize + 1;
+    a.out_stride = d.length;
+    a.ntiles = (int)ntiles;
+    a.halo_rows = t.halo_rows;
+    a.chunk_rows = t.chunk_rows;
+    a.stage_bytes = t.stage_bytes;
+    a.stages = t.stages;
+    a.taps_tmem = t.taps_tmem;
+    a.wsmem_bytes = t.wsmem_bytes;
+    a.wpack_tmem = tm_img;
+    a.wpack_smem = reinterpret_cast<const uint4 *>(sm_img);
+    a.status = status;
+    const size_t smem = (size_t)t.wsmem_bytes + (size_t)t.stages * t.stage_bytes;
+    void (*kern)(tc::Args) = nullptr;
+    switch (a.cin / 16) {
+    case 1: kern = tc::conv_tc_kernel<1>; break;
+    case 2: kern = tc::conv_tc_kernel<2>; break;
+    case 3: kern = tc::conv_tc_kernel<3>; break;
+    case 4: kern = tc::conv_tc_kernel<4>; break;
+    case 5: kern = tc::conv_tc_kernel<5>; break;
+    case 6: kern = tc::conv_tc_kernel<6>; break;
+    case 7: kern = tc::conv_tc_kernel<7>; break;
+    case 8: kern = tc::conv_tc_kernel<8>; break;
+    default: return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be 16..128");
+    }
+    BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int dev = 0, sms = 0;
+    BKMA_CUDA_TRY(cudaGetDevice(&dev));
+    BKMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t items = (int64_t)a.B * a.ntiles;
+    const int grid = (int)std::min<int64_t>(sms, items);
+    kern<<<grid, tc::THREADS, smem, st>>>(a);
+    BKMA_CUDA_TRY(cudaGetLastError());
+    return BKMA_OK;
+}
+
+}  // namespace bkma

@@ -1,0 +1,71 @@
+"""The allocation-free conv1d entry point, called through the C ABI.
+
+bkma_conv1d_bf16_inplace_noalloc serves callers that must not allocate device
+memory while they run (replayable stream captures, runtimes that own the whole
+device heap, allocation-free loops); it keeps its scratch in a fixed device
+array inside the library. This file is collected last so that a run stopping
+at the first failure has already run every other test.
+
+Its output must equal the plan-based entry point's (bkma_conv_run): the same
+kernels run in the same order, so the check is exact; the tensor-path
+tolerance of the other tests (1e-2 * max|ref| against FP64) is also asserted.
+Two calls in a row use different inputs, so a stale scratch array would show.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(cuda, seed, B, Ch, L, K):
+    import torch
+    g = torch.Generator(device=cuda).manual_seed(seed)
+    s = 1.0 / (Ch * K) ** 0.5
+    x = ((torch.rand((B, Ch, L), generator=g, device=cuda) * 2 - 1) * s).to(torch.bfloat16)
+    w = ((torch.rand((Ch, Ch, K), generator=g, device=cuda) * 2 - 1) * s).to(torch.bfloat16)
+    b = ((torch.rand((Ch,), generator=g, device=cuda) * 2 - 1) * s).to(torch.bfloat16)
+    return x, w, b
+
+
+def _noalloc(lib, x, w, b, stream):
+    B, Ch, L = x.shape
+    K = w.shape[2]
+    return lib.bkma_conv1d_bf16_inplace_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
+                                                C.c_void_p(b.data_ptr()), B, Ch, L, K,
+                                                C.c_void_p(stream))
+
+
+def test_noalloc_matches_plan_entry_point_twice(bkma, cuda, oracle):
+    import torch
+    lib = bkma.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    shapes = [(2, 128, 1024, 7), (3, 64, 2048, 5)]
+    for call, (B, Ch, L, K) in enumerate(shapes):
+        x, w, b = _inputs(cuda, 100 + call, B, Ch, L, K)
+        want = x.clone()
+        plan = bkma.Conv1dPlan(B, Ch, Ch, L, K, dtype="bf16", impl="tensor")
+        plan.run(want, w, b)
+        plan.status()
+        got = x.clone()
+        assert _noalloc(lib, got, w, b, stream) == 0, lib.bkma_last_error().decode()
+        torch.cuda.synchronize()
+        assert torch.equal(got, want), f"call {call}: differs from bkma_conv_run"
+        ref = oracle.conv_torch(x.double().cpu().numpy(), w.double().cpu().numpy(),
+                                b.double().cpu().numpy())
+        err = np.abs(got.double().cpu().numpy()[:, :, :L - K + 1] - ref).max()
+        assert err <= 1e-2 * np.abs(ref).max()
+
+
+def test_noalloc_rejects_shapes_beyond_its_array(bkma, cuda):
+    import torch
+    lib = bkma.load()
+    x = torch.zeros(8, 16, 16, dtype=torch.bfloat16, device=cuda)  # pointer only
+    w = torch.zeros(16, 16, 7, dtype=torch.bfloat16, device=cuda)
+    # 1000 rows x 64 tiles x 128 channels x 16 bytes = 131 MB > 15.5 MiB: rejected
+    # before any device work, so the small buffers above are never touched
+    rc = lib.bkma_conv1d_bf16_inplace_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
+                                              None, 1000, 128, 8192, 7, None)
+    assert rc == 1
+    assert "split the batch" in lib.bkma_last_error().decode()
