@@ -81,7 +81,9 @@ def build_host_apps(force: bool = False) -> list[str]:
     hdrs = glob.glob(os.path.join(HOST, "*.hpp")) + [os.path.join(INCLUDE, "bkma_gb300.h")]
     out = []
     cxx = os.environ.get("CXX", "g++")
-    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+    cuda_root = os.path.dirname(os.path.dirname(nvcc()))
+    cuda_inc = os.path.join(cuda_root, "include")
+    cuda_lib = os.path.join(cuda_root, "lib64")
     for app in apps:
         name = os.path.basename(app)[len("app_"):-len(".cpp")]
         exe = os.path.join(BIN, name)
@@ -89,7 +91,8 @@ def build_host_apps(force: bool = False) -> list[str]:
         if force or not os.path.exists(exe) or os.path.getmtime(exe) < _newest(deps):
             _run([cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-I", INCLUDE, "-I", HOST,
                   "-I", cuda_inc, app] + common +
-                 ["-o", exe, "-L", PKG_ROOT, "-lbkma_gb300", "-Wl,-rpath,$ORIGIN/.."])
+                 ["-o", exe, "-L", PKG_ROOT, "-lbkma_gb300", "-L", cuda_lib, "-lcudart",
+                  "-Wl,-rpath,$ORIGIN/..", "-Wl,-rpath," + cuda_lib])
         out.append(exe)
     return out
 
