@@ -37,6 +37,17 @@ def _stream(stream) -> int | None:
     return stream.cuda_stream
 
 
+def shard_lines(n0: int, rank: int, world: int) -> tuple[int, int]:
+    """Contiguous slab of velocity lines for one rank: (i0_offset, i0_count).
+    Lines are independent, so shards need no exchange; the first n0 % world
+    ranks take one extra line."""
+    if world < 1 or not (0 <= rank < world) or n0 < world:
+        raise ValueError("need world >= 1, 0 <= rank < world and n0 >= world")
+    base, extra = divmod(n0, world)
+    offset = rank * base + min(rank, extra)
+    return offset, base + (1 if rank < extra else 0)
+
+
 def impl_from_name(name: str) -> tuple[int, bool]:
     """impl_selector (src/tools/impl_selector.hpp:31-49) over the C ABI."""
     impl, inplace = C.c_int32(), C.c_int32()
