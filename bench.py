@@ -286,6 +286,7 @@ def run_gpu(args):
         result["cpu_baseline"] = cpu_baseline_sample(os.cpu_count() or 1)
         result["conv1d"] = conv_block(bkma_gb300, dev)
         result["batched"] = batched_block(bkma_gb300, dev)
+        result["learned"] = learned_block(bkma_gb300, dev)
     if rank == 0:
         print(json.dumps(result))
     if dist is not None:
@@ -472,6 +473,82 @@ def batched_block(bkma_gb300, dev, nfields: int = 64, steps: int = 10):
     return out
 
 
+def learned_block(bkma_gb300, dev, steps: int = 100):
+    """Learned-stencil advection: the 4-point MLP stencil (1 -> 32 -> 32 -> 4,
+    GELU, FP32) trained on the GPU on 10^6 (shift, degree-9 Lagrange) samples of
+    random periodic lines (n1 = 1024), then applied to n0=1024 x n1=1024 x
+    n2=256 FP32 for 100 steps, next to the plain degree-5 kernel and degree-3
+    Lagrange (the same 4-point layout without the network). Accuracy is the RMS
+    error against the exact shifted solution of a band-limited initial field."""
+    import numpy as np
+    import torch
+    out = {"workload": "learned 4-point stencil vs degree 5 / degree 3, 1024x1024x256 FP32, "
+                       "100 steps"}
+    try:
+        n0, n1, n2 = 1024, 1024, 256
+        net = bkma_gb300.LearnedStencil(seed=SEED)
+        a, f4, t = bkma_gb300.LearnedStencil.samples(1_000_000, SEED)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss = net.train(a, f4, t, steps=2000, batch=8192, lr=3e-3)
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t0
+        va, vf, vt = bkma_gb300.LearnedStencil.samples(1 << 18, SEED, first=1 << 30)
+        w = net.infer(va)
+        mse_l = float(((w * vf).sum(1) - vt).double().pow(2).mean())
+        xs = 1.0 + va.double()
+        l3 = torch.stack([((xs - m1) * (xs - m2) * (xs - m3)) / ((j - m1) * (j - m2) * (j - m3))
+                          for j, (m1, m2, m3) in enumerate([(1, 2, 3), (0, 2, 3), (0, 1, 3),
+                                                            (0, 1, 2)])], 1)
+        mse_3 = float(((l3 * vf.double()).sum(1) - vt.double()).pow(2).mean())
+        del a, f4, t, va, vf, vt
+        vel = velocities(n0)
+        rng = np.random.default_rng(SEED)
+        modes = np.arange(1, 33)
+        am = rng.uniform(-1, 1, modes.size) / modes
+        bm = rng.uniform(-1, 1, modes.size) / modes
+
+        def f(x):
+            ph = 2 * np.pi * np.outer(x, modes)
+            return (np.cos(ph) * am + np.sin(ph) * bm).sum(1)
+
+        x = np.arange(n1) / n1
+        init = torch.tensor(f(x), dtype=torch.float32, device=dev)
+        kw = dict(dt=DT, minX=MINX, maxX=MAXX, minVx=-1.0, maxVx=1.0, velocity=vel)
+        plans = {"learned_4pt": net.plan_for(n0, n1, n2, **kw),
+                 "degree5_reference": bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f32", **kw),
+                 "degree3_lagrange": bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f32", degree=3,
+                                                              weights="lagrange", **kw)}
+        sample = np.arange(0, n0, 64)
+        st = torch.cuda.current_stream()
+        for name, plan in plans.items():
+            d = init[None, :, None].expand(n0, n1, n2).contiguous()
+            plan.step(d, nsteps=2)  # warm-up, then restart from the initial field
+            d.copy_(init[None, :, None].expand(n0, n1, n2))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            plan.step(d, nsteps=steps)
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            got = d[sample, :, 0].double().cpu().numpy()
+            err = 0.0
+            for r, i0 in enumerate(sample):
+                exact = f((x - vel[i0] * steps * DT) % 1.0)
+                err += ((got[r] - exact) ** 2).mean()
+            out[name] = {"gcells_s": n0 * n1 * n2 * steps / (ms / 1e3) / 1e9,
+                         "rms_err_vs_exact": (err / len(sample)) ** 0.5}
+            del d
+        out["training"] = {"samples": 1_000_000, "steps": 2000, "batch": 8192, "seconds": train_s,
+                           "last_batch_mse": loss, "held_out_mse_learned": mse_l,
+                           "held_out_mse_degree3": mse_3, "mse_ratio": mse_l / mse_3}
+    except Exception as e:  # reported, not hidden
+        out["error"] = repr(e)
+    torch.cuda.empty_cache()
+    return out
+
+
 def e2e(plan, dev, cells):
     """The same metric through the C ABI with a HOST field: every e2e step
     copies the field host->device, runs the 50 time steps and copies it back
@@ -508,7 +585,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip error/e2e/cpu/conv blocks")
     ap.add_argument("--n0", type=int, default=None, help="smaller field for profiling captures")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", default="advection", choices=["advection", "conv", "batched"],
+    ap.add_argument("--workload", default="advection", choices=["advection", "conv", "batched", "learned"],
                     help="conv: only the conv1d block, as its own JSON line")
     ap.add_argument("--conv-batch", type=int, default=256, help="smaller batch for captures")
     args = ap.parse_args()
@@ -517,10 +594,11 @@ def main():
         N0 = args.n0
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload == "batched" and args.impl != "reference":
+    if args.workload in ("batched", "learned") and args.impl != "reference":
         import torch
         import bkma_gb300
-        r = batched_block(bkma_gb300, torch.device("cuda", 0))
+        blk = batched_block if args.workload == "batched" else learned_block
+        r = blk(bkma_gb300, torch.device("cuda", 0))
         print(json.dumps(r))
         return 0 if "error" not in r else 1
     if args.workload == "conv" and args.impl != "reference":

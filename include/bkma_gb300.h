@@ -238,6 +238,40 @@ bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *weight, con
                                              int64_t batch, int64_t channels, int64_t length,
                                              int64_t ksize, void *stream);
 
+/* ------------------------------------------------------- learned stencil */
+/* A small MLP (1 -> 32 -> 32 -> 4, GELU, FP32) maps a line's fractional shift
+ * a in [0,1) to a corrected 4-point stencil w(a) = L3(a) + c(a) - mean(c(a))
+ * (L3: degree-3 Lagrange; the weights keep summing to one). No counterpart in
+ * the reference (which only has the fixed degree-5 stencil); the trained
+ * weights feed an advection plan created with BKMA_W_TABLE and degree 3
+ * through bkma_adv_plan_set_weights. Parameter layout (1252 floats):
+ * W1[32] b1[32] W2[32][32] b2[32] W3[4][32] b3[4]; the output layer starts at
+ * zero, so an untrained model is the degree-3 Lagrange stencil. */
+typedef struct bkma_mlp bkma_mlp;
+bkma_status bkma_mlp_create(uint64_t seed, bkma_mlp **mlp);
+/* Copy the 1252 parameters to (set = 0) or from (set = 1) a host array. */
+bkma_status bkma_mlp_params(bkma_mlp *mlp, float *host_params, int32_t set);
+/* Training samples first .. first+n-1 into device arrays alpha[n],
+ * taps4[n][4], target[n]: a random periodic line (48 Fourier modes with
+ * amplitudes U[-1,1]/m), its 4 nodes j-1..j+2 and the degree-9 Lagrange value
+ * at j + alpha. */
+bkma_status bkma_mlp_samples(int64_t n, uint64_t seed, int64_t first, float *alpha, float *taps4,
+                             float *target, void *stream);
+/* Mean squared error over all n samples and its gradient (host float[1252]). */
+bkma_status bkma_mlp_grad(bkma_mlp *mlp, const float *alpha, const float *taps4,
+                          const float *target, int64_t n, float *host_grad, double *host_loss,
+                          void *stream);
+/* `steps` Adam steps on random batches of `batch` samples drawn from the n
+ * samples, cosine learning rate from lr_max; host_loss gets the last batch's
+ * mean squared error. */
+bkma_status bkma_mlp_train(bkma_mlp *mlp, const float *alpha, const float *taps4,
+                           const float *target, int64_t n, int32_t steps, int32_t batch,
+                           float lr_max, uint64_t seed, double *host_loss, void *stream);
+/* Stencils of n shifts: device alpha[n] -> device weights[n][4]. */
+bkma_status bkma_mlp_infer(const bkma_mlp *mlp, const float *alpha, int64_t n, float *weights,
+                           void *stream);
+bkma_status bkma_mlp_destroy(bkma_mlp *mlp);
+
 #ifdef __cplusplus
 }
 #endif

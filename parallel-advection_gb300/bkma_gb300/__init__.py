@@ -222,6 +222,83 @@ class AdvectionBatch:
             pass
 
 
+class LearnedStencil:
+    """Learned 4-point stencil (bkma_mlp_*): training data, training, gradient
+    and inference all run in the library's CUDA kernels."""
+
+    NP = 1252
+
+    def __init__(self, seed: int = 0):
+        h = C.c_void_p()
+        check(load().bkma_mlp_create(seed, C.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def samples(n: int, seed: int, first: int = 0, device=None):
+        import torch
+        dev = device or torch.device("cuda", torch.cuda.current_device())
+        a = torch.empty(n, dtype=torch.float32, device=dev)
+        f4 = torch.empty(n, 4, dtype=torch.float32, device=dev)
+        t = torch.empty(n, dtype=torch.float32, device=dev)
+        check(load().bkma_mlp_samples(n, seed, first, a.data_ptr(), f4.data_ptr(), t.data_ptr(),
+                                      _stream(None)))
+        return a, f4, t
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.NP, dtype=np.float32)
+        check(load().bkma_mlp_params(self._h, p.ctypes.data, 0))
+        return p
+
+    def set_params(self, p):
+        q = np.ascontiguousarray(p, dtype=np.float32)
+        assert q.shape == (self.NP,)
+        check(load().bkma_mlp_params(self._h, q.ctypes.data, 1))
+
+    def grad(self, a, f4, t) -> tuple[float, np.ndarray]:
+        g = np.zeros(self.NP, dtype=np.float32)
+        loss = C.c_double()
+        check(load().bkma_mlp_grad(self._h, a.data_ptr(), f4.data_ptr(), t.data_ptr(), a.numel(),
+                                   g.ctypes.data, C.byref(loss), _stream(None)))
+        return loss.value, g
+
+    def train(self, a, f4, t, steps: int, batch: int = 4096, lr: float = 3e-3,
+              seed: int = 1) -> float:
+        loss = C.c_double()
+        check(load().bkma_mlp_train(self._h, a.data_ptr(), f4.data_ptr(), t.data_ptr(), a.numel(),
+                                    steps, batch, lr, seed, C.byref(loss), _stream(None)))
+        return loss.value
+
+    def infer(self, alpha):
+        import torch
+        out = torch.empty(alpha.numel(), 4, dtype=torch.float32, device=alpha.device)
+        check(load().bkma_mlp_infer(self._h, alpha.data_ptr(), alpha.numel(), out.data_ptr(),
+                                    _stream(None)))
+        return out
+
+    def plan_for(self, n0: int, n1: int, n2: int, **kw) -> "AdvectionPlan":
+        """An FP32 advection plan whose per-line 4-point weights come from the
+        network (degree-3 tap layout, the plan's own departure offsets)."""
+        import torch
+        plan = AdvectionPlan(n0, n1, n2, dtype="f32", degree=3, weights="table", **kw)
+        _, shifts = plan.line_table()
+        a = torch.tensor(shifts, dtype=torch.float32, device="cuda")
+        w = self.infer(a)
+        plan.set_weights(w)
+        torch.cuda.synchronize()
+        return plan
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bkma_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _dtype_name(t) -> str:
     s = str(t.dtype)
     if "float32" in s:

@@ -92,6 +92,14 @@ SIGNATURES = {
     "bkma_conv_plan_destroy": (_st, [_vp]),
     "bkma_conv1d_bf16_inplace_noalloc": (_st, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64,
                                                C.c_int64, _vp]),
+    "bkma_mlp_create": (_st, [C.c_uint64, C.POINTER(_vp)]),
+    "bkma_mlp_params": (_st, [_vp, _vp, C.c_int32]),
+    "bkma_mlp_samples": (_st, [C.c_int64, C.c_uint64, C.c_int64, _vp, _vp, _vp, _vp]),
+    "bkma_mlp_grad": (_st, [_vp, _vp, _vp, _vp, C.c_int64, _vp, _dp, _vp]),
+    "bkma_mlp_train": (_st, [_vp, _vp, _vp, _vp, C.c_int64, C.c_int32, C.c_int32, C.c_float,
+                             C.c_uint64, _dp, _vp]),
+    "bkma_mlp_infer": (_st, [_vp, _vp, C.c_int64, _vp, _vp]),
+    "bkma_mlp_destroy": (_st, [_vp]),
 }
 
 _LIB = None
