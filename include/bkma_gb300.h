@@ -252,7 +252,7 @@ bkma_status bkma_mlp_create(uint64_t seed, bkma_mlp **mlp);
 /* Copy the 1252 parameters to (set = 0) or from (set = 1) a host array. */
 bkma_status bkma_mlp_params(bkma_mlp *mlp, float *host_params, int32_t set);
 /* Training samples first .. first+n-1 into device arrays alpha[n],
- * taps4[n][4], target[n]: a random periodic line (48 Fourier modes with
+ * taps4[n][4], target[n]: a random periodic line (32 Fourier modes with
  * amplitudes U[-1,1]/m), its 4 nodes j-1..j+2 and the degree-9 Lagrange value
  * at j + alpha. */
 bkma_status bkma_mlp_samples(int64_t n, uint64_t seed, int64_t first, float *alpha, float *taps4,

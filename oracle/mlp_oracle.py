@@ -24,7 +24,7 @@ from scipy.special import erf
 
 NP = 1252
 OFF_W1, OFF_B1, OFF_W2, OFF_B2, OFF_W3, OFF_B3 = 0, 32, 64, 1088, 1120, 1248
-MODES = 48
+MODES = 32
 N1 = 1024
 PER_SAMPLE = 2 + 2 * MODES  # random draws per sample
 

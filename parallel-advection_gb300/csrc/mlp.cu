@@ -22,7 +22,7 @@ namespace mlp {
 
 constexpr int NP = 1252;
 constexpr int OW1 = 0, OB1 = 32, OW2 = 64, OB2 = 1088, OW3 = 1120, OB3 = 1248;
-constexpr int MODES = 48;
+constexpr int MODES = 32;
 constexpr int PER_SAMPLE = 2 + 2 * MODES;
 constexpr int N1 = 1024;
 constexpr int TB = 128;   // samples per block in the gradient kernel
