@@ -49,17 +49,18 @@ __global__ void __launch_bounds__(512) adv_plain(AdvPlainArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double *sm = reinterpret_cast<double *>(smem_raw);
     const TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, a.R, a.W, a.ncb);
-    const int sstride = slab_stride(a.n1, 0, tc.wc, 8);
-    stage_tile<double>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, 0, a.vec_ok,
-                       sstride);
+    const int ws = staged_row_stride(a.n2, tc.wc, 8);
+    const int sstride = slab_stride(a.n1, 0, ws, 8);
+    stage_tile<double>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, ws, 0, sstride);
     const int n1 = (int)a.n1;
     const int wc = tc.wc;
     const int total = n1 * wc;
     const uint64_t un1 = (uint64_t)a.n1;
     for (int s = 0; s < tc.nslab; ++s) {
         const int64_t line = tc.line0 + s;
-        const double *S = sm + (int64_t)s * sstride;
-        double *G = a.dst + line * a.n1 * a.n2 + tc.c0;
+        const int64_t g0 = line * a.n1 * a.n2 + tc.c0;
+        const double *S = sm + (int64_t)s * sstride + chunk_lead(a.src + g0);
+        double *G = a.dst + g0;
         const double vx = a.vx[line];
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
             const int r = idx / wc;
@@ -73,7 +74,7 @@ __global__ void __launch_bounds__(512) adv_plain(AdvPlainArgs a) {
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
                 const uint64_t id = (un1 + (uint64_t)(int64_t)ipos1 + (uint64_t)k) % un1;
-                value = dadd(value, dmul(coef[k], S[(int64_t)id * wc + c]));
+                value = dadd(value, dmul(coef[k], S[(int64_t)id * ws + c]));
             }
             G[(int64_t)r * a.n2 + c] = value;
         }
@@ -206,15 +207,6 @@ bkma_status upload_tables(AdvPlanImpl &p) {
     return BKMA_OK;
 }
 
-// 16-byte chunks are legal when the field base is aligned and every row
-// (column tiles) or every slab (whole-row tiles) starts on 16 bytes.
-bool vec_ok(const AdvPlanImpl &p, const void *src, int W) {
-    const int64_t es = p.esize;
-    if ((uintptr_t)src % 16 != 0) return false;
-    if (W >= p.desc.n2) return (p.desc.n1 * p.desc.n2 * es) % 16 == 0;
-    return ((p.desc.n2 * es) % 16 == 0) && ((int64_t)W * es % 16 == 0);
-}
-
 template <typename T, int NT>
 cudaError_t launch_staged_t(const AdvPlanImpl &p, const T *src, T *dst, int W, int R,
                             int threads, cudaStream_t st) {
@@ -227,7 +219,6 @@ cudaError_t launch_staged_t(const AdvPlanImpl &p, const T *src, T *dst, int W, i
     a.W = W;
     a.R = R;
     a.ncb = p.ncb(W);
-    a.vec_ok = vec_ok(p, src, W) ? 1 : 0;
     a.base = p.d_base;
     a.w = (const T *)p.d_w;
     a.exc_index = p.d_exc_index;
@@ -266,7 +257,6 @@ cudaError_t launch_plain(const AdvPlanImpl &p, const double *src, double *dst, i
     a.W = W;
     a.R = R;
     a.ncb = p.ncb(W);
-    a.vec_ok = vec_ok(p, src, W) ? 1 : 0;
     a.vx = p.d_vx;
     a.phys = p.phys;
     const size_t smem = p.smem_bytes(W, R);

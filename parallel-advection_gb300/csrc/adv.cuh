@@ -22,7 +22,6 @@ struct AdvStagedArgs {
     int64_t n1, n2, lines;
     int W, R;          // tile: W columns (i2) x R slabs (i0) x all n1 rows
     int64_t ncb;       // column blocks per slab
-    int vec_ok;        // 16-byte cp.async allowed
     const int32_t *base;       // [lines]
     const T *w;                // [lines][NT]
     const int32_t *exc_index;  // [lines]
@@ -47,15 +46,26 @@ struct AdvPlainArgs {
     int64_t n1, n2, lines;
     int W, R;
     int64_t ncb;
-    int vec_ok;
     const double *vx;  // [lines]
     AdvPhys phys;
 };
 
-// Shared-memory elements per staged slab, padded to 16 bytes.
-__host__ __device__ __forceinline__ int slab_stride(int64_t n1, int halo, int wc, int esize) {
-    const int e = (int)(n1 + halo) * wc;
+// Shared-memory row stride of a staged tile of wc columns. It is congruent
+// to n2 modulo 16 bytes, so every staged element keeps its global address's
+// position inside a 16-byte chunk and the aligned interior of each row is
+// copied in 16-byte pieces whatever n2 is.
+__host__ __device__ __forceinline__ int staged_row_stride(int64_t n2, int wc, int esize) {
     const int q = 16 / esize;
+    const int64_t gap = n2 - wc;
+    return wc + (int)(((gap % q) + q) % q);
+}
+
+// Shared-memory elements per staged slab: up to q-1 leading elements (the
+// slab start's offset inside its 16-byte chunk) plus rows of ws elements,
+// rounded up to 16 bytes.
+__host__ __device__ __forceinline__ int slab_stride(int64_t n1, int halo, int ws, int esize) {
+    const int q = 16 / esize;
+    const int e = q - 1 + (int)(n1 + halo) * ws;
     return (e + q - 1) / q * q;
 }
 

@@ -22,53 +22,79 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// Element offset of `p` inside its 16-byte chunk.
+template <typename T>
+__device__ __forceinline__ int chunk_lead(const T *p) {
+    return (int)(((uintptr_t)p / sizeof(T)) & (16 / sizeof(T) - 1));
+}
+
+// Block j of a run of `len` elements at `grow` -> `srow`: the elements of
+// the j-th 16-byte chunk of global memory that the run touches. A chunk that
+// lies wholly inside the run, with source and destination at the same place
+// inside their 16-byte chunks, moves as one 16-byte copy; the ragged ends
+// move element by element. Nothing outside the run is read.
+template <typename T>
+__device__ __forceinline__ void copy_block(T *srow, const T *grow, int len, int j) {
+    constexpr int Q = 16 / (int)sizeof(T);
+    const int a = j * Q - chunk_lead(grow);
+    const int lo = max(a, 0), hi = min(a + Q, len);
+    const bool cong = ((__cvta_generic_to_shared(srow) ^ (uintptr_t)grow) & 15) == 0;
+    if (cong && lo == a && hi == a + Q) {
+        cp_async(srow + a, grow + a, 16);
+    } else {
+        for (int e = lo; e < hi; ++e) cp_async(srow + e, grow + e, (int)sizeof(T));
+    }
+}
+
 // Stage rows [0, n1) plus halo rows [n1, n1+H) (copies of rows 0..H-1) of
-// `nslab` slabs x `wc` columns into shared memory laid out
-// [slab (stride sstride elements)][row][col]. When a tile holds whole rows
-// (wc == n2) each slab is one contiguous block in HBM and is copied flat.
-// vec_ok: the global field allows 16-byte chunks for this tile.
+// `nslab` slabs x `wc` columns into shared memory. Slab s starts at element
+// s*sstride; element (r, c) of the slab sits at chunk_lead(gs) + r*ws + c,
+// gs = the slab's first global element (see staged_row_stride). When a tile
+// holds whole rows (wc == n2) each slab is one contiguous run in HBM.
 template <typename T>
 __device__ __forceinline__ void stage_tile(T *sm, const T *__restrict__ g, int64_t n1,
                                            int64_t n2, int64_t line0, int nslab, int64_t c0,
-                                           int wc, int halo, int vec_ok, int sstride) {
-    constexpr int VEC = 16 / (int)sizeof(T);
+                                           int wc, int ws, int halo, int sstride) {
+    constexpr int Q = 16 / (int)sizeof(T);
     if (wc == n2) {
         const int body = (int)n1 * wc;
         const int hal = halo * wc;
-        const bool v = vec_ok && (body % VEC) == 0;
-        const int chunks = v ? body / VEC : body;
-        const int per_slab = chunks + hal;
-        const int total = nslab * per_slab;
-        for (int i = threadIdx.x; i < total; i += blockDim.x) {
-            const int s = i / per_slab;
-            const int j = i - s * per_slab;
+        const int nb = (body + 2 * Q - 2) / Q;  // chunks a run of `body` can touch
+        const int per_slab = nb + (hal + 2 * Q - 2) / Q;
+        for (int s = 0; s < nslab; ++s) {
             const T *gs = g + (line0 + s) * n1 * n2;
-            T *ss = sm + (int64_t)s * sstride;
-            if (j < chunks) {
-                if (v)
-                    cp_async(ss + j * VEC, gs + (int64_t)j * VEC, 16);
+            T *ss = sm + (int64_t)s * sstride + chunk_lead(gs);
+            for (int i = threadIdx.x; i < per_slab; i += blockDim.x) {
+                if (i < nb)
+                    copy_block(ss, gs, body, i);
                 else
-                    cp_async(ss + j, gs + j, (int)sizeof(T));
-            } else {
-                const int h = j - chunks;
-                cp_async(ss + body + h, gs + h, (int)sizeof(T));
+                    copy_block(ss + body, gs, hal, i - nb);
             }
         }
     } else {
+        // (row, chunk) walk with incremental indices. When n2 is a multiple
+        // of 16 bytes every row has the same lead and the chunk count is
+        // exact; otherwise it is the most a row of wc elements can touch.
         const int rows = (int)n1 + halo;
-        const int vec = (vec_ok && (wc % VEC) == 0) ? VEC : 1;
-        const int cpr = wc / vec;
+        const int lead0 = chunk_lead(g + line0 * n1 * n2 + c0);
+        const int cpr = (n2 % Q == 0) ? (lead0 + wc + Q - 1) / Q : (wc + 2 * Q - 2) / Q;
         const int per_slab = rows * cpr;
-        const int total = nslab * per_slab;
-        for (int i = threadIdx.x; i < total; i += blockDim.x) {
-            const int s = i / per_slab;
-            const int rem = i - s * per_slab;
-            const int r = rem / cpr;
-            const int ch = rem - r * cpr;
-            const int gr = r < n1 ? r : r - (int)n1;
-            const T *src = g + ((line0 + s) * n1 + gr) * n2 + c0 + (int64_t)ch * vec;
-            T *dst = sm + (int64_t)s * sstride + r * wc + ch * vec;
-            cp_async(dst, src, vec * (int)sizeof(T));
+        const int dr = blockDim.x / cpr, dch = blockDim.x - dr * cpr;
+        const int r_init = threadIdx.x / cpr, ch_init = threadIdx.x - r_init * cpr;
+        for (int s = 0; s < nslab; ++s) {
+            const T *gs = g + (line0 + s) * n1 * n2 + c0;
+            T *ss = sm + (int64_t)s * sstride + chunk_lead(gs);
+            int r = r_init, ch = ch_init;
+            for (int i = threadIdx.x; i < per_slab; i += blockDim.x) {
+                const int gr = r < n1 ? r : r - (int)n1;
+                copy_block(ss + r * ws, gs + (int64_t)gr * n2, wc, ch);
+                ch += dch;
+                r += dr;
+                if (ch >= cpr) {
+                    ch -= cpr;
+                    r += 1;
+                }
+            }
         }
     }
     cp_async_wait_all();
@@ -95,15 +121,68 @@ __device__ __forceinline__ TileCoord tile_of(int64_t t, int64_t lines, int64_t n
     return tc;
 }
 
+// FP32 rows of one slab, four columns per thread: NT float4 tap loads and
+// packed FMAs in the same order as the scalar loop below (d = f_k - f_c as
+// fma(f_c, -1, f_k), acc = fma(w_k, d, acc), out = f_c + acc), so the bits
+// match it. Needs wc and ws multiples of 4 and S on 16 bytes.
+template <int NT>
+__device__ __forceinline__ void rows_f32x4(const float *S, float *G, int n1, int64_t n2, int ws,
+                                           int wc, int base, const float *__restrict__ wl) {
+    constexpr int C = NT / 2 - 1;
+    const int ng = wc >> 2;  // column groups per row
+    const int rpp = blockDim.x / ng;
+    const int r0 = threadIdx.x / ng;
+    if (r0 >= rpp) return;
+    const int g4 = (threadIdx.x - r0 * ng) * 4;
+    float2 w2[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) w2[k] = make_float2(wl[k], wl[k]);
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const bool st_vec = (((uintptr_t)G | (uintptr_t)(n2 * 4)) & 15) == 0;
+    int rr = r0 + base;
+    if (rr >= n1) rr -= n1;
+    int rstep = rpp % n1;
+    for (int r = r0; r < n1; r += rpp) {
+        const float *p = S + rr * ws + g4;
+        float4 f[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) f[k] = *reinterpret_cast<const float4 *>(p + k * ws);
+        const float2 cl = make_float2(f[C].x, f[C].y);
+        const float2 ch = make_float2(f[C].z, f[C].w);
+        float2 al = make_float2(0.f, 0.f), ah = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            if (k == C) continue;
+            const float2 dl = __ffma2_rn(cl, m1, make_float2(f[k].x, f[k].y));
+            const float2 dh = __ffma2_rn(ch, m1, make_float2(f[k].z, f[k].w));
+            al = __ffma2_rn(w2[k], dl, al);
+            ah = __ffma2_rn(w2[k], dh, ah);
+        }
+        const float2 ol = __fadd2_rn(cl, al);
+        const float2 oh = __fadd2_rn(ch, ah);
+        float *q = G + (int64_t)r * n2 + g4;
+        if (st_vec) {
+            *reinterpret_cast<float4 *>(q) = make_float4(ol.x, ol.y, oh.x, oh.y);
+        } else {
+            q[0] = ol.x;
+            q[1] = ol.y;
+            q[2] = oh.x;
+            q[3] = oh.y;
+        }
+        rr += rstep;
+        if (rr >= n1) rr -= n1;
+    }
+}
+
 // One staged tile: `tc.nslab` slabs x `tc.wc` columns x all n1 rows of the
 // field `a.src` -> `a.dst` (may alias). Shared by the single-field kernel and
 // the batched persistent kernel, so both produce the same bits.
 template <typename T, int NT>
 __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const TileCoord &tc, T *sm) {
     constexpr int C = NT / 2 - 1;  // centre tap: the left node of the foot cell
-    const int sstride = slab_stride(a.n1, NT - 1, tc.wc, (int)sizeof(T));
-    stage_tile<T>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, NT - 1, a.vec_ok,
-                  sstride);
+    const int ws = staged_row_stride(a.n2, tc.wc, (int)sizeof(T));
+    const int sstride = slab_stride(a.n1, NT - 1, ws, (int)sizeof(T));
+    stage_tile<T>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, ws, NT - 1, sstride);
 
     const int n1 = (int)a.n1;
     const int wc = tc.wc;
@@ -114,11 +193,19 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
     const int c_init = threadIdx.x - r_init * wc;
     for (int s = 0; s < tc.nslab; ++s) {
         const int64_t line = tc.line0 + s;
-        const T *S = sm + (int64_t)s * sstride;
-        T *G = a.dst + line * a.n1 * a.n2 + tc.c0;
+        const int64_t g0 = line * a.n1 * a.n2 + tc.c0;
+        const int lead = chunk_lead(a.src + g0);
+        const T *S = sm + (int64_t)s * sstride + lead;
+        T *G = a.dst + g0;
         const int exc = a.exc_index[line];
         if (exc < 0) {
             const int base = a.base[line];
+            if constexpr (sizeof(T) == 4) {
+                if (((wc | ws | lead) & 3) == 0) {
+                    rows_f32x4<NT>(S, G, n1, a.n2, ws, wc, base, a.w + line * NT);
+                    continue;
+                }
+            }
             T w[NT];
 #pragma unroll
             for (int k = 0; k < NT; ++k) w[k] = a.w[line * NT + k];
@@ -126,12 +213,12 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
             for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
                 int rr = r + base;
                 if (rr >= n1) rr -= n1;
-                const T *p = S + rr * wc + c;
-                const T fc = p[C * wc];
+                const T *p = S + rr * ws + c;
+                const T fc = p[C * ws];
                 T acc = T(0);
 #pragma unroll
                 for (int k = 0; k < NT; ++k)
-                    if (k != C) acc = fma(w[k], p[k * wc] - fc, acc);
+                    if (k != C) acc = fma(w[k], p[k * ws] - fc, acc);
                 G[(int64_t)r * a.n2 + c] = fc + acc;
                 c += dc;
                 r += dr;
@@ -148,12 +235,12 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
                 const AdvExcCell<T> &e = cells[r];
                 int rr = r + e.base;
                 if (rr >= n1) rr -= n1;
-                const T *p = S + rr * wc + c;
-                const T fc = p[C * wc];
+                const T *p = S + rr * ws + c;
+                const T fc = p[C * ws];
                 T acc = T(0);
 #pragma unroll
                 for (int k = 0; k < NT; ++k)
-                    if (k != C) acc = fma(e.w[k], p[k * wc] - fc, acc);
+                    if (k != C) acc = fma(e.w[k], p[k * ws] - fc, acc);
                 G[(int64_t)r * a.n2 + c] = fc + acc;
                 c += dc;
                 r += dr;

@@ -59,9 +59,14 @@ struct AdvPlanImpl {
 
     int halo() const { return desc.impl == BKMA_ADV_PLAIN ? 0 : npts - 1; }
     int64_t ncb(int w) const { return (desc.n2 + w - 1) / w; }
+    // Shared memory of an R-slab tile of w columns: the widest row stride of
+    // the full tiles and of the ragged last column tile.
     size_t smem_bytes(int w, int r) const {
         const int wc = (int)std::min<int64_t>(w, desc.n2);
-        return (size_t)r * (size_t)slab_stride(desc.n1, halo(), wc, esize) * (size_t)esize;
+        int ws = staged_row_stride(desc.n2, wc, esize);
+        const int last = (int)(desc.n2 % wc);
+        if (last) ws = std::max(ws, staged_row_stride(desc.n2, last, esize));
+        return (size_t)r * (size_t)slab_stride(desc.n1, halo(), ws, esize) * (size_t)esize;
     }
     int64_t tiles(int w, int r) const { return ((lines + r - 1) / r) * ncb(w); }
 };

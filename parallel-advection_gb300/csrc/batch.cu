@@ -126,10 +126,6 @@ bkma_status build_batch(BatchImpl &b, cudaStream_t st) {
         a.W = W;
         a.R = R;
         a.ncb = p.ncb(W);
-        const int64_t es = b.esize;
-        const bool al = (uintptr_t)b.data[(size_t)i] % 16 == 0;
-        a.vec_ok = (W >= p.desc.n2) ? (al && (p.desc.n1 * p.desc.n2 * es) % 16 == 0)
-                                    : (al && (p.desc.n2 * es) % 16 == 0 && (W * es) % 16 == 0);
         a.base = p.d_base;
         a.w = (const T *)p.d_w;
         a.exc_index = p.d_exc_index;
