@@ -36,7 +36,9 @@ CFG_STEPS = 50
 METRIC = "advection GCells/s (FP32 storage, FP64 foot-point, degree 5)"
 UNIT = "GCells/s"
 WORKLOAD = "large single advection FP32 2048x1024x512, degree 5, 50 steps"
-PROFILE_JSON = os.path.join(ROOT, "profiles", "adv_tma_f32_2048x1024x512.json")
+# per plan path: the ncu DRAM traffic of the kernel that path launches
+PROFILE_JSON = {1: os.path.join(ROOT, "profiles", "adv_tma_f32_2048x1024x512.json"),
+                2: os.path.join(ROOT, "profiles", "adv_stream_f32_2048x1024x512.json")}
 
 
 def velocities(n0: int):
@@ -250,13 +252,15 @@ def run_gpu(args):
     hbm, _, peak_kind = peaks()
     avg_launch_s = statistics.mean(launch_ms) / 1e3
     achieved = cells * 8 / avg_launch_s / 1e9
+    info = plan.info()
+    kernel = {1: f"adv_tma_f32<6,{info['tile_cols']}>", 2: "adv_stream_f32<6>"}.get(
+        info["path"], "adv_staged<float,6>")
     traffic = None
     try:
-        with open(PROFILE_JSON) as fp:
+        with open(PROFILE_JSON[info["path"]]) as fp:
             traffic = json.load(fp).get("dram_bytes_per_launch")
     except Exception:
         pass
-    info = plan.info()
     del f
     torch.cuda.empty_cache()
 
@@ -272,11 +276,10 @@ def run_gpu(args):
                                                   "smem_bytes", "tiles", "exception_lines")}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
-                     "kernel": (f"adv_tma_f32<6,{info['tile_cols']}>" if info["path"] == 1
-                                else "adv_staged<float,6>"),
+                     "kernel": kernel,
                      "peak_kind": f"{peak_kind} copy bandwidth",
                      "algorithmic_bytes_per_launch": cells * 8},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (2 if info["path"] == 2 and info["exception_lines"] else 1),
         "clocks": clocks,
     }
 
@@ -421,8 +424,9 @@ def conv_block(bkma_gb300, dev, batch: int = 256, with_fp64: bool = True):
 
 
 def batched_block(bkma_gb300, dev, nfields: int = 64, steps: int = 10):
-    """Batched uneven advection: 64 fields per graph-captured persistent
-    launch, n0 ~ U{64..1024}, n1 in {256, 512, 1024, 2048}, n2 ~ U{1..256},
+    """Batched uneven advection: 64 fields advanced by one graph launch per
+    step (streamed kernels per tap count + the persistent staged kernel for
+    what cannot stream), n0 ~ U{64..1024}, n1 in {256, 512, 1024, 2048}, n2 ~ U{1..256},
     FP32, degree 3 or 5 per field, line velocities ~ U[-2, 2], seeded
     sin(2 pi x) + U[-0.01, 0.01] init. GCells/s over all fields; roofline at
     8 B per cell-step against the measured HBM copy peak."""
@@ -460,7 +464,8 @@ def batched_block(bkma_gb300, dev, nfields: int = 64, steps: int = 10):
         hbm, _, kind = peaks()
         gcs = batch.cells / (ms / 1e3) / 1e9
         out.update({"value": gcs, "ms_per_step": ms, "cells": batch.cells, "fields": nfields,
-                    "launches_per_step": 1, "graph": True,
+                    "launches_per_step": batch.launches_per_step(), "graph": True,
+                    "streamed_fields": sum(1 for w in tiles["W"] if w == 0),
                     "tiles": {"count": tiles["tiles"], "threads": tiles["threads"],
                               "smem_bytes": tiles["smem_bytes"]},
                     "roofline": {"bound": "hbm", "achieved": gcs * 8, "peak": hbm,
@@ -588,6 +593,7 @@ def main():
     ap.add_argument("--workload", default="advection", choices=["advection", "conv", "batched", "learned"],
                     help="conv: only the conv1d block, as its own JSON line")
     ap.add_argument("--conv-batch", type=int, default=256, help="smaller batch for captures")
+    ap.add_argument("--fields", type=int, default=64, help="batched workload: field count")
     args = ap.parse_args()
     if args.n0:
         global N0
@@ -597,8 +603,11 @@ def main():
     if args.workload in ("batched", "learned") and args.impl != "reference":
         import torch
         import bkma_gb300
-        blk = batched_block if args.workload == "batched" else learned_block
-        r = blk(bkma_gb300, torch.device("cuda", 0))
+        dev = torch.device("cuda", 0)
+        if args.workload == "batched":
+            r = batched_block(bkma_gb300, dev, nfields=args.fields)
+        else:
+            r = learned_block(bkma_gb300, dev)
         print(json.dumps(r))
         return 0 if "error" not in r else 1
     if args.workload == "conv" and args.impl != "reference":

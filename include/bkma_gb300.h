@@ -114,7 +114,11 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
 bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, void *stream);
 /* Explicit tile choice (the reference's pref_wg_size / seq_size knobs):
  * W columns x R slabs per CTA, `threads` per CTA (128, 256 or 512), staging
- * path 0 (cp.async) or 1 (TMA; FP32, n2 % 4 == 0, W in {8,16,32}, R == 1). */
+ * path 0 (cp.async) or 1 (TMA; FP32, n2 % 4 == 0, W in {8,16,32}, R == 1),
+ * or path 2: streamed columns (FP32, every line's per-step shift within the
+ * streamed window, n1 >= 64), where R is the row-segment mode (0 = from the
+ * field's size, k = up to k segments per 32-column group, k <= 8) and W the
+ * tile width of the staged pass over exception lines. */
 bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
                                    int32_t path);
 /* BKMA_W_TABLE: per-line weights, i0_count x (degree+1) floats (host or
@@ -173,8 +177,11 @@ bkma_status bkma_adv_batch_step(bkma_adv_batch *batch, int32_t nsteps, void *str
  * CTA) on the live fields - their contents advance by the timed steps - and
  * keeps the fastest. */
 bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream);
-/* Chosen tiles: per field W (columns) and R (slabs) (arrays of nfields), the
- * total tile count, threads per CTA and shared memory per CTA. */
+/* Chosen tiles: per field W (columns) and R (slabs) (arrays of nfields; for
+ * a field that runs in the streamed form W = 0 and R = its row segments per
+ * 32-column group, and its exception lines, if any, stay staged), the total
+ * staged tile count, and threads and shared memory per CTA of the staged
+ * kernel. */
 bkma_status bkma_adv_batch_tiles(const bkma_adv_batch *batch, int32_t *W, int32_t *R, int64_t *tiles,
                                  int32_t *threads, int64_t *smem_bytes);
 /* Total cells over all fields, and kernel launches per step. */

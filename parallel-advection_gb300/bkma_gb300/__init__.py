@@ -202,6 +202,12 @@ class AdvectionBatch:
         check(load().bkma_adv_batch_autotune(self._h, _stream(stream)))
         return self.tiles()
 
+    def launches_per_step(self) -> int:
+        """Kernel launches in one step's graph (staged + streamed groups)."""
+        cells, launches = C.c_int64(), C.c_int32()
+        check(load().bkma_adv_batch_info(self._h, C.byref(cells), C.byref(launches)))
+        return launches.value
+
     def tiles(self) -> dict:
         W = (C.c_int32 * self.nfields)()
         R = (C.c_int32 * self.nfields)()

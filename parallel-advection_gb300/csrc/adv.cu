@@ -165,6 +165,13 @@ void default_tile(AdvPlanImpl &p) {
     const void *aligned_probe = reinterpret_cast<const void *>(uintptr_t(256));
     p.path = (p.R == 1 && adv_tma_eligible(p, aligned_probe, p.W) &&
               adv_tma_smem(p, p.W) <= kMaxSmem) ? 1 : 0;
+    if (p.path == 0 && p.stream_ok && n2 >= 8) {
+        // rows that are not 16-byte aligned, or tiles too tall for the TMA
+        // form: stream the columns (row segments chosen from the size)
+        p.path = 2;
+        p.R = 0;
+        p.W = (int)std::min<int64_t>(16, n2);
+    }
 }
 
 template <typename T>
@@ -182,6 +189,14 @@ bkma_status upload_tables(AdvPlanImpl &p) {
     BKMA_CUDA_TRY(cudaMemcpy(p.d_exc_index, p.exc_index.data(), sizeof(int32_t) * L,
                              cudaMemcpyHostToDevice));
     BKMA_CUDA_TRY(cudaMemcpy(p.d_vx, p.vx.data(), sizeof(double) * L, cudaMemcpyHostToDevice));
+    if (p.n_exc > 0) {
+        std::vector<int32_t> lst;
+        for (int64_t l = 0; l < L; ++l)
+            if (p.exc_index[(size_t)l] >= 0) lst.push_back((int32_t)l);
+        BKMA_CUDA_TRY(cudaMalloc(&p.d_exc_lines, sizeof(int32_t) * lst.size()));
+        BKMA_CUDA_TRY(cudaMemcpy(p.d_exc_lines, lst.data(), sizeof(int32_t) * lst.size(),
+                                 cudaMemcpyHostToDevice));
+    }
     if (p.n_exc > 0) {
         // Per-cell tables for exception lines.
         const int64_t n1 = p.desc.n1;
@@ -207,41 +222,45 @@ bkma_status upload_tables(AdvPlanImpl &p) {
     return BKMA_OK;
 }
 
+// `list`, when given, restricts the launch to its `nlist` lines (R = 1).
 template <typename T, int NT>
 cudaError_t launch_staged_t(const AdvPlanImpl &p, const T *src, T *dst, int W, int R,
-                            int threads, cudaStream_t st) {
+                            int threads, cudaStream_t st, const int32_t *list, int64_t nlist) {
     AdvStagedArgs<T> a;
     a.src = src;
     a.dst = dst;
     a.n1 = p.desc.n1;
     a.n2 = p.desc.n2;
-    a.lines = p.lines;
+    a.lines = list ? nlist : p.lines;
     a.W = W;
-    a.R = R;
+    a.R = list ? 1 : R;
     a.ncb = p.ncb(W);
     a.base = p.d_base;
     a.w = (const T *)p.d_w;
     a.exc_index = p.d_exc_index;
     a.exc = (const AdvExcCell<T> *)p.d_exc;
-    const size_t smem = p.smem_bytes(W, R);
+    a.line_list = list;
+    const size_t smem = p.smem_bytes(W, a.R);
     auto kern = adv_staged<T, NT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    const int64_t grid = p.tiles(W, R);
+    const int64_t grid = list ? nlist * a.ncb : p.tiles(W, R);
+    if (grid == 0) return cudaSuccess;
     kern<<<(unsigned)grid, threads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_staged_npts(const AdvPlanImpl &p, const void *src, void *dst, int W, int R,
-                               int threads, cudaStream_t st) {
+                               int threads, cudaStream_t st, const int32_t *list = nullptr,
+                               int64_t nlist = 0) {
     const T *s = (const T *)src;
     T *d = (T *)dst;
     switch (p.npts) {
-    case 4: return launch_staged_t<T, 4>(p, s, d, W, R, threads, st);
-    case 6: return launch_staged_t<T, 6>(p, s, d, W, R, threads, st);
-    case 10: return launch_staged_t<T, 10>(p, s, d, W, R, threads, st);
+    case 4: return launch_staged_t<T, 4>(p, s, d, W, R, threads, st, list, nlist);
+    case 6: return launch_staged_t<T, 6>(p, s, d, W, R, threads, st, list, nlist);
+    case 10: return launch_staged_t<T, 10>(p, s, d, W, R, threads, st, list, nlist);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -271,6 +290,14 @@ cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R
                         int path, cudaStream_t st) {
     if (path == 1 && R == 1 && adv_tma_eligible(p, src, W))
         return adv_tma_launch(p, src, dst, W, threads, st);
+    if (path == 2 && p.stream_ok) {
+        // streamed lines, then the exception lines through the staged kernel
+        (void)threads;  // the streamed kernel has a fixed CTA; R = row-segment mode
+        cudaError_t e = adv_stream_launch(p, src, dst, R, st);
+        if (e != cudaSuccess || p.n_exc == 0) return e;
+        const int Wx = (int)std::min<int64_t>(16, p.desc.n2);
+        return launch_staged_npts<float>(p, src, dst, Wx, 1, 256, st, p.d_exc_lines, p.n_exc);
+    }
     if (p.desc.impl == BKMA_ADV_PLAIN)
         return launch_plain(p, (const double *)src, (double *)dst, W, R, threads, st);
     if (p.desc.dtype == BKMA_F32) return launch_staged_npts<float>(p, src, dst, W, R, threads, st);
@@ -334,6 +361,10 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
         }
     }
     if (d.impl == BKMA_ADV_PLAIN) return BKMA_OK;
+    p.stream_ok = d.dtype == BKMA_F32;
+    for (int64_t l = 0; l < p.lines && p.stream_ok; ++l)
+        if (p.exc_index[(size_t)l] < 0 && !stream_line_ok(p.base[(size_t)l], n1, NT))
+            p.stream_ok = false;
     if (d.dtype == BKMA_F32) return upload_tables<float>(p);
     return upload_tables<double>(p);
 }
@@ -363,6 +394,8 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
                     if (adv_tma_eligible(p, field, W)) cands.push_back({W, 1, t, 1});
                 }
     }
+    if (p.stream_ok)
+        for (int segs : {0, 1, 2, 4, 8}) cands.push_back({(int)std::min<int64_t>(16, n2), segs, 256, 2});
     for (int R : {1, 2, 4, 8, 16})
         if (n2 < 32 && R <= p.lines)
             for (int t : ths) cands.push_back({(int)n2, R, t, 0});
@@ -372,7 +405,8 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     float best = 1e30f;
     TuneVal bestv{p.W, p.R, p.threads, p.path};
     for (const TuneVal &c : cands) {
-        const size_t need = c.path == 1 ? adv_tma_smem(p, c.W) : p.smem_bytes(c.W, c.R);
+        const size_t need = c.path == 1 ? adv_tma_smem(p, c.W)
+                            : c.path == 2 ? 0 : p.smem_bytes(c.W, c.R);
         if (need > kMaxSmem) continue;
         cudaError_t err = launch_once(p, field, field, c.W, c.R, c.threads, c.path, st);  // warm-up
         if (err != cudaSuccess) {
@@ -480,7 +514,10 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
         }
     }
     default_tile(p);
-    if (p.smem_bytes(p.W, p.R) > kMaxSmem) {
+    // the staged kernel runs every line, or (streamed form) the exception lines
+    const bool staged = p.path != 2 || p.n_exc > 0;
+    const int ws = p.path == 2 ? (int)std::min<int64_t>(16, p.desc.n2) : p.W;
+    if (staged && p.smem_bytes(ws, p.path == 2 ? 1 : p.R) > kMaxSmem) {
         delete pl;
         return fail(BKMA_ERR_UNSUPPORTED, "n1 too long for a shared-memory line tile");
     }
@@ -496,7 +533,9 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
     info->tile_cols = (int32_t)std::min<int64_t>(p.W, p.desc.n2);
     info->tile_slabs = p.R;
     info->threads = p.threads;
-    info->smem_bytes = (int32_t)(p.path == 1 ? adv_tma_smem(p, p.W) : p.smem_bytes(p.W, p.R));
+    info->smem_bytes = (int32_t)(p.path == 1   ? adv_tma_smem(p, p.W)
+                                 : p.path == 2 ? adv_stream_smem()
+                                               : p.smem_bytes(p.W, p.R));
     info->npts = p.npts;
     info->autotuned = p.autotuned ? 1 : 0;
     info->tiles = p.tiles(p.W, p.R);
@@ -524,15 +563,18 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                                    int32_t path) {
     BKMA_CHECK_ARG(plan, "null argument");
     AdvPlanImpl &p = plan->impl;
-    BKMA_CHECK_ARG(W >= 1 && W <= 64 && R >= 1 && R <= 64, "W must be in [1,64], R in [1,64]");
+    BKMA_CHECK_ARG(W >= 1 && W <= 64 && R >= (path == 2 ? 0 : 1) && R <= 64,
+                   "W must be in [1,64], R in [1,64] (path 2: row-segment mode 0..8)");
     BKMA_CHECK_ARG(threads == 128 || threads == 256 || threads == 512, "threads must be 128, 256 or 512");
-    BKMA_CHECK_ARG(path == 0 || path == 1, "path must be 0 or 1");
-    BKMA_CHECK_ARG(R == 1 || W >= p.desc.n2, "R > 1 needs whole-row tiles (W >= n2)");
+    BKMA_CHECK_ARG(path >= 0 && path <= 2, "path must be 0, 1 or 2");
+    BKMA_CHECK_ARG(path != 2 || p.stream_ok, "streamed form not available for this plan");
+    BKMA_CHECK_ARG(path == 2 || R == 1 || W >= p.desc.n2, "R > 1 needs whole-row tiles (W >= n2)");
+    BKMA_CHECK_ARG(path != 2 || R <= 8, "path 2: R is the row-segment mode, 0 (auto) to 8");
     if (path == 1) {
         const void *probe = reinterpret_cast<const void *>(uintptr_t(256));
         BKMA_CHECK_ARG(R == 1 && adv_tma_eligible(p, probe, W), "TMA staging not available for this tile");
         BKMA_CHECK_ARG(adv_tma_smem(p, W) <= kMaxSmem, "tile does not fit shared memory");
-    } else {
+    } else if (path == 0) {
         BKMA_CHECK_ARG(p.smem_bytes(W, R) <= kMaxSmem, "tile does not fit shared memory");
     }
     p.W = W;

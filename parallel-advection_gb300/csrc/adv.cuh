@@ -26,7 +26,36 @@ struct AdvStagedArgs {
     const T *w;                // [lines][NT]
     const int32_t *exc_index;  // [lines]
     const AdvExcCell<T> *exc;  // [exception lines][n1]
+    const int32_t *line_list;  // optional: tile row lt covers line line_list[lt] (R = 1)
 };
+
+// Streamed form (adv_stream.cu): each lane walks one (line, i2) column down
+// all n1 rows. A line streams when its offset is constant along n1 and its
+// signed tap-0 offset d (base, or base - n1 above n1/2) lies in
+// [-kStreamBack, kStreamSeam - npts + 1]; n1 >= kStreamMinN1.
+constexpr int kStreamBack = 16;  // d >= -16: every row is read before it is overwritten
+constexpr int kStreamSeam = 24;  // rows 0 .. d+npts-2 saved before row 0 is overwritten
+constexpr int kStreamMinN1 = 64;
+
+struct StreamField {
+    const float *src;
+    float *dst;
+    int64_t n1, n2, lines;
+    const int32_t *base;       // [lines]
+    const float *w;            // [lines][npts]
+    const int32_t *exc_index;  // [lines]; exception lines are left to the staged pass
+    int npts;
+    int segs;                  // row segments per 32-column group (warps per group)
+    int64_t cta0;              // first CTA of this field in the launch
+};
+
+__host__ __device__ __forceinline__ int stream_offset(int32_t base, int64_t n1) {
+    return 2 * (int64_t)base > n1 ? (int)(base - n1) : (int)base;
+}
+__host__ __device__ __forceinline__ bool stream_line_ok(int32_t base, int64_t n1, int npts) {
+    const int d = stream_offset(base, n1);
+    return n1 >= kStreamMinN1 && d >= -kStreamBack && d + npts - 1 <= kStreamSeam;
+}
 
 struct AdvTmaArgs {
     float *dst;

@@ -101,6 +101,37 @@ __device__ __forceinline__ void stage_tile(T *sm, const T *__restrict__ g, int64
     __syncthreads();
 }
 
+// Stage like stage_tile, but into rows of ws elements that all start on 16
+// bytes (lead 0), element by element. Used for FP32 tiles whose global rows
+// do not start on 16 bytes, so the four-column compute can run on them.
+template <typename T>
+__device__ __forceinline__ void stage_tile_elems(T *sm, const T *__restrict__ g, int64_t n1,
+                                                 int64_t n2, int64_t line0, int nslab,
+                                                 int64_t c0, int wc, int ws, int halo,
+                                                 int sstride) {
+    const int rows = (int)n1 + halo;
+    const int total = rows * wc;
+    const int dr = blockDim.x / wc, dc = blockDim.x - dr * wc;
+    const int r_init = threadIdx.x / wc, c_init = threadIdx.x - r_init * wc;
+    for (int s = 0; s < nslab; ++s) {
+        const T *gs = g + (line0 + s) * n1 * n2 + c0;
+        T *ss = sm + (int64_t)s * sstride;
+        int r = r_init, c = c_init;
+        for (int i = threadIdx.x; i < total; i += blockDim.x) {
+            const int gr = r < n1 ? r : r - (int)n1;
+            cp_async(ss + r * ws + c, gs + (int64_t)gr * n2 + c, (int)sizeof(T));
+            c += dc;
+            r += dr;
+            if (c >= wc) {
+                c -= wc;
+                r += 1;
+            }
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+}
+
 // Tile coordinates of block `t`.
 struct TileCoord {
     int64_t line0;
@@ -124,21 +155,23 @@ __device__ __forceinline__ TileCoord tile_of(int64_t t, int64_t lines, int64_t n
 // FP32 rows of one slab, four columns per thread: NT float4 tap loads and
 // packed FMAs in the same order as the scalar loop below (d = f_k - f_c as
 // fma(f_c, -1, f_k), acc = fma(w_k, d, acc), out = f_c + acc), so the bits
-// match it. Needs wc and ws multiples of 4 and S on 16 bytes.
+// match it. Needs ws a multiple of 4 and S on 16 bytes; a last group past
+// wc computes on unused shared memory and stores only its columns < wc.
+// Stores are 16, 8 or 4 bytes wide as each row's address allows.
 template <int NT>
 __device__ __forceinline__ void rows_f32x4(const float *S, float *G, int n1, int64_t n2, int ws,
-                                           int wc, int base, const float *__restrict__ wl) {
+                                           int wc, int base, const float (&wl)[NT]) {
     constexpr int C = NT / 2 - 1;
-    const int ng = wc >> 2;  // column groups per row
+    const int ng = (wc + 3) >> 2;  // column groups per row
     const int rpp = blockDim.x / ng;
     const int r0 = threadIdx.x / ng;
     if (r0 >= rpp) return;
     const int g4 = (threadIdx.x - r0 * ng) * 4;
+    const int nval = min(4, wc - g4);  // columns of this group inside the tile
     float2 w2[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) w2[k] = make_float2(wl[k], wl[k]);
     const float2 m1 = make_float2(-1.0f, -1.0f);
-    const bool st_vec = (((uintptr_t)G | (uintptr_t)(n2 * 4)) & 15) == 0;
     int rr = r0 + base;
     if (rr >= n1) rr -= n1;
     int rstep = rpp % n1;
@@ -161,13 +194,17 @@ __device__ __forceinline__ void rows_f32x4(const float *S, float *G, int n1, int
         const float2 ol = __fadd2_rn(cl, al);
         const float2 oh = __fadd2_rn(ch, ah);
         float *q = G + (int64_t)r * n2 + g4;
-        if (st_vec) {
+        const unsigned qa = (unsigned)(uintptr_t)q & 15u;
+        if (nval == 4 && qa == 0) {
             *reinterpret_cast<float4 *>(q) = make_float4(ol.x, ol.y, oh.x, oh.y);
+        } else if (nval == 4 && (qa & 7u) == 0) {
+            *reinterpret_cast<float2 *>(q) = ol;
+            *reinterpret_cast<float2 *>(q + 2) = oh;
         } else {
             q[0] = ol.x;
-            q[1] = ol.y;
-            q[2] = oh.x;
-            q[3] = oh.y;
+            if (nval > 1) q[1] = ol.y;
+            if (nval > 2) q[2] = oh.x;
+            if (nval > 3) q[3] = oh.y;
         }
         rr += rstep;
         if (rr >= n1) rr -= n1;
@@ -180,9 +217,28 @@ __device__ __forceinline__ void rows_f32x4(const float *S, float *G, int n1, int
 template <typename T, int NT>
 __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const TileCoord &tc, T *sm) {
     constexpr int C = NT / 2 - 1;  // centre tap: the left node of the foot cell
-    const int ws = staged_row_stride(a.n2, tc.wc, (int)sizeof(T));
+    // Parameters of the first line, loaded before the staging wait so their
+    // latency hides behind the copies.
+    const int exc0 = a.exc_index[tc.line0];
+    const int base0 = a.base[tc.line0];
+    T w0[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) w0[k] = a.w[tc.line0 * NT + k];
+    // FP32 rows that do not start on 16 bytes are staged element by element
+    // into 16-byte-aligned rows (`packed`), so every FP32 tile runs the
+    // four-column compute; otherwise the shared layout keeps each element's
+    // place inside its 16-byte chunk and moves 16-byte pieces.
+    bool packed = false;
+    if constexpr (sizeof(T) == 4)
+        packed = (a.n2 & 3) != 0 || chunk_lead(a.src + tc.line0 * a.n1 * a.n2 + tc.c0) != 0;
+    const int ws = packed ? (tc.wc + 3) & ~3 : staged_row_stride(a.n2, tc.wc, (int)sizeof(T));
     const int sstride = slab_stride(a.n1, NT - 1, ws, (int)sizeof(T));
-    stage_tile<T>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, ws, NT - 1, sstride);
+    if (packed)
+        stage_tile_elems<T>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, ws, NT - 1,
+                            sstride);
+    else
+        stage_tile<T>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, ws, NT - 1,
+                      sstride);
 
     const int n1 = (int)a.n1;
     const int wc = tc.wc;
@@ -194,21 +250,21 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
     for (int s = 0; s < tc.nslab; ++s) {
         const int64_t line = tc.line0 + s;
         const int64_t g0 = line * a.n1 * a.n2 + tc.c0;
-        const int lead = chunk_lead(a.src + g0);
+        const int lead = packed ? 0 : chunk_lead(a.src + g0);
         const T *S = sm + (int64_t)s * sstride + lead;
         T *G = a.dst + g0;
-        const int exc = a.exc_index[line];
+        const int exc = s == 0 ? exc0 : a.exc_index[line];
         if (exc < 0) {
-            const int base = a.base[line];
+            const int base = s == 0 ? base0 : a.base[line];
+            T w[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k) w[k] = s == 0 ? w0[k] : a.w[line * NT + k];
             if constexpr (sizeof(T) == 4) {
-                if (((wc | ws | lead) & 3) == 0) {
-                    rows_f32x4<NT>(S, G, n1, a.n2, ws, wc, base, a.w + line * NT);
+                if (((ws | lead) & 3) == 0) {
+                    rows_f32x4<NT>(S, G, n1, a.n2, ws, wc, base, w);
                     continue;
                 }
             }
-            T w[NT];
-#pragma unroll
-            for (int k = 0; k < NT; ++k) w[k] = a.w[line * NT + k];
             int r = r_init, c = c_init;
             for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
                 int rr = r + base;
@@ -256,7 +312,8 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
 template <typename T, int NT>
 __global__ void __launch_bounds__(512) adv_staged(AdvStagedArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, a.R, a.W, a.ncb);
+    TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, a.R, a.W, a.ncb);
+    if (a.line_list) tc.line0 = a.line_list[tc.line0];
     staged_tile<T, NT>(a, tc, reinterpret_cast<T *>(smem_raw));
 }
 

@@ -30,7 +30,11 @@ struct AdvPlanImpl {
     int32_t *d_exc_index = nullptr;
     void *d_exc = nullptr;
     double *d_vx = nullptr;
-    // launch shape: path 0 = cp.async staging (any shape), 1 = TMA staging
+    int32_t *d_exc_lines = nullptr;  // [n_exc] the exception lines, ascending
+    // every non-exception line can stream (FP32 tables, see stream_line_ok)
+    bool stream_ok = false;
+    // launch shape: path 0 = cp.async staging (any shape), 1 = TMA staging,
+    // 2 = streamed columns (+ staged exception lines)
     int W = 16, R = 1, threads = 256, path = 0;
     bool autotuned = false;
     struct TmapCache {
@@ -52,6 +56,7 @@ struct AdvPlanImpl {
         cudaFree(d_exc_index);
         cudaFree(d_exc);
         cudaFree(d_vx);
+        cudaFree(d_exc_lines);
         cudaFree(d_host_buf);
         cudaFree(d_partials);
         cudaFree(d_status);
@@ -60,16 +65,41 @@ struct AdvPlanImpl {
     int halo() const { return desc.impl == BKMA_ADV_PLAIN ? 0 : npts - 1; }
     int64_t ncb(int w) const { return (desc.n2 + w - 1) / w; }
     // Shared memory of an R-slab tile of w columns: the widest row stride of
-    // the full tiles and of the ragged last column tile.
+    // the full tiles and of the ragged last column tile, in either staged
+    // layout (chunk-congruent rows, or rows padded to 16 bytes).
     size_t smem_bytes(int w, int r) const {
+        const int q = 16 / esize;
+        auto widest = [&](int wc) {
+            return std::max(staged_row_stride(desc.n2, wc, esize), (wc + q - 1) / q * q);
+        };
         const int wc = (int)std::min<int64_t>(w, desc.n2);
-        int ws = staged_row_stride(desc.n2, wc, esize);
+        int ws = widest(wc);
         const int last = (int)(desc.n2 % wc);
-        if (last) ws = std::max(ws, staged_row_stride(desc.n2, last, esize));
+        if (last) ws = std::max(ws, widest(last));
         return (size_t)r * (size_t)slab_stride(desc.n1, halo(), ws, esize) * (size_t)esize;
     }
     int64_t tiles(int w, int r) const { return ((lines + r - 1) / r) * ncb(w); }
 };
+
+// Streamed form (adv_stream.cu): the kernel over all streamable lines of a
+// plan (exception lines are skipped; the caller runs them staged). `segs`:
+// row segments per 32-column group, 0 = chosen from the field's size (see
+// adv_stream_segs).
+cudaError_t adv_stream_launch(AdvPlanImpl &p, const void *src, void *dst, int segs,
+                              cudaStream_t st);
+// Row segments for a field of n1 rows and `groups` 32-column groups: mode 0
+// splits until the GPU is filled a few times over, mode k >= 1 = up to k
+// (a power of two <= 8); segments keep at least 64 rows.
+int adv_stream_segs(int64_t n1, int64_t groups, int mode);
+int64_t adv_stream_groups(const AdvPlanImpl &p);
+int64_t adv_stream_ctas(const AdvPlanImpl &p, int segs);
+// Device descriptor of a plan's field for the streamed kernel.
+StreamField adv_stream_field(const AdvPlanImpl &p, const void *src, void *dst, int segs);
+size_t adv_stream_smem();  // static shared memory per CTA of the streamed kernel
+// All fields of `d_fields` (device array, ascending cta0) have npts taps;
+// nctas = the sum of their CTA counts.
+cudaError_t adv_stream_launch_fields(int npts, const StreamField *d_fields, int nfields,
+                                     int64_t nctas, cudaStream_t st);
 
 bool adv_tma_eligible(const AdvPlanImpl &p, const void *src, int W);
 size_t adv_tma_smem(const AdvPlanImpl &p, int W);

@@ -1,0 +1,246 @@
+// Streamed FP32 advection: no shared-memory staging of whole column strips.
+//
+// Work unit: a group of 32 consecutive columns of the field's (line i0,
+// column i2) space, one column per lane, so a row of a line is one coalesced
+// 128-byte access whatever n2 is (lanes may belong to different lines, each
+// with its own offset d and weights). The n1 rows of a group are split into
+// `segs` row segments, one warp each; a CTA of 8 warps holds 8/segs groups.
+//
+// A warp walks its segment [a, b) in blocks of U = 8 rows, keeping the
+// stencil window in registers: a ring of 4 blocks holds rows of the ORIGINAL
+// field from r0+d on (d = the line's signed tap-0 offset); the loads of the
+// block three ahead are issued before the current block's stores, so two
+// blocks of loads are always in flight. Output row r0+i is the incremental
+// form f_c + sum_k w_k (f_k - f_c) over the npts rows from r0+d+i, the same
+// operations in the same order as the staged kernels (identical bits).
+//
+// In place: inside its segment a lane reads every row before it overwrites
+// it (loads at block r0 reach rows >= r0 + d + 24 >= r0 when d >= -16, and a
+// lane's loads are ordered before its later stores). Rows outside the
+// segment belong to other warps, which overwrite them: before any store,
+// each warp saves in shared memory the first d+npts-1 rows of its segment
+// (needed by the segment above it, or at the periodic wrap by the last one)
+// and, when d < 0, its last -d rows (needed by the segment below it, or by
+// the first one at the wrap); one barrier, then every warp streams.
+//
+// Exception lines (offset not constant along n1) are skipped here and run
+// by the staged kernel. This replaces the whole-strip staging of the
+// reference's scratch-memory kernels (src/core/AdaptiveWg.hpp:57-140) for
+// the usual small per-step displacement.
+#include <type_traits>
+
+#include "adv.cuh"
+#include "adv_plan.cuh"
+#include "common.cuh"
+
+namespace bkma {
+
+namespace {
+
+constexpr int kU = 8;         // output rows per block
+constexpr int kWarps = 8;     // warps per CTA
+constexpr int kSeamRows = kStreamSeam + kStreamBack;
+constexpr int kPitch = 33;    // shared-memory row pitch (floats) of a warp's seams
+
+template <int NT>
+__device__ __forceinline__ void stream_group(const StreamField &F, int64_t group, int seg,
+                                             float (*seams)[kSeamRows * kPitch]) {
+    constexpr int C = NT / 2 - 1;
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int n1 = (int)F.n1;
+    const int64_t n2 = F.n2;
+    const int S = F.segs;
+    const int64_t q = group * 32 + lane;
+    bool ok = q < F.lines * n2;
+    int64_t line = 0, col = 0;
+    if (ok) {
+        line = q / n2;
+        col = q - line * n2;
+    }
+    int d = 0;
+    float w[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) w[k] = 0.f;
+    if (ok) {
+        const int32_t b = F.base[line];
+        ok = F.exc_index[line] < 0 && stream_line_ok(b, F.n1, NT);
+        d = stream_offset(b, F.n1);
+#pragma unroll
+        for (int k = 0; k < NT; ++k) w[k] = F.w[line * NT + k];
+    }
+    const int M = d + NT - 1;  // rows above the segment that it reads
+    const int L = (n1 + S - 1) / S;
+    const int a = seg * L, b = min(a + L, n1);
+    const int64_t off = line * F.n1 * n2 + col;
+    const float *src = F.src + off;
+    float *dst = F.dst + off;
+    // Save this segment's first M rows (seam rows 0..M-1) and, when d < 0,
+    // its last -d rows (seam rows kStreamSeam + t = row b + d + t).
+    float *mine = seams[warp];
+    if (ok) {
+        for (int t = 0; t < M; ++t) {
+            int j = a + t;
+            if (j >= n1) j -= n1;
+            mine[t * kPitch + lane] = src[(int64_t)j * n2];
+        }
+        for (int t = 0; t < -d; ++t) {
+            int j = b + d + t;
+            if (j < 0) j += n1;
+            mine[(kStreamSeam + t) * kPitch + lane] = src[(int64_t)j * n2];
+        }
+    }
+    __syncthreads();  // every seam is saved before any warp overwrites rows
+    if (!ok || a >= b) return;
+    const int g0 = warp - seg;  // first warp of this column group
+    const float *above = seams[g0 + (seg + 1 == S ? 0 : seg + 1)];
+    const float *below = seams[g0 + (seg == 0 ? S - 1 : seg - 1)];
+    // original value of row j, a + d <= j < b + d + 32 (unwrapped)
+    auto ld = [&](int j) -> float {
+        if (j >= b) return above[min(j - b, kStreamSeam - 1) * kPitch + lane];
+        if (j < a) return below[(kStreamSeam + (j - a) - d) * kPitch + lane];
+        return src[(int64_t)j * n2];
+    };
+    // Ring of 4 blocks of kU rows: slot (t % 4) holds rows r0(t)+d .. +kU-1
+    // of block t. At block t the loads of block t+3 are issued (into the
+    // slot block t-1 used), and block t's outputs read slots t and t+1, so
+    // two blocks of loads stay in flight behind the one being computed.
+    float B[4 * kU];
+#pragma unroll
+    for (int i = 0; i < 3 * kU; ++i) B[i] = ld(a + d + i);
+    const float *pn = src + (int64_t)(a + d + 3 * kU) * n2;  // first row of block t+3
+    float *po = dst + (int64_t)a * n2;
+    auto block = [&](auto ph_c, int r0) {
+        constexpr int ph = decltype(ph_c)::value;  // t % 4
+        constexpr int ld_slot = (ph + 3) % 4;
+        const int j0 = r0 + d + 3 * kU;
+        if (j0 >= a && j0 + kU <= b) {
+#pragma unroll
+            for (int i = 0; i < kU; ++i) {
+                B[ld_slot * kU + i] = *pn;
+                pn += n2;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < kU; ++i) B[ld_slot * kU + i] = ld(j0 + i);
+            pn += kU * n2;
+        }
+        const int nr = min(kU, b - r0);
+#pragma unroll
+        for (int i = 0; i < kU; ++i) {
+            if (i < nr) {
+                const float fc = B[(ph * kU + i + C) % (4 * kU)];
+                float acc = 0.f;
+#pragma unroll
+                for (int k = 0; k < NT; ++k)
+                    if (k != C) acc = fmaf(w[k], B[(ph * kU + i + k) % (4 * kU)] - fc, acc);
+                *po = fc + acc;
+            }
+            po += n2;
+        }
+    };
+    for (int r0 = a; r0 < b; r0 += 4 * kU) {
+        block(std::integral_constant<int, 0>{}, r0);
+        if (r0 + kU >= b) break;
+        block(std::integral_constant<int, 1>{}, r0 + kU);
+        if (r0 + 2 * kU >= b) break;
+        block(std::integral_constant<int, 2>{}, r0 + 2 * kU);
+        if (r0 + 3 * kU >= b) break;
+        block(std::integral_constant<int, 3>{}, r0 + 3 * kU);
+    }
+}
+
+// `many` (device array of nfields fields, ascending cta0; all with npts ==
+// NT) or, when null, the single field `one`.
+template <int NT>
+__global__ void __launch_bounds__(kWarps * 32) adv_stream_f32(StreamField one,
+                                                               const StreamField *__restrict__ many,
+                                                               int nfields) {
+    __shared__ float seams[kWarps][kSeamRows * kPitch];
+    StreamField F = one;
+    if (many) {
+        int lo = 0, hi = nfields - 1;  // last field with cta0 <= blockIdx.x
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (many[mid].cta0 <= (int64_t)blockIdx.x) lo = mid;
+            else hi = mid - 1;
+        }
+        F = many[lo];
+    }
+    const int warp = threadIdx.x >> 5;
+    const int per_cta = kWarps / F.segs;  // column groups per CTA
+    const int64_t group = ((int64_t)blockIdx.x - F.cta0) * per_cta + warp / F.segs;
+    stream_group<NT>(F, group, warp % F.segs, seams);
+}
+
+template <int NT>
+cudaError_t launch_stream(StreamField one, const StreamField *many, int nfields, int64_t ctas,
+                          cudaStream_t st) {
+    if (ctas == 0) return cudaSuccess;
+    adv_stream_f32<NT><<<(unsigned)ctas, kWarps * 32, 0, st>>>(one, many, nfields);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_npts(int npts, StreamField one, const StreamField *many, int nfields,
+                               int64_t ctas, cudaStream_t st) {
+    switch (npts) {
+    case 4: return launch_stream<4>(one, many, nfields, ctas, st);
+    case 6: return launch_stream<6>(one, many, nfields, ctas, st);
+    case 10: return launch_stream<10>(one, many, nfields, ctas, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+size_t adv_stream_smem() { return sizeof(float) * kWarps * kSeamRows * kPitch; }
+
+int adv_stream_segs(int64_t n1, int64_t groups, int mode) {
+    // mode 0: split rows until there are enough warps to fill the GPU a few
+    // times over; mode k >= 1: up to k segments. Segments keep >= 64 rows.
+    int s = 1;
+    if (mode == 0) {
+        while (s < kWarps && n1 / (2 * s) >= 64 && groups * s < 16384) s *= 2;
+    } else {
+        while (2 * s <= mode && s < kWarps && n1 / (2 * s) >= 64) s *= 2;
+    }
+    return s;
+}
+
+int64_t adv_stream_groups(const AdvPlanImpl &p) { return (p.lines * p.desc.n2 + 31) / 32; }
+
+int64_t adv_stream_ctas(const AdvPlanImpl &p, int segs) {
+    const int per_cta = kWarps / segs;
+    return (adv_stream_groups(p) + per_cta - 1) / per_cta;
+}
+
+StreamField adv_stream_field(const AdvPlanImpl &p, const void *src, void *dst, int segs) {
+    StreamField f;
+    f.src = (const float *)src;
+    f.dst = (float *)dst;
+    f.n1 = p.desc.n1;
+    f.n2 = p.desc.n2;
+    f.lines = p.lines;
+    f.base = p.d_base;
+    f.w = (const float *)p.d_w;
+    f.exc_index = p.d_exc_index;
+    f.npts = p.npts;
+    f.segs = segs;
+    f.cta0 = 0;
+    return f;
+}
+
+cudaError_t adv_stream_launch(AdvPlanImpl &p, const void *src, void *dst, int segs,
+                              cudaStream_t st) {
+    const int s = adv_stream_segs(p.desc.n1, adv_stream_groups(p), segs);
+    return launch_stream_npts(p.npts, adv_stream_field(p, src, dst, s), nullptr, 1,
+                              adv_stream_ctas(p, s), st);
+}
+
+cudaError_t adv_stream_launch_fields(int npts, const StreamField *d_fields, int nfields,
+                                     int64_t nctas, cudaStream_t st) {
+    StreamField none{};
+    return launch_stream_npts(npts, none, d_fields, nfields, nctas, st);
+}
+
+}  // namespace bkma

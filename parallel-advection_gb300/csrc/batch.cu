@@ -31,7 +31,7 @@ struct BatchFieldDev {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(512) adv_batch_kernel(const BatchFieldDev<T> *__restrict__ fields,
+__global__ void __launch_bounds__(256) adv_batch_kernel(const BatchFieldDev<T> *__restrict__ fields,
                                                         int nfields, int64_t ntiles,
                                                         unsigned long long *counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -48,13 +48,18 @@ __global__ void __launch_bounds__(512) adv_batch_kernel(const BatchFieldDev<T> *
             if (fields[mid].tile0 <= t) lo = mid;
             else hi = mid - 1;
         }
-        const BatchFieldDev<T> &F = fields[lo];
-        const TileCoord tc = tile_of(t - F.tile0, F.args.lines, F.args.n2, F.args.R, F.args.W,
-                                     F.args.ncb);
-        if (F.npts == 6)
-            staged_tile<T, 6>(F.args, tc, sm);
+        // Copy the field's argument block into registers: read through a
+        // pointer to global memory, every store to the field would force
+        // the compiler to reload it.
+        const AdvStagedArgs<T> args = fields[lo].args;
+        const int npts = fields[lo].npts;
+        TileCoord tc = tile_of(t - fields[lo].tile0, args.lines, args.n2, args.R, args.W,
+                               args.ncb);
+        if (args.line_list) tc.line0 = args.line_list[tc.line0];
+        if (npts == 6)
+            staged_tile<T, 6>(args, tc, sm);
         else
-            staged_tile<T, 4>(F.args, tc, sm);
+            staged_tile<T, 4>(args, tc, sm);
         __syncthreads();  // shared memory is restaged by the next tile
     }
 }
@@ -67,31 +72,54 @@ struct BatchImpl {
     std::vector<bkma_adv_plan *> plans;
     std::vector<void *> data;
     std::vector<int> W, R;
-    void *d_fields = nullptr;
+    void *d_fields = nullptr;  // staged work list entries
+    int nstaged = 0;
     unsigned long long *d_counter = nullptr;
+    // streamed fields, one group per tap count (4, 6, 10)
+    StreamField *d_stream[3] = {nullptr, nullptr, nullptr};
+    int nstream[3] = {0, 0, 0};
+    int64_t items[3] = {0, 0, 0};  // CTAs of each streamed launch
+    bool stream = true;  // stream the fields that allow it (FP32, small shifts)
+    int segs_mode = 0;   // row segments of streamed fields (adv_stream_segs mode)
     int nfields = 0;
     int64_t ntiles = 0, cells = 0;
     size_t smem = 0;
-    int threads = 256, grid = 0;
+    int threads = 256, grid = 0, launches = 0;
     size_t cap = 48 * 1024;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t cs = nullptr;
 
+    void free_lists() {
+        cudaFree(d_fields);
+        d_fields = nullptr;
+        for (auto &d : d_stream) {
+            cudaFree(d);
+            d = nullptr;
+        }
+    }
     ~BatchImpl() {
         if (exec) cudaGraphExecDestroy(exec);
         if (cs) cudaStreamDestroy(cs);
-        cudaFree(d_fields);
+        free_lists();
         cudaFree(d_counter);
         for (auto *p : plans) bkma_adv_plan_destroy(p);
     }
 };
+
+int stream_group(int npts) { return npts == 4 ? 0 : npts == 6 ? 1 : 2; }
+
+// Streamed when every line allows it and rows have at least 8 columns: with
+// fewer, a warp's 32 lanes spread over many lines and rows stop coalescing,
+// and whole-row staged tiles do better.
+bool streams(const AdvPlanImpl &p) { return p.stream_ok && p.desc.n2 >= 8; }
 
 // Tile of one field under a shared-memory cap.
 void choose_tile(const AdvPlanImpl &p, size_t cap, int &W, int &R) {
     const int64_t n2 = p.desc.n2;
     W = (int)n2;
     R = 1;
-    if (n2 >= 8) {
+    // Up to 32 columns: whole rows (no ragged column tile), when they fit.
+    if (n2 >= 8 && (n2 > 32 || p.smem_bytes((int)n2, 1) > cap)) {
         for (int w : {32, 16, 8, 4}) {
             if (w <= n2 && p.smem_bytes(w, 1) <= cap) {
                 W = w;
@@ -107,46 +135,92 @@ void choose_tile(const AdvPlanImpl &p, size_t cap, int &W, int &R) {
 }
 
 template <typename T>
+void staged_entry(std::vector<BatchFieldDev<T>> &f, BatchImpl &b, const AdvPlanImpl &p,
+                  void *data, int W, int R, const int32_t *list, int64_t nlist) {
+    BatchFieldDev<T> e{};
+    AdvStagedArgs<T> &a = e.args;
+    a.src = (const T *)data;
+    a.dst = (T *)data;
+    a.n1 = p.desc.n1;
+    a.n2 = p.desc.n2;
+    a.lines = list ? nlist : p.lines;
+    a.W = W;
+    a.R = list ? 1 : R;
+    a.ncb = p.ncb(W);
+    a.base = p.d_base;
+    a.w = (const T *)p.d_w;
+    a.exc_index = p.d_exc_index;
+    a.exc = (const AdvExcCell<T> *)p.d_exc;
+    a.line_list = list;
+    e.npts = p.npts;
+    e.tile0 = b.ntiles;
+    b.ntiles += ((a.lines + a.R - 1) / a.R) * a.ncb;
+    b.smem = std::max(b.smem, p.smem_bytes(W, a.R));
+    f.push_back(e);
+}
+
+template <typename T>
 bkma_status build_batch(BatchImpl &b, cudaStream_t st) {
-    std::vector<BatchFieldDev<T>> f((size_t)b.nfields);
+    std::vector<BatchFieldDev<T>> f;
+    std::vector<StreamField> sf[3];
+    b.free_lists();
     b.ntiles = 0;
     b.smem = 0;
+    for (int g = 0; g < 3; ++g) b.items[g] = 0;
+    int64_t stream_groups = 0;  // 32-column groups of all streamed fields
+    for (int i = 0; i < b.nfields; ++i) {
+        const AdvPlanImpl &p = plan_impl(b.plans[(size_t)i]);
+        if (sizeof(T) == 4 && b.stream && streams(p)) stream_groups += adv_stream_groups(p);
+    }
     for (int i = 0; i < b.nfields; ++i) {
         AdvPlanImpl &p = plan_impl(b.plans[(size_t)i]);
+        void *data = b.data[(size_t)i];
         int W, R;
         choose_tile(p, b.cap, W, R);
+        if (sizeof(T) == 4 && b.stream && streams(p)) {
+            // streamed; its exception lines (if any) stay on the staged list
+            const int g = stream_group(p.npts);
+            const int segs = adv_stream_segs(p.desc.n1, stream_groups, b.segs_mode);
+            StreamField s = adv_stream_field(p, data, data, segs);
+            s.cta0 = b.items[g];
+            b.items[g] += adv_stream_ctas(p, segs);
+            sf[g].push_back(s);
+            b.W[(size_t)i] = 0;
+            b.R[(size_t)i] = segs;
+            if (p.n_exc > 0) staged_entry<T>(f, b, p, data, W, 1, p.d_exc_lines, p.n_exc);
+            continue;
+        }
         b.W[(size_t)i] = W;
         b.R[(size_t)i] = R;
-        AdvStagedArgs<T> &a = f[(size_t)i].args;
-        a.src = (const T *)b.data[(size_t)i];
-        a.dst = (T *)b.data[(size_t)i];
-        a.n1 = p.desc.n1;
-        a.n2 = p.desc.n2;
-        a.lines = p.lines;
-        a.W = W;
-        a.R = R;
-        a.ncb = p.ncb(W);
-        a.base = p.d_base;
-        a.w = (const T *)p.d_w;
-        a.exc_index = p.d_exc_index;
-        a.exc = (const AdvExcCell<T> *)p.d_exc;
-        f[(size_t)i].npts = p.npts;
-        f[(size_t)i].tile0 = b.ntiles;
-        b.ntiles += p.tiles(W, R);
-        b.smem = std::max(b.smem, p.smem_bytes(W, R));
+        staged_entry<T>(f, b, p, data, W, R, nullptr, 0);
     }
-    if (!b.d_fields) BKMA_CUDA_TRY(cudaMalloc(&b.d_fields, sizeof(BatchFieldDev<T>) * f.size()));
-    BKMA_CUDA_TRY(cudaMemcpy(b.d_fields, f.data(), sizeof(BatchFieldDev<T>) * f.size(),
-                             cudaMemcpyHostToDevice));
+    b.nstaged = (int)f.size();
+    if (!f.empty()) {
+        BKMA_CUDA_TRY(cudaMalloc(&b.d_fields, sizeof(BatchFieldDev<T>) * f.size()));
+        BKMA_CUDA_TRY(cudaMemcpy(b.d_fields, f.data(), sizeof(BatchFieldDev<T>) * f.size(),
+                                 cudaMemcpyHostToDevice));
+    }
+    for (int g = 0; g < 3; ++g) {
+        b.nstream[g] = (int)sf[g].size();
+        if (sf[g].empty()) continue;
+        BKMA_CUDA_TRY(cudaMalloc(&b.d_stream[g], sizeof(StreamField) * sf[g].size()));
+        BKMA_CUDA_TRY(cudaMemcpy(b.d_stream[g], sf[g].data(), sizeof(StreamField) * sf[g].size(),
+                                 cudaMemcpyHostToDevice));
+    }
     auto kern = adv_batch_kernel<T>;
-    BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b.smem));
-    int per_sm = 0, dev = 0, sms = 0;
-    BKMA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, b.threads, b.smem));
-    cudaGetDevice(&dev);
-    BKMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    if (per_sm < 1) return fail(BKMA_ERR_UNSUPPORTED, "batched tile does not fit an SM");
-    b.grid = (int)std::min<int64_t>((int64_t)per_sm * sms, b.ntiles);
-    // capture: counter reset + persistent launch
+    b.grid = 0;
+    if (b.ntiles > 0) {
+        BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)b.smem));
+        int per_sm = 0, dev = 0, sms = 0;
+        BKMA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, b.threads, b.smem));
+        cudaGetDevice(&dev);
+        BKMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        if (per_sm < 1) return fail(BKMA_ERR_UNSUPPORTED, "batched tile does not fit an SM");
+        b.grid = (int)std::min<int64_t>((int64_t)per_sm * sms, b.ntiles);
+    }
+    // capture: counter reset + persistent staged launch, then the streamed
+    // launches (disjoint lines, so the order does not matter)
     if (b.exec) {
         cudaGraphExecDestroy(b.exec);
         b.exec = nullptr;
@@ -154,10 +228,20 @@ bkma_status build_batch(BatchImpl &b, cudaStream_t st) {
     if (!b.cs) BKMA_CUDA_TRY(cudaStreamCreateWithFlags(&b.cs, cudaStreamNonBlocking));
     (void)st;
     cudaGraph_t g = nullptr;
+    b.launches = 0;
     BKMA_CUDA_TRY(cudaStreamBeginCapture(b.cs, cudaStreamCaptureModeThreadLocal));
-    cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), b.cs);
-    kern<<<b.grid, b.threads, b.smem, b.cs>>>((const BatchFieldDev<T> *)b.d_fields, b.nfields,
-                                             b.ntiles, b.d_counter);
+    if (b.ntiles > 0) {
+        cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), b.cs);
+        kern<<<b.grid, b.threads, b.smem, b.cs>>>((const BatchFieldDev<T> *)b.d_fields,
+                                                 b.nstaged, b.ntiles, b.d_counter);
+        ++b.launches;
+    }
+    const int npts_of[3] = {4, 6, 10};
+    for (int k = 0; k < 3; ++k) {
+        if (b.items[k] == 0) continue;
+        adv_stream_launch_fields(npts_of[k], b.d_stream[k], b.nstream[k], b.items[k], b.cs);
+        ++b.launches;
+    }
     cudaError_t e = cudaStreamEndCapture(b.cs, &g);
     if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
     e = cudaGraphInstantiate(&b.exec, g, 0);
@@ -261,11 +345,20 @@ bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream) {
     float best = 1e30f;
     size_t best_cap = b.cap;
     int best_thr = b.threads;
+    bool best_stream = b.stream;
+    int best_segs = b.segs_mode;
+    // candidates: streamed fields (row segments: fill the GPU, or up to 8)
+    // or none x shared-memory cap x CTA size of the staged kernel
+    for (int sm : {0, 8, -1})
     for (size_t cap : {24 * 1024, 32 * 1024, 48 * 1024, 64 * 1024, 96 * 1024}) {
-        for (int thr : {256, 512}) {
+        for (int thr : {128, 256}) {
+            b.stream = sm >= 0;
+            b.segs_mode = sm >= 0 ? sm : 0;
             b.cap = cap;
             b.threads = thr;
             if (rebuild(b, st) != BKMA_OK) continue;
+            // nothing left for the staged kernel: cap and CTA size are moot
+            if (b.ntiles == 0 && (cap != 24 * 1024 || thr != 128)) continue;
             cudaGraphLaunch(b.exec, st);  // warm-up
             cudaEventRecord(e0, st);
             for (int r = 0; r < 2; ++r) cudaGraphLaunch(b.exec, st);
@@ -277,6 +370,8 @@ bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream) {
                 best = ms;
                 best_cap = cap;
                 best_thr = thr;
+                best_stream = b.stream;
+                best_segs = b.segs_mode;
             }
         }
     }
@@ -284,13 +379,15 @@ bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream) {
     cudaEventDestroy(e1);
     b.cap = best_cap;
     b.threads = best_thr;
+    b.stream = best_stream;
+    b.segs_mode = best_segs;
     return rebuild(b, st);
 }
 
 bkma_status bkma_adv_batch_info(const bkma_adv_batch *batch, int64_t *cells, int32_t *launches_per_step) {
     BKMA_CHECK_ARG(batch, "null argument");
     if (cells) *cells = batch->impl.cells;
-    if (launches_per_step) *launches_per_step = 1;
+    if (launches_per_step) *launches_per_step = batch->impl.launches;
     return BKMA_OK;
 }
 

@@ -118,25 +118,24 @@ def test_departure_offsets_bitexact(bkma, cuda, oracle, case):
 
 
 def test_exception_lines_use_per_cell_stencils(bkma, cuda, oracle):
-    """A shape whose departure offset changes along n1 (n1 = 1000, dt chosen so
-    v*dt/dx sits on a half-integer boundary): the per-cell table must give the
-    oracle's results."""
+    """Lines whose departure offset changes along n1 (n1 = 1000 and
+    whole-cell displacements): the per-cell tables must give the oracle's
+    results."""
     import torch
-    found = None
-    for dt in (0.0005, 0.0015, 0.0025, 0.00025, 0.0035):
-        p = AdvParams(16, 1000, 2, dt, 0.0, 1.0, -1.0, 1.0)
-        plan = _plan(bkma, p, dtype="f64")
-        if plan.info()["exception_lines"] > 0:
-            found = (p, plan)
-            break
-    if found is None:
-        pytest.skip("no shape with exception lines found")
-    p, plan = found
+    p = AdvParams(*EXC_CASE)
+    plan = _plan(bkma, p, dtype="f64", velocity=EXC_VEL)
+    assert plan.info()["exception_lines"] > 0
     f0 = _init(p, 3)
     d = _to(cuda, f0, torch.float64)
     plan.step(d, nsteps=2)
-    want = oracle.adv_step(p, f0.copy(), 2)
+    want = oracle.adv_step(p, f0.copy(), 2, velocity=EXC_VEL)
     assert np.abs(d.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+# n1 = 1000 (dx inexact) and whole-cell displacements v*dt = k*dx: the
+# departure cell's floor flips along n1, so these lines carry per-cell tables.
+EXC_CASE = (6, 1000, 3, 0.001, 0.0, 1.0, -2.0, 3.0)
+EXC_VEL = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
 
 
 @pytest.mark.parametrize("dtype", ["f32", "f64"])
@@ -381,3 +380,66 @@ def test_plain_fp64_bitexact_unaligned(bkma, cuda, oracle, off):
     _, d = _offset_field(cuda, f0, torch.float64, off)
     plan.step(d, nsteps=2)
     assert np.array_equal(d.cpu().numpy(), oracle.adv_step(p, f0.copy(), 2))
+
+
+STREAM_CASES = [
+    # (n0, n1, n2, dt, minX, maxX, minVx, maxVx), velocity or None
+    ((4, 1024, 7, 0.001, 0.0, 1.0, -2.0, 2.0), None),       # odd n2, d of both signs
+    ((3, 2048, 1, 0.0007, 0.0, 1.0, -2.0, 2.0), None),      # one column per line
+    ((2, 100, 33, 0.01, 0.0, 1.0, -1.0, 1.0), None),        # n1 not a multiple of 16
+    ((3, 64, 5, 0.004, 0.0, 1.0, -1.0, 1.0), None),         # shortest streamed n1
+    ((4, 256, 64, 0.02, 0.0, 1.0, -1.0, 1.0), None),        # shifts of ~5 cells
+    (EXC_CASE, EXC_VEL),                                    # exception lines (staged pass)
+    # uneven row segments (n1 = 1030) and shifts near both ends of the window
+    ((4, 1030, 5, 0.001, 0.0, 1.0, -20.0, 20.0), np.array([11.0, -17.5, 0.3, -0.3])),
+]
+
+
+@pytest.mark.parametrize("case,vel", STREAM_CASES)
+@pytest.mark.parametrize("degree,weights", [(5, "reference"), (3, "lagrange"), (9, "lagrange")])
+def test_streamed_path_bit_identical(bkma, cuda, oracle, case, vel, degree, weights):
+    """The streamed kernel (each lane walks one column down the rows with a
+    register window) gives the staged kernel's bits, in place from any base
+    alignment and out of place, and stays within the FP32 tolerance of the
+    FP64 oracle."""
+    import torch
+    p = AdvParams(*case)
+    kw = dict(dtype="f32", degree=degree, weights=weights)
+    if vel is not None:
+        kw["velocity"] = vel
+    f0 = _init(p, 21).astype(np.float32).astype(np.float64)
+    ref_plan = _plan(bkma, p, **kw)
+    ref_plan.set_tile(min(16, p.n2), 1, 256, 0)
+    ref = _to(cuda, f0, torch.float32)
+    ref_plan.step(ref, nsteps=3)
+    plan = _plan(bkma, p, **kw)
+    # row-segment modes: from the size, one segment, up to 2, up to 8
+    for segs, off in ((0, 0), (1, 1), (2, 2), (8, 0), (8, 1)):
+        info = plan.set_tile(16, segs, 256, 2)
+        assert info["path"] == 2
+        _, d = _offset_field(cuda, f0, torch.float32, off)
+        plan.step(d, nsteps=3)
+        plan.status()
+        assert torch.equal(d, ref), (segs, off)
+    oop = _plan(bkma, p, inplace=False, **kw)
+    oop.set_tile(16, 8, 256, 2)
+    _, src = _offset_field(cuda, f0, torch.float32, 3)
+    dst = torch.zeros_like(src)
+    oop.step(src, out=dst, nsteps=3)
+    assert torch.equal(dst, ref)
+    want = oracle.adv_step(p, f0.copy(), 3, degree=degree,
+                           ref_weights=(weights == "reference"), velocity=vel)
+    err = np.abs(ref.cpu().numpy().astype(np.float64) - want).max() / np.abs(want).max()
+    assert err <= 3e-7 * 3 + 2e-7, err
+
+
+def test_streamed_path_needs_small_shifts(bkma, cuda):
+    """Lines whose per-step shift is beyond the streamed window keep the
+    staged forms: the plan refuses the streamed path."""
+    p = AdvParams(4, 256, 8, 0.37, 0.0, 1.0, -3.0, 3.3)
+    plan = _plan(bkma, p, dtype="f32")
+    with pytest.raises(bkma.BkmaError):
+        plan.set_tile(16, 1, 256, 2)
+    f64 = _plan(bkma, AdvParams(*STREAM_CASES[0][0]), dtype="f64")
+    with pytest.raises(bkma.BkmaError):
+        f64.set_tile(16, 1, 256, 2)
