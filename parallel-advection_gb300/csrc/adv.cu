@@ -141,6 +141,7 @@ namespace bkma {
 namespace {
 
 constexpr size_t kMaxSmem = 227 * 1024;
+constexpr int kRunHostChunks = 16;  // slab chunks of bkma_adv_run_host's copy/compute pipeline
 
 // Default tile: columns of one slab when n2 is wide enough for 64-byte row
 // segments, otherwise whole slabs; about 32-64 KB of shared memory per CTA.
@@ -618,7 +619,8 @@ bkma_status bkma_adv_step(bkma_adv_plan *plan, void *data, void *out, int32_t ns
 bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nsteps, void *stream) {
     BKMA_CHECK_ARG(plan && host_data, "bkma_adv_run_host: null argument");
     AdvPlanImpl &p = plan->impl;
-    const size_t bytes = (size_t)(p.lines * p.desc.n1 * p.desc.n2) * (size_t)p.esize;
+    const size_t slab = (size_t)(p.desc.n1 * p.desc.n2) * (size_t)p.esize;
+    const size_t bytes = (size_t)p.lines * slab;
     if (p.host_buf_bytes < bytes) {
         cudaFree(p.d_host_buf);
         p.d_host_buf = nullptr;
@@ -627,11 +629,69 @@ bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nste
         p.host_buf_bytes = bytes;
     }
     cudaStream_t st = (cudaStream_t)stream;
-    BKMA_CUDA_TRY(cudaMemcpyAsync(p.d_host_buf, host_data, bytes, cudaMemcpyHostToDevice, st));
-    bkma_status s = adv_launch(p, p.d_host_buf, nullptr, nsteps, st);
-    if (s != BKMA_OK) return s;
-    BKMA_CUDA_TRY(cudaMemcpyAsync(host_data, p.d_host_buf, bytes, cudaMemcpyDeviceToHost, st));
+    // Small fields, or no steps: copy in, step, copy out on the caller's stream.
+    const int nch = (bytes >= ((size_t)256 << 20) && nsteps > 0)
+                        ? (int)std::min<int64_t>(kRunHostChunks, p.lines) : 1;
+    if (nch <= 1) {
+        BKMA_CUDA_TRY(cudaMemcpyAsync(p.d_host_buf, host_data, bytes, cudaMemcpyHostToDevice, st));
+        bkma_status s = adv_launch(p, p.d_host_buf, nullptr, nsteps, st);
+        if (s != BKMA_OK) return s;
+        BKMA_CUDA_TRY(cudaMemcpyAsync(host_data, p.d_host_buf, bytes, cudaMemcpyDeviceToHost, st));
+        BKMA_CUDA_TRY(cudaStreamSynchronize(st));
+        return BKMA_OK;
+    }
+    // Pipeline over slab chunks: chunk c = copy in, nsteps steps, copy out, on
+    // stream c % 3; each chunk is a sub-plan of the same lines (same tables,
+    // bit-identical results), so copies of one chunk overlap steps of others.
+    if ((int)p.chunks.size() != nch) {
+        for (auto *c : p.chunks) bkma_adv_plan_destroy(c);
+        p.chunks.clear();
+        p.chunk_l0.clear();
+        for (int c = 0; c < nch; ++c) {
+            const int64_t l0 = p.lines * c / nch, l1 = p.lines * (c + 1) / nch;
+            bkma_adv_desc d = p.desc;
+            d.i0_offset = p.desc.i0_offset + l0;
+            d.i0_count = l1 - l0;
+            d.velocity = p.vx.data() + l0;
+            bkma_adv_plan *sub = nullptr;
+            bkma_status s = bkma_adv_plan_create(&d, &sub);
+            if (s != BKMA_OK) return s;
+            p.chunks.push_back(sub);
+            p.chunk_l0.push_back(l0);
+        }
+    }
+    for (auto &q : p.pipe)
+        if (!q) BKMA_CUDA_TRY(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+    for (auto &e : p.pipe_ev)
+        if (!e) BKMA_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    BKMA_CUDA_TRY(cudaEventRecord(p.pipe_ev[3], st));
+    for (auto &q : p.pipe) BKMA_CUDA_TRY(cudaStreamWaitEvent(q, p.pipe_ev[3], 0));
+    for (int c = 0; c < nch; ++c) {
+        AdvPlanImpl &sp = plan_impl(p.chunks[(size_t)c]);
+        sp.W = p.W;  // the parent's tile choice (set or autotuned)
+        sp.R = p.R;
+        sp.threads = p.threads;
+        sp.path = p.path;
+        sp.autotuned = p.autotuned;
+        const int64_t l0 = p.chunk_l0[(size_t)c];
+        const size_t nb = (size_t)sp.lines * slab;
+        char *dev = (char *)p.d_host_buf + (size_t)l0 * slab;
+        char *host = (char *)host_data + (size_t)l0 * slab;
+        cudaStream_t q = p.pipe[c % 3];
+        BKMA_CUDA_TRY(cudaMemcpyAsync(dev, host, nb, cudaMemcpyHostToDevice, q));
+        bkma_status s = adv_launch(sp, dev, nullptr, nsteps, q);
+        if (s != BKMA_OK) return s;
+        BKMA_CUDA_TRY(cudaMemcpyAsync(host, dev, nb, cudaMemcpyDeviceToHost, q));
+    }
+    for (int k = 0; k < 3; ++k) {
+        BKMA_CUDA_TRY(cudaEventRecord(p.pipe_ev[k], p.pipe[k]));
+        BKMA_CUDA_TRY(cudaStreamWaitEvent(st, p.pipe_ev[k], 0));
+    }
     BKMA_CUDA_TRY(cudaStreamSynchronize(st));
+    for (auto *c : p.chunks) {
+        bkma_status s = bkma_adv_plan_status(c, stream);
+        if (s != BKMA_OK) return s;
+    }
     return BKMA_OK;
 }
 

@@ -44,13 +44,24 @@ struct AdvPlanImpl {
     };
     std::vector<TmapCache> tmaps;  // TMA descriptors of recently used fields
     int *d_status = nullptr;       // device status word of the bounded waits
-    // host-run buffer
+    // host-run buffer, and bkma_adv_run_host's pipeline: sub-plans over slab
+    // chunks (lines are independent) on three streams, so the copies of one
+    // chunk overlap the time steps of another
     void *d_host_buf = nullptr;
     size_t host_buf_bytes = 0;
+    std::vector<bkma_adv_plan *> chunks;
+    std::vector<int64_t> chunk_l0;
+    cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t pipe_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     double *d_partials = nullptr;
     int device = 0;
 
     ~AdvPlanImpl() {
+        for (auto *c : chunks) bkma_adv_plan_destroy(c);
+        for (auto &q : pipe)
+            if (q) cudaStreamDestroy(q);
+        for (auto &e : pipe_ev)
+            if (e) cudaEventDestroy(e);
         cudaFree(d_base);
         cudaFree(d_w);
         cudaFree(d_exc_index);

@@ -219,6 +219,28 @@ def test_run_host_matches_device_path(bkma, cuda):
     assert np.array_equal(h, d.cpu().numpy())
 
 
+@pytest.mark.parametrize("n2,velocity", [(512, None), (509, "exc")])
+def test_run_host_pipeline_matches_device_path(bkma, cuda, n2, velocity):
+    """A field of >= 256 MB goes through the chunked copy/compute pipeline
+    (sub-plans over slab chunks on three streams): same bits as the device
+    path, including exception lines and odd n2 (streamed kernel)."""
+    import torch
+    n0, n1 = 130, 1000
+    p = AdvParams(n0, n1, n2, 0.001, 0.0, 1.0, -2.0, 3.0)
+    vel = None
+    if velocity == "exc":
+        vel = np.resize(EXC_VEL, n0)
+    plan = _plan(bkma, p, dtype="f32", velocity=vel)
+    f0 = np.random.default_rng(8).uniform(-1, 1, (n0, n1, n2)).astype(np.float32)
+    d = _to(cuda, f0, torch.float32)
+    plan.step(d, nsteps=2)
+    h = torch.from_numpy(f0.copy()).pin_memory()
+    plan.run_host(h.numpy(), nsteps=2)
+    assert np.array_equal(h.numpy(), d.cpu().numpy())
+    del d
+    torch.cuda.empty_cache()
+
+
 def test_autotune_is_result_neutral(bkma, cuda):
     import torch
     p = AdvParams(6, 512, 48, 0.001, 0.0, 1.0, -1.0, 1.0)
