@@ -34,6 +34,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -296,8 +297,8 @@ cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R
         (void)threads;  // the streamed kernel has a fixed CTA; R = row-segment mode
         cudaError_t e = adv_stream_launch(p, src, dst, R, st);
         if (e != cudaSuccess || p.n_exc == 0) return e;
-        const int Wx = (int)std::min<int64_t>(16, p.desc.n2);
-        return launch_staged_npts<float>(p, src, dst, Wx, 1, 256, st, p.d_exc_lines, p.n_exc);
+        return launch_staged_npts<float>(p, src, dst, p.exc_tile_w(kMaxSmem), 1, 256, st,
+                                         p.d_exc_lines, p.n_exc);
     }
     if (p.desc.impl == BKMA_ADV_PLAIN)
         return launch_plain(p, (const double *)src, (double *)dst, W, R, threads, st);
@@ -341,26 +342,52 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
     p.exc_index.assign((size_t)p.lines, -1);
     p.n_exc = 0;
     const int64_t n1 = d.n1;
-    for (int64_t l = 0; l < p.lines; ++l) {
-        const int64_t g = d.i0_offset + l;
-        const double v = d.velocity ? d.velocity[l] : adv_coord((int)g, p.phys.minVx, p.phys.dvx);
-        p.vx[(size_t)l] = v;
-        double d0;
-        const int left0 = adv_departure(p.phys, 0, v, &d0);
-        const int64_t b0 = tap0_offset(left0, NT, 0, n1);
-        p.base[(size_t)l] = (int32_t)b0;
-        p.shift[(size_t)l] = d0 - 2.0;
-        stencil_weights(d.weights, NT, d0, &p.w64[(size_t)(l * NT)]);
-        if (d.impl == BKMA_ADV_PLAIN) continue;
-        for (int64_t i1 = 1; i1 < n1; ++i1) {
-            double di;
-            const int left = adv_departure(p.phys, (int)i1, v, &di);
-            if (tap0_offset(left, NT, i1, n1) != b0) {
-                p.exc_index[(size_t)l] = (int32_t)p.n_exc++;
-                break;
+    // A line's tap offset can change along n1 only where its fractional shift
+    // lies within rounding error of a cell boundary: the FP64 coordinate
+    // arithmetic of the departure point is off by far less than 1e-8 cells
+    // for n1 <= 2^24, so a line whose shift (at i1 = 0) is in
+    // (kEdge, 1 - kEdge) has one offset for every i1; the others are scanned
+    // cell by cell. Lines are independent: host threads split them.
+    constexpr double kEdge = 1e-6;
+    std::vector<uint8_t> varying((size_t)p.lines, 0);
+    auto work = [&](int64_t lo, int64_t hi) {
+        for (int64_t l = lo; l < hi; ++l) {
+            const int64_t g = d.i0_offset + l;
+            const double v =
+                d.velocity ? d.velocity[l] : adv_coord((int)g, p.phys.minVx, p.phys.dvx);
+            p.vx[(size_t)l] = v;
+            double d0;
+            const int left0 = adv_departure(p.phys, 0, v, &d0);
+            const int64_t b0 = tap0_offset(left0, NT, 0, n1);
+            p.base[(size_t)l] = (int32_t)b0;
+            p.shift[(size_t)l] = d0 - 2.0;
+            stencil_weights(d.weights, NT, d0, &p.w64[(size_t)(l * NT)]);
+            if (d.impl == BKMA_ADV_PLAIN) continue;
+            const double f = d0 - 2.0;
+            if (f > kEdge && f < 1.0 - kEdge) continue;
+            for (int64_t i1 = 1; i1 < n1; ++i1) {
+                double di;
+                const int left = adv_departure(p.phys, (int)i1, v, &di);
+                if (tap0_offset(left, NT, i1, n1) != b0) {
+                    varying[(size_t)l] = 1;
+                    break;
+                }
             }
         }
+    };
+    const int64_t per_thread = 1 << 14;  // lines
+    const int nthr = (int)std::min<int64_t>(
+        std::max(1u, std::thread::hardware_concurrency()), (p.lines + per_thread - 1) / per_thread);
+    if (nthr <= 1) {
+        work(0, p.lines);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthr; ++t)
+            pool.emplace_back(work, p.lines * t / nthr, p.lines * (t + 1) / nthr);
+        for (auto &th : pool) th.join();
     }
+    for (int64_t l = 0; l < p.lines; ++l)
+        if (varying[(size_t)l]) p.exc_index[(size_t)l] = (int32_t)p.n_exc++;
     if (d.impl == BKMA_ADV_PLAIN) return BKMA_OK;
     p.stream_ok = d.dtype == BKMA_F32;
     for (int64_t l = 0; l < p.lines && p.stream_ok; ++l)
@@ -516,9 +543,9 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
     }
     default_tile(p);
     // the staged kernel runs every line, or (streamed form) the exception lines
-    const bool staged = p.path != 2 || p.n_exc > 0;
-    const int ws = p.path == 2 ? (int)std::min<int64_t>(16, p.desc.n2) : p.W;
-    if (staged && p.smem_bytes(ws, p.path == 2 ? 1 : p.R) > kMaxSmem) {
+    const bool too_long = p.path == 2 ? (p.n_exc > 0 && p.exc_tile_w(kMaxSmem) == 0)
+                                      : p.smem_bytes(p.W, p.R) > kMaxSmem;
+    if (too_long) {
         delete pl;
         return fail(BKMA_ERR_UNSUPPORTED, "n1 too long for a shared-memory line tile");
     }

@@ -33,7 +33,7 @@ struct AdvStagedArgs {
 // all n1 rows. A line streams when its offset is constant along n1 and its
 // signed tap-0 offset d (base, or base - n1 above n1/2) lies in
 // [-kStreamBack, kStreamSeam - npts + 1]; n1 >= kStreamMinN1.
-constexpr int kStreamBack = 16;  // d >= -16: every row is read before it is overwritten
+constexpr int kStreamBack = 24;  // d >= -24: every row is read before it is overwritten
 constexpr int kStreamSeam = 24;  // rows 0 .. d+npts-2 saved before row 0 is overwritten
 constexpr int kStreamMinN1 = 64;
 

@@ -224,14 +224,18 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
     T w0[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) w0[k] = a.w[tc.line0 * NT + k];
-    // FP32 rows that do not start on 16 bytes are staged element by element
-    // into 16-byte-aligned rows (`packed`), so every FP32 tile runs the
-    // four-column compute; otherwise the shared layout keeps each element's
-    // place inside its 16-byte chunk and moves 16-byte pieces.
-    bool packed = false;
+    // Rows narrower than a 16-byte chunk are staged element by element into
+    // unpadded rows; FP32 rows of 4+ columns that do not start on 16 bytes
+    // element by element into 16-byte-aligned rows, so they run the
+    // four-column compute (both `packed`). Otherwise the shared layout keeps
+    // each element's place inside its 16-byte chunk and moves 16-byte pieces.
+    constexpr int Q = 16 / (int)sizeof(T);
+    bool packed = tc.wc < Q;
     if constexpr (sizeof(T) == 4)
-        packed = (a.n2 & 3) != 0 || chunk_lead(a.src + tc.line0 * a.n1 * a.n2 + tc.c0) != 0;
-    const int ws = packed ? (tc.wc + 3) & ~3 : staged_row_stride(a.n2, tc.wc, (int)sizeof(T));
+        packed = packed || (a.n2 & 3) != 0 ||
+                 chunk_lead(a.src + tc.line0 * a.n1 * a.n2 + tc.c0) != 0;
+    const int ws = !packed ? staged_row_stride(a.n2, tc.wc, (int)sizeof(T))
+                   : tc.wc < Q ? tc.wc : (tc.wc + 3) & ~3;
     const int sstride = slab_stride(a.n1, NT - 1, ws, (int)sizeof(T));
     if (packed)
         stage_tile_elems<T>(sm, a.src, a.n1, a.n2, tc.line0, tc.nslab, tc.c0, tc.wc, ws, NT - 1,

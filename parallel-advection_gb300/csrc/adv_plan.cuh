@@ -81,7 +81,10 @@ struct AdvPlanImpl {
     size_t smem_bytes(int w, int r) const {
         const int q = 16 / esize;
         auto widest = [&](int wc) {
-            return std::max(staged_row_stride(desc.n2, wc, esize), (wc + q - 1) / q * q);
+            if (wc < q) return wc;  // narrower than a chunk: unpadded rows
+            const int ws = staged_row_stride(desc.n2, wc, esize);
+            // FP32 rows off the 16-byte grid: padded to 16 bytes
+            return esize == 4 ? std::max(ws, (wc + q - 1) / q * q) : ws;
         };
         const int wc = (int)std::min<int64_t>(w, desc.n2);
         int ws = widest(wc);
@@ -90,6 +93,14 @@ struct AdvPlanImpl {
         return (size_t)r * (size_t)slab_stride(desc.n1, halo(), ws, esize) * (size_t)esize;
     }
     int64_t tiles(int w, int r) const { return ((lines + r - 1) / r) * ncb(w); }
+    // Tile width of the staged pass over the exception lines of a streamed
+    // plan: the widest of 16, 8, 4, 2, 1 columns that fits shared memory
+    // (0 if none does).
+    int exc_tile_w(size_t max_smem) const {
+        for (int w : {16, 8, 4, 2, 1})
+            if (w <= desc.n2 && smem_bytes(w, 1) <= max_smem) return w;
+        return 0;
+    }
 };
 
 // Streamed form (adv_stream.cu): the kernel over all streamable lines of a

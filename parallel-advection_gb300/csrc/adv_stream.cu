@@ -15,7 +15,7 @@
 // operations in the same order as the staged kernels (identical bits).
 //
 // In place: inside its segment a lane reads every row before it overwrites
-// it (loads at block r0 reach rows >= r0 + d + 24 >= r0 when d >= -16, and a
+// it (loads at block r0 reach rows >= r0 + d + 24 >= r0 when d >= -24, and a
 // lane's loads are ordered before its later stores). Rows outside the
 // segment belong to other warps, which overwrite them: before any store,
 // each warp saves in shared memory the first d+npts-1 rows of its segment
@@ -40,7 +40,7 @@ namespace {
 constexpr int kU = 8;         // output rows per block
 constexpr int kWarps = 8;     // warps per CTA
 constexpr int kSeamRows = kStreamSeam + kStreamBack;
-constexpr int kPitch = 33;    // shared-memory row pitch (floats) of a warp's seams
+constexpr int kPitch = 32;    // shared-memory row pitch (floats) of a warp's seams
 
 template <int NT>
 __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group, int seg,

@@ -413,7 +413,7 @@ STREAM_CASES = [
     ((4, 256, 64, 0.02, 0.0, 1.0, -1.0, 1.0), None),        # shifts of ~5 cells
     (EXC_CASE, EXC_VEL),                                    # exception lines (staged pass)
     # uneven row segments (n1 = 1030) and shifts near both ends of the window
-    ((4, 1030, 5, 0.001, 0.0, 1.0, -20.0, 20.0), np.array([11.0, -17.5, 0.3, -0.3])),
+    ((4, 1030, 5, 0.001, 0.0, 1.0, -20.0, 20.0), np.array([19.0, -17.5, 0.3, -0.3])),
 ]
 
 
