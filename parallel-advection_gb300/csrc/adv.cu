@@ -149,7 +149,11 @@ constexpr int kRunHostChunks = 16;  // slab chunks of bkma_adv_run_host's copy/c
 void default_tile(AdvPlanImpl &p) {
     const int64_t n2 = p.desc.n2;
     const int min_cols = 64 / p.esize;  // 16 FP32 / 8 FP64 columns = 64 B rows
-    if (n2 >= min_cols) {
+    // Short lines: a column tile would hold few cells, so take whole rows of
+    // several slabs when a slab's rows fit in 48 KB.
+    const bool short_lines =
+        p.desc.n1 * min_cols < 8192 && p.smem_bytes((int)n2, 1) <= 48 * 1024;
+    if (n2 >= min_cols && !short_lines) {
         p.W = min_cols;
         p.R = 1;
     } else {
@@ -591,8 +595,8 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                                    int32_t path) {
     BKMA_CHECK_ARG(plan, "null argument");
     AdvPlanImpl &p = plan->impl;
-    BKMA_CHECK_ARG(W >= 1 && W <= 64 && R >= (path == 2 ? 0 : 1) && R <= 64,
-                   "W must be in [1,64], R in [1,64] (path 2: row-segment mode 0..8)");
+    BKMA_CHECK_ARG(W >= 1 && W <= 1024 && R >= (path == 2 ? 0 : 1) && R <= 64,
+                   "W must be in [1,1024], R in [1,64] (path 2: row-segment mode 0..8)");
     BKMA_CHECK_ARG(threads == 128 || threads == 256 || threads == 512, "threads must be 128, 256 or 512");
     BKMA_CHECK_ARG(path >= 0 && path <= 2, "path must be 0, 1 or 2");
     BKMA_CHECK_ARG(path != 2 || p.stream_ok, "streamed form not available for this plan");

@@ -61,14 +61,28 @@ __device__ __forceinline__ void stage_tile(T *sm, const T *__restrict__ g, int64
         const int hal = halo * wc;
         const int nb = (body + 2 * Q - 2) / Q;  // chunks a run of `body` can touch
         const int per_slab = nb + (hal + 2 * Q - 2) / Q;
-        for (int s = 0; s < nslab; ++s) {
-            const T *gs = g + (line0 + s) * n1 * n2;
-            T *ss = sm + (int64_t)s * sstride + chunk_lead(gs);
-            for (int i = threadIdx.x; i < per_slab; i += blockDim.x) {
-                if (i < nb)
-                    copy_block(ss, gs, body, i);
+        if (per_slab < (int)blockDim.x) {
+            // small slabs: threads over (slab, chunk) pairs of all slabs
+            for (int i = threadIdx.x; i < nslab * per_slab; i += blockDim.x) {
+                const int s = i / per_slab;
+                const int j = i - s * per_slab;
+                const T *gs = g + (line0 + s) * n1 * n2;
+                T *ss = sm + (int64_t)s * sstride + chunk_lead(gs);
+                if (j < nb)
+                    copy_block(ss, gs, body, j);
                 else
-                    copy_block(ss + body, gs, hal, i - nb);
+                    copy_block(ss + body, gs, hal, j - nb);
+            }
+        } else {
+            for (int s = 0; s < nslab; ++s) {
+                const T *gs = g + (line0 + s) * n1 * n2;
+                T *ss = sm + (int64_t)s * sstride + chunk_lead(gs);
+                for (int i = threadIdx.x; i < per_slab; i += blockDim.x) {
+                    if (i < nb)
+                        copy_block(ss, gs, body, i);
+                    else
+                        copy_block(ss + body, gs, hal, i - nb);
+                }
             }
         }
     } else {
@@ -111,6 +125,20 @@ __device__ __forceinline__ void stage_tile_elems(T *sm, const T *__restrict__ g,
                                                  int sstride) {
     const int rows = (int)n1 + halo;
     const int total = rows * wc;
+    if (total < (int)blockDim.x) {
+        // small slabs: threads over the elements of all slabs
+        for (int i = threadIdx.x; i < nslab * total; i += blockDim.x) {
+            const int s = i / total;
+            const int e = i - s * total;
+            const int r = e / wc, c = e - (e / wc) * wc;
+            const int gr = r < n1 ? r : r - (int)n1;
+            cp_async(sm + (int64_t)s * sstride + r * ws + c,
+                     g + (line0 + s) * n1 * n2 + c0 + (int64_t)gr * n2 + c, (int)sizeof(T));
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        return;
+    }
     const int dr = blockDim.x / wc, dc = blockDim.x - dr * wc;
     const int r_init = threadIdx.x / wc, c_init = threadIdx.x - r_init * wc;
     for (int s = 0; s < nslab; ++s) {
@@ -224,16 +252,18 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
     T w0[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) w0[k] = a.w[tc.line0 * NT + k];
-    // Rows narrower than a 16-byte chunk are staged element by element into
-    // unpadded rows; FP32 rows of 4+ columns that do not start on 16 bytes
-    // element by element into 16-byte-aligned rows, so they run the
-    // four-column compute (both `packed`). Otherwise the shared layout keeps
-    // each element's place inside its 16-byte chunk and moves 16-byte pieces.
+    // Column tiles narrower than a 16-byte chunk are staged element by
+    // element into unpadded rows; FP32 rows of 4+ columns that do not start on
+    // 16 bytes element by element into 16-byte-aligned rows, so they run the
+    // four-column compute (both `packed`). Otherwise (whole rows, aligned
+    // columns) the shared layout keeps each element's place inside its
+    // 16-byte chunk and moves 16-byte pieces.
     constexpr int Q = 16 / (int)sizeof(T);
-    bool packed = tc.wc < Q;
+    bool packed = tc.wc < Q && tc.wc < a.n2;
     if constexpr (sizeof(T) == 4)
-        packed = packed || (a.n2 & 3) != 0 ||
-                 chunk_lead(a.src + tc.line0 * a.n1 * a.n2 + tc.c0) != 0;
+        packed = packed ||
+                 (tc.wc >= 4 && ((a.n2 & 3) != 0 ||
+                                 chunk_lead(a.src + tc.line0 * a.n1 * a.n2 + tc.c0) != 0));
     const int ws = !packed ? staged_row_stride(a.n2, tc.wc, (int)sizeof(T))
                    : tc.wc < Q ? tc.wc : (tc.wc + 3) & ~3;
     const int sstride = slab_stride(a.n1, NT - 1, ws, (int)sizeof(T));
@@ -251,6 +281,42 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
     const int dc = blockDim.x - dr * wc;
     const int r_init = threadIdx.x / wc;
     const int c_init = threadIdx.x - r_init * wc;
+    // Slabs of at most half a CTA's threads (short lines, few columns):
+    // several slabs at once, one thread per cell, same per-cell arithmetic.
+    if (tc.nslab > 1 && 2 * total <= (int)blockDim.x) {
+        const int conc = (int)blockDim.x / total;
+        const int sub = (int)threadIdx.x / total;
+        const int e = (int)threadIdx.x - sub * total;
+        const int r = e / wc, c = e - (e / wc) * wc;
+        for (int s = sub; s < tc.nslab && sub < conc; s += conc) {
+            const int64_t line = tc.line0 + s;
+            const int64_t g0 = line * a.n1 * a.n2 + tc.c0;
+            const int lead = packed ? 0 : chunk_lead(a.src + g0);
+            const T *S = sm + (int64_t)s * sstride + lead;
+            const int exc = a.exc_index[line];
+            int rr;
+            T w[NT];
+            if (exc < 0) {
+                rr = r + a.base[line];
+#pragma unroll
+                for (int k = 0; k < NT; ++k) w[k] = a.w[line * NT + k];
+            } else {
+                const AdvExcCell<T> &ec = a.exc[(int64_t)exc * n1 + r];
+                rr = r + ec.base;
+#pragma unroll
+                for (int k = 0; k < NT; ++k) w[k] = ec.w[k];
+            }
+            if (rr >= n1) rr -= n1;
+            const T *p = S + rr * ws + c;
+            const T fc = p[C * ws];
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < NT; ++k)
+                if (k != C) acc = fma(w[k], p[k * ws] - fc, acc);
+            a.dst[g0 + (int64_t)r * a.n2 + c] = fc + acc;
+        }
+        return;
+    }
     for (int s = 0; s < tc.nslab; ++s) {
         const int64_t line = tc.line0 + s;
         const int64_t g0 = line * a.n1 * a.n2 + tc.c0;

@@ -81,7 +81,7 @@ struct AdvPlanImpl {
     size_t smem_bytes(int w, int r) const {
         const int q = 16 / esize;
         auto widest = [&](int wc) {
-            if (wc < q) return wc;  // narrower than a chunk: unpadded rows
+            if (wc < q) return wc;  // narrower than a chunk (or whole rows of n2 < q): unpadded
             const int ws = staged_row_stride(desc.n2, wc, esize);
             // FP32 rows off the 16-byte grid: padded to 16 bytes
             return esize == 4 ? std::max(ws, (wc + q - 1) / q * q) : ws;

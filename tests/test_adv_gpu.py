@@ -344,6 +344,8 @@ STAGED_CASES = [
     (2, 301, 50, 0.002, 0.0, 1.0, -2.0, 2.0),   # odd n1: halo rows off the chunk grid
     (4, 128, 64, 0.01, 0.0, 1.0, -1.0, 1.0),    # aligned rows: four-column compute
     (5, 77, 3, 0.004, 0.0, 1.0, -1.5, 1.5),     # whole-row tiles, several slabs each
+    (40, 16, 1, 0.001, 0.0, 1.0, -1.0, 1.0),    # 16-cell slabs: several slabs at once
+    (12, 16, 128, 0.002, 0.0, 1.0, -1.0, 1.0),  # short lines, wide rows
 ]
 
 
@@ -360,7 +362,7 @@ def test_staged_tiles_and_alignments_bit_identical(bkma, cuda, oracle, case, dty
     if dtype == "f32":
         f0 = f0.astype(np.float32).astype(np.float64)
     tiles = [(W, 1) for W in (4, 6, 8, 12, 16, 32) if W < p.n2]
-    tiles += [(p.n2, 1), (p.n2, 2)]
+    tiles += [(p.n2, 1), (p.n2, 2), (p.n2, 8)]
     esize = 4 if dtype == "f32" else 8
     tiles = [(W, R) for (W, R) in tiles if (p.n1 + 8) * (W + 2) * R * esize <= 200 * 1024]
     ref = None
@@ -465,3 +467,25 @@ def test_streamed_path_needs_small_shifts(bkma, cuda):
     f64 = _plan(bkma, AdvParams(*STREAM_CASES[0][0]), dtype="f64")
     with pytest.raises(bkma.BkmaError):
         f64.set_tile(16, 1, 256, 2)
+
+
+def test_short_lines_with_exception_lines(bkma, cuda, oracle):
+    """n1 = 10 (dx inexact) with whole-cell displacements: exception lines
+    inside multi-slab tiles of 10-cell slabs (several slabs per CTA pass)
+    give the oracle's results, and every tile shape gives the same bits."""
+    import torch
+    p = AdvParams(5, 10, 3, 0.1, 0.0, 1.0, -1.0, 2.0)
+    vel = np.array([1.0, 2.0, 0.5, -1.0, 0.3])
+    f0 = _init(p, 13).astype(np.float32).astype(np.float64)
+    outs = []
+    for R in (1, 2, 5):
+        plan = _plan(bkma, p, dtype="f32", velocity=vel)
+        assert plan.info()["exception_lines"] == 2
+        plan.set_tile(p.n2, R, 256, 0)
+        d = _to(cuda, f0, torch.float32)
+        plan.step(d, nsteps=3)
+        outs.append(d.cpu())
+    assert all(torch.equal(o, outs[0]) for o in outs)
+    want = oracle.adv_step(p, f0.copy(), 3, velocity=vel)
+    err = np.abs(outs[0].numpy().astype(np.float64) - want).max() / np.abs(want).max()
+    assert err <= 3e-7 * 3 + 2e-7, err
