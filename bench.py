@@ -346,6 +346,25 @@ def extras(plan, bkma_gb300, dev, vel, kw, cells):
         "speedup_vs_plain_fp64": ms_plain / f32ms,
         "speedup_vs_staged_fp64": ms_staged64 / f32ms,
     }
+    # Multi-step fusion, reported apart from the metric: k steps per launch on
+    # shared-memory strips cut HBM traffic to 8/k B per cell-step.
+    fz = bkma_gb300.AdvectionPlan(N0, N1, N2, dtype="f32", velocity=vel, **kw)
+    a1 = f.clone()
+    plan.step(a1, nsteps=CFG_STEPS)
+    fused = {}
+    for k in (5, 10, 25):
+        fz.set_fusion(k)
+        a2 = f.clone()
+        fz.step(a2, nsteps=CFG_STEPS)
+        same = bool(torch.equal(a1, a2))
+        ms = timed(fz, a2, CFG_STEPS)
+        fused[str(k)] = {"gcells_s": cells / (ms / 1e3) / 1e9, "hbm_bytes_per_cell_step": 8.0 / k,
+                         "bit_identical_to_one_step_per_launch": same}
+        del a2
+    out["fused_steps"] = {"steps_per_launch": fused, "steps": CFG_STEPS,
+                          "kernel": "adv_fused<float,6> (512 threads, 16-column strips)",
+                          "note": "not the metric: state stays in shared memory between steps"}
+    del a1, fz
     del ref, f
     torch.cuda.empty_cache()
     return out

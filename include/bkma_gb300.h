@@ -121,6 +121,15 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * tile width of the staged pass over exception lines. */
 bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
                                    int32_t path);
+/* Multi-step fusion: bkma_adv_step runs `steps_per_launch` time steps per
+ * kernel launch on column strips held in shared memory (the last launch of
+ * a call runs the remainder), 1 = one step per launch (default). Results
+ * are bit-identical to one step per launch; HBM traffic per cell-step falls
+ * by the factor. Out of place, `data` is left unchanged. Not for the plain
+ * FP64 form; BKMA_ERR_UNSUPPORTED when a strip of the plan's n1 rows does
+ * not fit shared memory. No counterpart in the reference, which runs one
+ * step per kernel (src/advection.cpp:55-59). */
+bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_launch);
 /* BKMA_W_TABLE: per-line weights, i0_count x (degree+1) floats (host or
  * device pointer), applied on the plan's own departure offsets. */
 bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device);

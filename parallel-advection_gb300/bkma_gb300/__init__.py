@@ -110,6 +110,10 @@ class AdvectionPlan:
         """Raise if a bounded device wait timed out since the last query."""
         check(load().bkma_adv_plan_status(self._h, _stream(stream)))
 
+    def set_fusion(self, steps_per_launch: int):
+        """Time steps per kernel launch (shared-memory strips; 1 = off)."""
+        check(load().bkma_adv_plan_set_fusion(self._h, steps_per_launch))
+
     def autotune(self, field, stream=None):
         check(load().bkma_adv_plan_autotune(self._h, _ptr(field), _stream(stream)))
         return self.info()

@@ -314,6 +314,21 @@ cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R
 
 bkma_status adv_launch(AdvPlanImpl &p, void *data, void *out, int nsteps, cudaStream_t st) {
     const bool inplace = (out == nullptr || out == data);
+    if (p.fuse > 1 && nsteps > 0) {
+        // k steps per launch; out of place the first launch reads `data` and
+        // writes `out`, later ones run in place on `out`
+        const int W = adv_fused_tile_w(p, kMaxSmem);
+        const void *src = data;
+        void *dst = inplace ? data : out;
+        for (int done = 0; done < nsteps;) {
+            const int k = std::min(p.fuse, nsteps - done);
+            cudaError_t e = adv_fused_launch(p, src, dst, W, k, st);
+            if (e != cudaSuccess) return cuda_fail(e, "adv fused kernel launch");
+            src = dst;
+            done += k;
+        }
+        return BKMA_OK;
+    }
     // Out of place: an odd number of steps alternates data->out->data...->out;
     // an even number first steps `data` in place, then alternates.
     int t0 = 0;
@@ -613,6 +628,19 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
     p.R = R;
     p.threads = threads;
     p.path = path;
+    return BKMA_OK;
+}
+
+bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_launch) {
+    BKMA_CHECK_ARG(plan && steps_per_launch >= 1, "steps_per_launch must be >= 1");
+    AdvPlanImpl &p = plan->impl;
+    if (steps_per_launch > 1) {
+        if (p.desc.impl == BKMA_ADV_PLAIN)
+            return fail(BKMA_ERR_UNSUPPORTED, "the plain FP64 form runs one step per launch");
+        if (adv_fused_tile_w(p, kMaxSmem) == 0)
+            return fail(BKMA_ERR_UNSUPPORTED, "lines too long for a fused shared-memory strip");
+    }
+    p.fuse = steps_per_launch;
     return BKMA_OK;
 }
 

@@ -1,0 +1,165 @@
+// Multi-step fused advection: k time steps per launch for column strips that
+// fit in shared memory.
+//
+// A CTA stages W columns x n1 rows (+ npts-1 wrap rows) of one slab, then
+// runs k steps on the shared copy: each thread computes its cells of the
+// next step into registers from the shared strip (the same per-cell
+// arithmetic as the staged kernel, f_c + sum_k w_k (f_k - f_c), so k fused
+// steps give the bits of k separate steps), the CTA waits, writes them back,
+// refreshes the wrap rows and waits again; after the last step the strip goes
+// back to HBM once. Lines are independent and the departure tables do not
+// change with time, so nothing outside the strip is needed between steps.
+// HBM traffic is 8/k (FP32) or 16/k (FP64) bytes per cell-step, so results
+// are reported apart from the one-step-per-launch roofline. The reference
+// runs one step per kernel (src/advection.cpp:55-59).
+//
+// Thread map: column c = tid % wc, rows r0, r0 + rstep, ... with
+// r0 = tid / wc and rstep = blockDim / wc; at most 32 (FP32) or 16 (FP64)
+// rows per thread, held in registers across the barrier.
+#include "adv.cuh"
+#include "adv_device.cuh"
+#include "adv_plan.cuh"
+#include "common.cuh"
+
+namespace bkma {
+
+namespace {
+
+// cells per thread, held in registers across the barrier
+template <typename T>
+__host__ __device__ constexpr int fuse_rows() { return sizeof(T) == 4 ? 32 : 16; }
+constexpr int kFuseThreads = 512;
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(kFuseThreads) adv_fused(AdvStagedArgs<T> a, int ksteps) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *S = reinterpret_cast<T *>(smem_raw);
+    constexpr int C = NT / 2 - 1;
+    TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, 1, a.W, a.ncb);
+    if (a.line_list) tc.line0 = a.line_list[tc.line0];
+    const int n1 = (int)a.n1;
+    const int wc = tc.wc;
+    const int ws = wc;  // unpadded rows, element-wise staging (any alignment)
+    const int64_t line = tc.line0;
+    stage_tile_elems<T>(S, a.src, a.n1, a.n2, line, 1, tc.c0, wc, ws, NT - 1,
+                        slab_stride(a.n1, NT - 1, ws, (int)sizeof(T)));
+    const int exc = a.exc_index[line];
+    const int base = exc < 0 ? a.base[line] : 0;
+    T w[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) w[k] = exc < 0 ? a.w[line * NT + k] : T(0);
+    const AdvExcCell<T> *cells = exc < 0 ? nullptr : a.exc + (int64_t)exc * n1;
+    const int rstep = (int)blockDim.x / wc;
+    const int r0 = (int)threadIdx.x / wc;
+    const int c = (int)threadIdx.x - r0 * wc;
+    const bool active = r0 < rstep;
+    constexpr int kFuseRows = fuse_rows<T>();
+    T v[kFuseRows];
+    for (int step = 0; step < ksteps; ++step) {
+#pragma unroll
+        for (int j = 0; j < kFuseRows; ++j) {
+            const int r = r0 + j * rstep;
+            if (active && r < n1) {
+                int rr;
+                T wk[NT];
+                if (exc < 0) {
+                    rr = r + base;
+#pragma unroll
+                    for (int k = 0; k < NT; ++k) wk[k] = w[k];
+                } else {
+                    const AdvExcCell<T> &e = cells[r];
+                    rr = r + e.base;
+#pragma unroll
+                    for (int k = 0; k < NT; ++k) wk[k] = e.w[k];
+                }
+                if (rr >= n1) rr -= n1;
+                const T *p = S + rr * ws + c;
+                const T fc = p[C * ws];
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < NT; ++k)
+                    if (k != C) acc = fma(wk[k], p[k * ws] - fc, acc);
+                v[j] = fc + acc;
+            }
+        }
+        __syncthreads();  // every thread has read the old strip
+#pragma unroll
+        for (int j = 0; j < kFuseRows; ++j) {
+            const int r = r0 + j * rstep;
+            if (active && r < n1) S[r * ws + c] = v[j];
+        }
+        __syncthreads();
+        // wrap rows n1 .. n1+NT-2 repeat rows 0 .. NT-2
+        for (int i = threadIdx.x; i < (NT - 1) * wc; i += blockDim.x) {
+            const int hr = i / wc, hc = i - hr * wc;
+            S[(n1 + hr) * ws + hc] = S[hr * ws + hc];
+        }
+        __syncthreads();
+    }
+    T *G = a.dst + line * a.n1 * a.n2 + tc.c0;
+    for (int i = threadIdx.x; i < n1 * wc; i += blockDim.x) {
+        const int r = i / wc, cc = i - r * wc;
+        G[(int64_t)r * a.n2 + cc] = S[r * ws + cc];
+    }
+}
+
+template <typename T, int NT>
+cudaError_t launch_fused_t(const AdvPlanImpl &p, const void *src, void *dst, int W, int ksteps,
+                           cudaStream_t st) {
+    AdvStagedArgs<T> a{};
+    a.src = (const T *)src;
+    a.dst = (T *)dst;
+    a.n1 = p.desc.n1;
+    a.n2 = p.desc.n2;
+    a.lines = p.lines;
+    a.W = W;
+    a.R = 1;
+    a.ncb = p.ncb(W);
+    a.base = p.d_base;
+    a.w = (const T *)p.d_w;
+    a.exc_index = p.d_exc_index;
+    a.exc = (const AdvExcCell<T> *)p.d_exc;
+    a.line_list = nullptr;
+    const size_t smem =
+        (size_t)slab_stride(p.desc.n1, p.npts - 1, W, p.esize) * (size_t)p.esize;
+    auto kern = adv_fused<T, NT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)p.tiles(W, 1), kFuseThreads, smem, st>>>(a, ksteps);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_fused_npts(const AdvPlanImpl &p, const void *src, void *dst, int W, int k,
+                              cudaStream_t st) {
+    switch (p.npts) {
+    case 4: return launch_fused_t<T, 4>(p, src, dst, W, k, st);
+    case 6: return launch_fused_t<T, 6>(p, src, dst, W, k, st);
+    case 10: return launch_fused_t<T, 10>(p, src, dst, W, k, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+int adv_fused_tile_w(const AdvPlanImpl &p, size_t max_smem) {
+    // widest strip with at most fuse_rows rows per thread that fits
+    for (int w : {16, 8, 4, 2, 1}) {
+        if (w > p.desc.n2 && w != 1) continue;
+        const int rstep = kFuseThreads / w;
+        const size_t smem =
+            (size_t)slab_stride(p.desc.n1, p.npts - 1, w, p.esize) * (size_t)p.esize;
+        const int rows = p.esize == 4 ? fuse_rows<float>() : fuse_rows<double>();
+        if ((p.desc.n1 + rstep - 1) / rstep <= rows && smem <= max_smem) return w;
+    }
+    return 0;
+}
+
+cudaError_t adv_fused_launch(const AdvPlanImpl &p, const void *src, void *dst, int W, int k,
+                             cudaStream_t st) {
+    if (p.desc.dtype == BKMA_F32) return launch_fused_npts<float>(p, src, dst, W, k, st);
+    return launch_fused_npts<double>(p, src, dst, W, k, st);
+}
+
+}  // namespace bkma

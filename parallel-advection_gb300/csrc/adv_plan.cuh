@@ -37,6 +37,7 @@ struct AdvPlanImpl {
     // 2 = streamed columns (+ staged exception lines)
     int W = 16, R = 1, threads = 256, path = 0;
     bool autotuned = false;
+    int fuse = 1;  // time steps per launch (adv_fused.cu when > 1)
     struct TmapCache {
         const void *ptr;
         int W;
@@ -122,6 +123,12 @@ size_t adv_stream_smem();  // static shared memory per CTA of the streamed kerne
 // nctas = the sum of their CTA counts.
 cudaError_t adv_stream_launch_fields(int npts, const StreamField *d_fields, int nfields,
                                      int64_t nctas, cudaStream_t st);
+
+// Multi-step fused form (adv_fused.cu): strip width for a plan (0 if the
+// plan's lines are too long), and one launch of k fused steps src -> dst.
+int adv_fused_tile_w(const AdvPlanImpl &p, size_t max_smem);
+cudaError_t adv_fused_launch(const AdvPlanImpl &p, const void *src, void *dst, int W, int k,
+                             cudaStream_t st);
 
 bool adv_tma_eligible(const AdvPlanImpl &p, const void *src, int W);
 size_t adv_tma_smem(const AdvPlanImpl &p, int W);

@@ -489,3 +489,60 @@ def test_short_lines_with_exception_lines(bkma, cuda, oracle):
     want = oracle.adv_step(p, f0.copy(), 3, velocity=vel)
     err = np.abs(outs[0].numpy().astype(np.float64) - want).max() / np.abs(want).max()
     assert err <= 3e-7 * 3 + 2e-7, err
+
+
+FUSED_CASES = [
+    # (n0, n1, n2, dt, minX, maxX, minVx, maxVx), velocity or None
+    ((4, 1024, 16, 0.001, 0.0, 1.0, -1.0, 1.0), None),
+    ((3, 256, 37, 0.003, 0.0, 1.0, -2.0, 2.0), None),       # odd n2, ragged strip
+    ((5, 77, 3, 0.004, 0.0, 1.0, -1.5, 1.5), None),         # narrow rows
+    ((2, 2048, 20, 0.0007, 0.0, 1.0, -1.0, 1.0), None),     # 8-column strips
+    (EXC_CASE, EXC_VEL),                                    # exception lines
+]
+
+
+@pytest.mark.parametrize("case,vel", FUSED_CASES)
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_fused_steps_bit_identical(bkma, cuda, oracle, case, vel, dtype):
+    """k time steps per launch on strips held in shared memory give the bits
+    of one step per launch, for any k and a step count that k does not
+    divide; out of place, the input stays as it was."""
+    import torch
+    p = AdvParams(*case)
+    tdt = torch.float32 if dtype == "f32" else torch.float64
+    kw = dict(dtype=dtype)
+    if vel is not None:
+        kw["velocity"] = vel
+    f0 = _init(p, 31)
+    if dtype == "f32":
+        f0 = f0.astype(np.float32).astype(np.float64)
+    ref = _to(cuda, f0, tdt)
+    _plan(bkma, p, **kw).step(ref, nsteps=7)
+    for k in (2, 3, 7, 10):
+        plan = _plan(bkma, p, **kw)
+        plan.set_fusion(k)
+        d = _to(cuda, f0, tdt)
+        plan.step(d, nsteps=7)
+        plan.status()
+        assert torch.equal(d, ref), k
+    oop = _plan(bkma, p, inplace=False, **kw)
+    oop.set_fusion(3)
+    src = _to(cuda, f0, tdt)
+    out = torch.zeros_like(src)
+    oop.step(src, out=out, nsteps=7)
+    assert torch.equal(out, ref)
+    assert torch.equal(src, _to(cuda, f0, tdt))
+    want = oracle.adv_step(p, f0.copy(), 7, velocity=vel)
+    err = np.abs(ref.cpu().numpy().astype(np.float64) - want).max() / np.abs(want).max()
+    assert err <= (3e-7 * 7 + 2e-7 if dtype == "f32" else 1e-11), err
+
+
+def test_fused_steps_limits(bkma, cuda):
+    p = AdvParams(2, 64, 4, 0.001, 0.0, 1.0, -1.0, 1.0)
+    with pytest.raises(bkma.BkmaError):
+        _plan(bkma, p, dtype="f64", impl="plain").set_fusion(4)
+    long_lines = AdvParams(2, 40000, 4, 0.001, 0.0, 1.0, -1.0, 1.0)
+    with pytest.raises(bkma.BkmaError):
+        _plan(bkma, long_lines, dtype="f32").set_fusion(4)
+    with pytest.raises(bkma.BkmaError):
+        _plan(bkma, p, dtype="f32").set_fusion(0)
