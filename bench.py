@@ -362,7 +362,7 @@ def extras(plan, bkma_gb300, dev, vel, kw, cells):
                          "bit_identical_to_one_step_per_launch": same}
         del a2
     out["fused_steps"] = {"steps_per_launch": fused, "steps": CFG_STEPS,
-                          "kernel": "adv_fused<float,6> (512 threads, 16-column strips)",
+                          "kernel": "adv_fused_f32<6> (512 threads, 8-column strips, two shared buffers)",
                           "note": "not the metric: state stays in shared memory between steps"}
     del a1, fz
     del ref, f

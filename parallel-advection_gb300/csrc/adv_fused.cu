@@ -103,6 +103,145 @@ __global__ void __launch_bounds__(kFuseThreads) adv_fused(AdvStagedArgs<T> a, in
     }
 }
 
+// FP32 form: two shared buffers (the step reads one and writes the other,
+// one barrier per step, the periodic wrap by index arithmetic), four
+// columns x kRowsF32 consecutive rows per thread with the taps in a float4
+// register ring (one new row load per output row) and packed FP32x2 FMAs in
+// the staged kernel's order (same bits). The odd row count puts the rows
+// that the eight threads of a 16-byte shared-memory phase read on different
+// banks. Lines with per-cell stencils (exception lines) load their taps per
+// row.
+constexpr int kRowsF32 = 9;
+
+template <int NT>
+__global__ void __launch_bounds__(kFuseThreads) adv_fused_f32(AdvStagedArgs<float> a, int ksteps) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int C = NT / 2 - 1;
+    TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, 1, a.W, a.ncb);
+    const int n1 = (int)a.n1;
+    const int wc = tc.wc;
+    const int ws = (wc + 3) & ~3;
+    float *buf0 = reinterpret_cast<float *>(smem_raw);
+    float *buf1 = buf0 + (size_t)n1 * ws;
+    const int64_t line = tc.line0;
+    stage_tile_elems<float>(buf0, a.src, a.n1, a.n2, line, 1, tc.c0, wc, ws, 0, n1 * ws);
+    const int exc = a.exc_index[line];
+    const int base = exc < 0 ? a.base[line] : 0;
+    float2 w2[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        const float wk = exc < 0 ? a.w[line * NT + k] : 0.f;
+        w2[k] = make_float2(wk, wk);
+    }
+    const AdvExcCell<float> *cells = exc < 0 ? nullptr : a.exc + (int64_t)exc * n1;
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const int G = ws >> 2;  // column groups
+    const int g4 = ((int)threadIdx.x % G) * 4;
+    const int r0 = ((int)threadIdx.x / G) * kRowsF32;
+    const int nr = max(0, min(kRowsF32, n1 - r0));
+    auto cell = [&](const float4 (&f)[NT], const float2 (&wv)[NT]) -> float4 {
+        const float2 cl = make_float2(f[C].x, f[C].y);
+        const float2 ch = make_float2(f[C].z, f[C].w);
+        float2 al = make_float2(0.f, 0.f), ah = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            if (k == C) continue;
+            al = __ffma2_rn(wv[k], __ffma2_rn(cl, m1, make_float2(f[k].x, f[k].y)), al);
+            ah = __ffma2_rn(wv[k], __ffma2_rn(ch, m1, make_float2(f[k].z, f[k].w)), ah);
+        }
+        const float2 ol = __fadd2_rn(cl, al), oh = __fadd2_rn(ch, ah);
+        return make_float4(ol.x, ol.y, oh.x, oh.y);
+    };
+    float *in = buf0, *out = buf1;
+    for (int step = 0; step < ksteps; ++step) {
+        if (nr > 0 && exc < 0) {
+            int q0 = r0 + base;
+            if (q0 >= n1) q0 -= n1;
+            auto row = [&](int i) -> float4 {
+                int q = q0 + i;
+                if (q >= n1) q -= n1;
+                return *reinterpret_cast<const float4 *>(in + q * ws + g4);
+            };
+            float4 ring[NT];
+#pragma unroll
+            for (int i = 0; i < NT - 1; ++i) ring[i] = row(i);
+#pragma unroll
+            for (int i = 0; i < kRowsF32; ++i) {
+                ring[(i + NT - 1) % NT] = row(i + NT - 1);
+                if (i < nr) {
+                    float4 f[NT];
+#pragma unroll
+                    for (int k = 0; k < NT; ++k) f[k] = ring[(i + k) % NT];
+                    *reinterpret_cast<float4 *>(out + (r0 + i) * ws + g4) = cell(f, w2);
+                }
+            }
+        } else if (nr > 0) {
+            for (int i = 0; i < nr; ++i) {
+                const AdvExcCell<float> &e = cells[r0 + i];
+                int q = r0 + i + e.base;
+                if (q >= n1) q -= n1;
+                float4 f[NT];
+                float2 wv[NT];
+#pragma unroll
+                for (int k = 0; k < NT; ++k) {
+                    int qk = q + k;
+                    if (qk >= n1) qk -= n1;
+                    f[k] = *reinterpret_cast<const float4 *>(in + qk * ws + g4);
+                    wv[k] = make_float2(e.w[k], e.w[k]);
+                }
+                *reinterpret_cast<float4 *>(out + (r0 + i) * ws + g4) = cell(f, wv);
+            }
+        }
+        __syncthreads();
+        float *t = in;
+        in = out;
+        out = t;
+    }
+    float *Gp = a.dst + line * a.n1 * a.n2 + tc.c0;
+    for (int i = threadIdx.x; i < n1 * wc; i += blockDim.x) {
+        const int r = i / wc, cc = i - r * wc;
+        Gp[(int64_t)r * a.n2 + cc] = in[r * ws + cc];
+    }
+}
+
+int fused_f32_w(const AdvPlanImpl &p, size_t max_smem) {
+    // 8-column strips (three CTAs per SM for n1 = 1024); narrower for longer
+    // lines, so that rowblocks x kRowsF32 covers n1
+    for (int w : {8, 4}) {
+        const int ws = w;
+        const int rowblocks = kFuseThreads / (ws / 4);
+        const size_t smem = 2 * (size_t)p.desc.n1 * ws * sizeof(float);
+        if ((int64_t)rowblocks * kRowsF32 >= p.desc.n1 && smem <= max_smem) return w;
+    }
+    return 0;
+}
+
+template <int NT>
+cudaError_t launch_fused_f32(const AdvPlanImpl &p, const void *src, void *dst, int W, int ksteps,
+                             cudaStream_t st) {
+    AdvStagedArgs<float> a{};
+    a.src = (const float *)src;
+    a.dst = (float *)dst;
+    a.n1 = p.desc.n1;
+    a.n2 = p.desc.n2;
+    a.lines = p.lines;
+    a.W = W;
+    a.R = 1;
+    a.ncb = p.ncb(W);
+    a.base = p.d_base;
+    a.w = (const float *)p.d_w;
+    a.exc_index = p.d_exc_index;
+    a.exc = (const AdvExcCell<float> *)p.d_exc;
+    a.line_list = nullptr;
+    const size_t smem = 2 * (size_t)p.desc.n1 * ((W + 3) & ~3) * sizeof(float);
+    auto kern = adv_fused_f32<NT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)p.tiles(W, 1), kFuseThreads, smem, st>>>(a, ksteps);
+    return cudaGetLastError();
+}
+
 template <typename T, int NT>
 cudaError_t launch_fused_t(const AdvPlanImpl &p, const void *src, void *dst, int W, int ksteps,
                            cudaStream_t st) {
@@ -144,6 +283,10 @@ cudaError_t launch_fused_npts(const AdvPlanImpl &p, const void *src, void *dst, 
 }  // namespace
 
 int adv_fused_tile_w(const AdvPlanImpl &p, size_t max_smem) {
+    if (p.desc.dtype == BKMA_F32) {
+        const int w = fused_f32_w(p, max_smem);
+        if (w) return w;
+    }
     // widest strip with at most fuse_rows rows per thread that fits
     for (int w : {16, 8, 4, 2, 1}) {
         if (w > p.desc.n2 && w != 1) continue;
@@ -158,7 +301,17 @@ int adv_fused_tile_w(const AdvPlanImpl &p, size_t max_smem) {
 
 cudaError_t adv_fused_launch(const AdvPlanImpl &p, const void *src, void *dst, int W, int k,
                              cudaStream_t st) {
-    if (p.desc.dtype == BKMA_F32) return launch_fused_npts<float>(p, src, dst, W, k, st);
+    if (p.desc.dtype == BKMA_F32) {
+        if (W == fused_f32_w(p, (size_t)227 * 1024)) {
+            switch (p.npts) {
+            case 4: return launch_fused_f32<4>(p, src, dst, W, k, st);
+            case 6: return launch_fused_f32<6>(p, src, dst, W, k, st);
+            case 10: return launch_fused_f32<10>(p, src, dst, W, k, st);
+            default: return cudaErrorInvalidValue;
+            }
+        }
+        return launch_fused_npts<float>(p, src, dst, W, k, st);
+    }
     return launch_fused_npts<double>(p, src, dst, W, k, st);
 }
 
