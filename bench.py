@@ -297,6 +297,37 @@ def run_gpu(args):
     return 0
 
 
+def fused_block(bkma_gb300, dev, f, plan, vel, kw, cells):
+    """Multi-step fusion, reported apart from the metric: k steps per launch
+    on shared-memory strips cut HBM traffic to 8/k B per cell-step. Each k is
+    checked bit for bit against `plan` (one step per launch) from field f."""
+    import torch
+    st = torch.cuda.current_stream()
+    fz = bkma_gb300.AdvectionPlan(N0, N1, N2, dtype="f32", velocity=vel, **kw)
+    a1 = f.clone()
+    plan.step(a1, nsteps=CFG_STEPS)
+    fused = {}
+    for k in (5, 10, 25):
+        fz.set_fusion(k)
+        a2 = f.clone()
+        fz.step(a2, nsteps=CFG_STEPS)
+        same = bool(torch.equal(a1, a2))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(st)
+        fz.step(a2, nsteps=CFG_STEPS)
+        b.record(st)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / CFG_STEPS
+        fused[str(k)] = {"gcells_s": cells / (ms / 1e3) / 1e9, "hbm_bytes_per_cell_step": 8.0 / k,
+                         "bit_identical_to_one_step_per_launch": same}
+        del a2
+    del a1, fz
+    return {"steps_per_launch": fused, "steps": CFG_STEPS,
+            "kernel": "adv_fused_f32<6> (512 threads, 8-column strips, two shared buffers)",
+            "note": "not the metric: state stays in shared memory between steps"}
+
+
 def extras(plan, bkma_gb300, dev, vel, kw, cells):
     """Error of the 50-step FP32 run against the FP64 plain form (the
     reference's per-cell math, bit-identical to the oracle), and the speed of
@@ -346,25 +377,7 @@ def extras(plan, bkma_gb300, dev, vel, kw, cells):
         "speedup_vs_plain_fp64": ms_plain / f32ms,
         "speedup_vs_staged_fp64": ms_staged64 / f32ms,
     }
-    # Multi-step fusion, reported apart from the metric: k steps per launch on
-    # shared-memory strips cut HBM traffic to 8/k B per cell-step.
-    fz = bkma_gb300.AdvectionPlan(N0, N1, N2, dtype="f32", velocity=vel, **kw)
-    a1 = f.clone()
-    plan.step(a1, nsteps=CFG_STEPS)
-    fused = {}
-    for k in (5, 10, 25):
-        fz.set_fusion(k)
-        a2 = f.clone()
-        fz.step(a2, nsteps=CFG_STEPS)
-        same = bool(torch.equal(a1, a2))
-        ms = timed(fz, a2, CFG_STEPS)
-        fused[str(k)] = {"gcells_s": cells / (ms / 1e3) / 1e9, "hbm_bytes_per_cell_step": 8.0 / k,
-                         "bit_identical_to_one_step_per_launch": same}
-        del a2
-    out["fused_steps"] = {"steps_per_launch": fused, "steps": CFG_STEPS,
-                          "kernel": "adv_fused_f32<6> (512 threads, 8-column strips, two shared buffers)",
-                          "note": "not the metric: state stays in shared memory between steps"}
-    del a1, fz
+    out["fused_steps"] = fused_block(bkma_gb300, dev, f, plan, vel, kw, cells)
     del ref, f
     torch.cuda.empty_cache()
     return out
@@ -442,7 +455,7 @@ def conv_block(bkma_gb300, dev, batch: int = 256, with_fp64: bool = True):
     return out
 
 
-def batched_block(bkma_gb300, dev, nfields: int = 64, steps: int = 10):
+def batched_block(bkma_gb300, dev, nfields: int = 64, steps: int = 10, autotune: bool = True):
     """Batched uneven advection: 64 fields advanced by one graph launch per
     step (streamed kernels per tap count + the persistent staged kernel for
     what cannot stream), n0 ~ U{64..1024}, n1 in {256, 512, 1024, 2048}, n2 ~ U{1..256},
@@ -470,7 +483,7 @@ def batched_block(bkma_gb300, dev, nfields: int = 64, steps: int = 10):
                                minX=0.0, maxX=1.0, minVx=-2.0, maxVx=2.0,
                                velocity=rng.uniform(-2.0, 2.0, n0)))
         batch = bkma_gb300.AdvectionBatch(fields, dtype="f32")
-        tiles = batch.autotune()
+        tiles = batch.autotune() if autotune else batch.tiles()
         st = torch.cuda.current_stream()
         batch.step(3)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -620,7 +633,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip error/e2e/cpu/conv blocks")
     ap.add_argument("--n0", type=int, default=None, help="smaller field for profiling captures")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", default="advection", choices=["advection", "conv", "batched", "learned"],
+    ap.add_argument("--workload", default="advection", choices=["advection", "conv", "batched", "learned", "fused"],
                     help="conv: only the conv1d block, as its own JSON line")
     ap.add_argument("--conv-batch", type=int, default=256, help="smaller batch for captures")
     ap.add_argument("--fields", type=int, default=64, help="batched workload: field count")
@@ -630,12 +643,23 @@ def main():
         N0 = args.n0
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload in ("batched", "learned") and args.impl != "reference":
+    if args.workload in ("batched", "learned", "fused") and args.impl != "reference":
         import torch
         import bkma_gb300
         dev = torch.device("cuda", 0)
+        if args.workload == "fused":
+            vel = velocities(N0)
+            kw = dict(dt=DT, minX=MINX, maxX=MAXX, minVx=-1.0, maxVx=1.0)
+            plan = bkma_gb300.AdvectionPlan(N0, N1, N2, dtype="f32", velocity=vel, **kw)
+            f = torch.empty((N0, N1, N2), dtype=torch.float32, device=dev)
+            plan.fill(f, mode=1, amp=NOISE, seed=SEED)
+            r = {"workload": f"fused advection steps {N0}x{N1}x{N2} FP32, {CFG_STEPS} steps",
+                 **fused_block(bkma_gb300, dev, f, plan, vel, kw, N0 * N1 * N2)}
+            print(json.dumps(r))
+            return 0
         if args.workload == "batched":
-            r = batched_block(bkma_gb300, dev, nfields=args.fields)
+            r = batched_block(bkma_gb300, dev, nfields=args.fields,
+                              autotune=not args.no_autotune)
         else:
             r = learned_block(bkma_gb300, dev)
         print(json.dumps(r))
