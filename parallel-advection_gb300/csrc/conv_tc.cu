@@ -36,10 +36,12 @@ namespace bkma {
 namespace tc {
 
 constexpr int TILE = 128;   // output positions per item = N of every MMA
-constexpr int STAGES_MAX = 4;
+constexpr int STAGES_MAX = 6;
 constexpr int TMEM_COLS = 512;
-constexpr int ACC_COL0 = 256;     // two FP32 accumulators of 128 columns: 256, 384
-constexpr int W_TMEM_COLS = 256;  // TMEM columns for weights (taps 0 .. taps_tmem-1)
+// TMEM: weights of taps 0 .. taps_tmem-1 in columns [0, 512 - 128 nacc), then
+// nacc FP32 accumulators of 128 columns. One accumulator leaves 384 columns
+// for weights (6 taps of Cin = 128 instead of 4): the MMAs of the next item
+// wait only until the epilogue has read the accumulator into registers.
 constexpr int SMEM_LIMIT = 232448 - 1024;
 constexpr int NUM_EPI_WARPS = 4;
 constexpr int NUM_PROD_WARPS = 8;  // two groups of 4 warps, alternate items
@@ -53,7 +55,7 @@ struct Args {
     const __nv_bfloat16 *w;   // (Cout, Cin, K)
     const __nv_bfloat16 *bias;  // (Cout) or null
     const __nv_bfloat16 *halo;  // [B][ntiles][Cin][halo_rows] or null (out of place)
-    const uint32_t *wpack_tmem;  // [128][256] BF16 pairs: TMEM image of taps 0..taps_tmem-1
+    const uint32_t *wpack_tmem;  // [128][tm_cols] BF16 pairs: TMEM image of taps 0..taps_tmem-1
     const uint4 *wpack_smem;     // shared-memory image of taps taps_tmem..K-1
     int B, cin, cout, K;
     int64_t L, lout, out_stride;
@@ -63,6 +65,8 @@ struct Args {
     int stage_bytes;
     int stages;      // activation stages (2..STAGES_MAX)
     int taps_tmem;   // taps whose weights live in TMEM; the rest live in shared memory
+    int nacc;        // FP32 accumulators in TMEM (1 or 2)
+    int tm_cols;     // TMEM columns of the weight image: 512 - 128 * nacc
     int wsmem_bytes; // shared-memory weights, placed before the stages
     int *status;     // device status word (0 ok, 4 timeout)
 };
@@ -226,15 +230,16 @@ __device__ __forceinline__ void store_block(unsigned char *dst, const uint4 (&v)
 // output channel) and the shared-memory image of the other taps
 // ([tap][ci-chunk][co][8 ci], K-major no-swizzle A tiles of 128 rows).
 __global__ void conv_tc_pack_weights(const __nv_bfloat16 *w, int cin, int cout, int K,
-                                     int taps_tmem, uint32_t *tm_img, uint32_t *sm_img) {
+                                     int taps_tmem, int tm_cols, uint32_t *tm_img,
+                                     uint32_t *sm_img) {
     const int wcols = taps_tmem * cin / 2;
-    const int nA = 128 * 256;
+    const int nA = 128 * tm_cols;
     const int nB = (K - taps_tmem) * (cin / 8) * 128 * 4;  // 32-bit words
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA + nB; i += gridDim.x * blockDim.x) {
         int co, k, ci;
         if (i < nA) {
-            co = i / 256;
-            const int col = i % 256;
+            co = i / tm_cols;
+            const int col = i % tm_cols;
             if (col >= wcols || co >= cout) {
                 tm_img[i] = 0;
                 continue;
@@ -314,7 +319,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
         const int co = threadIdx.x;
         const int wcols = a.taps_tmem * cin / 2;
         const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.wpack_tmem + (size_t)co * 256);
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.wpack_tmem + (size_t)co * a.tm_cols);
         for (int c0 = 0; c0 < wcols; c0 += 32) {
             uint32_t v[32];
 #pragma unroll
@@ -395,11 +400,11 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
                 const int s = it % stages;
                 const uint32_t ph = (uint32_t)(it / stages) & 1u;
                 if (!mbar_wait(&full_bar[s], ph, &abort_flag, a.status)) break;
-                const int acc = it & 1;
-                const uint32_t aph = (uint32_t)(it >> 1) & 1u;
+                const int acc = a.nacc == 2 ? (it & 1) : 0;
+                const uint32_t aph = (uint32_t)(a.nacc == 2 ? (it >> 1) : it) & 1u;
                 if (!mbar_wait(&acce_bar[acc], aph ^ 1u, &abort_flag, a.status)) break;
                 fence_after();
-                const uint32_t d_tmem = tmem + (uint32_t)(ACC_COL0 + acc * TILE);
+                const uint32_t d_tmem = tmem + (uint32_t)(a.tm_cols + acc * TILE);
                 // descriptor low word: start address >> 4 (bits 0-13, < 256 KB so
                 // row / chunk offsets never carry into the LBO field at bit 16)
                 const uint32_t lo0 = ((stage0 + (uint32_t)(s * a.stage_bytes)) >> 4) | (lbo16 << 16);
@@ -427,13 +432,13 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
     } else if (is_epi) {
         const int co = threadIdx.x;
         const float bias = (a.bias && co < a.cout) ? __bfloat162float(a.bias[co]) : 0.0f;
-        const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)ACC_COL0;
+        const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)a.tm_cols;
         int it = 0;
         for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
-            const int acc = it & 1;
-            const uint32_t aph = (uint32_t)(it >> 1) & 1u;
+            const int acc = a.nacc == 2 ? (it & 1) : 0;
+            const uint32_t aph = (uint32_t)(a.nacc == 2 ? (it >> 1) : it) & 1u;
             if (!mbar_wait(&accf_bar[acc], aph, &abort_flag, a.status)) break;
             fence_after();
             const int64_t l0 = (int64_t)tile * TILE;
@@ -500,13 +505,17 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
 
 namespace {
 struct TcLayout {
-    int taps_tmem, wsmem_bytes, halo_rows, chunk_rows, stage_bytes, stages;
+    int taps_tmem, nacc, tm_cols, wsmem_bytes, halo_rows, chunk_rows, stage_bytes, stages;
 };
 
 TcLayout tc_layout(const bkma_conv_desc &d) {
     TcLayout t;
     const int cin = (int)d.cin, K = (int)d.ksize;
-    t.taps_tmem = std::min(K, tc::W_TMEM_COLS / (cin / 2));
+    // one accumulator when that moves more weight taps into TMEM
+    const int taps2 = std::min(K, 256 / (cin / 2)), taps1 = std::min(K, 384 / (cin / 2));
+    t.nacc = taps1 > taps2 ? 1 : 2;
+    t.tm_cols = tc::TMEM_COLS - 128 * t.nacc;
+    t.taps_tmem = t.nacc == 1 ? taps1 : taps2;
     t.wsmem_bytes = (K - t.taps_tmem) * cin * 256;
     t.wsmem_bytes = (t.wsmem_bytes + 1023) / 1024 * 1024;
     t.halo_rows = std::max(8, (K - 1 + 7) / 8 * 8);
@@ -534,7 +543,7 @@ bkma_status conv_tc_plan_init(ConvPlanImpl &p) {
     p.ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
     p.halo_width = t.halo_rows;
     p.halo_bytes = 2 * (size_t)(d.batch * p.ntiles * d.cin * p.halo_width);
-    p.wpack_bytes = (size_t)128 * 256 * 4 + (size_t)t.wsmem_bytes;
+    p.wpack_bytes = (size_t)128 * t.tm_cols * 4 + (size_t)t.wsmem_bytes;
     BKMA_CUDA_TRY(cudaMalloc(&p.d_wpack, p.wpack_bytes));
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -559,9 +568,9 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
     }
     const TcLayout t = tc_layout(d);
     uint32_t *tm_img = (uint32_t *)p.d_wpack;
-    uint32_t *sm_img = tm_img + 128 * 256;
+    uint32_t *sm_img = tm_img + 128 * t.tm_cols;
     tc::conv_tc_pack_weights<<<64, 256, 0, st>>>((const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout,
-                                                 (int)d.ksize, t.taps_tmem, tm_img, sm_img);
+                                                 (int)d.ksize, t.taps_tmem, t.tm_cols, tm_img, sm_img);
     BKMA_CUDA_TRY(cudaGetLastError());
     tc::Args a;
     a.x = (const __nv_bfloat16 *)data;
@@ -582,6 +591,8 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
     a.stage_bytes = t.stage_bytes;
     a.stages = t.stages;
     a.taps_tmem = t.taps_tmem;
+    a.nacc = t.nacc;
+    a.tm_cols = t.tm_cols;
     a.wsmem_bytes = t.wsmem_bytes;
     a.wpack_tmem = tm_img;
     a.wpack_smem = reinterpret_cast<const uint4 *>(sm_img);
@@ -623,7 +634,7 @@ bkma_status conv_tc_scratch_need(const bkma_conv_desc &d, size_t *halo_bytes, si
                     "tensor path: ksize*cin too large for on-chip weights (TMEM + shared memory)");
     const int64_t ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
     *halo_bytes = ((size_t)2 * (size_t)(d.batch * ntiles * d.cin * t.halo_rows) + 255) / 256 * 256;
-    *wpack_bytes = ((size_t)128 * 256 * 4 + (size_t)t.wsmem_bytes + 255) / 256 * 256;
+    *wpack_bytes = ((size_t)128 * t.tm_cols * 4 + (size_t)t.wsmem_bytes + 255) / 256 * 256;
     return BKMA_OK;
 }
 
@@ -642,9 +653,9 @@ bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w,
         if (s != BKMA_OK) return s;
     }
     uint32_t *tm_img = (uint32_t *)wpack;
-    uint32_t *sm_img = tm_img + 128 * 256;
+    uint32_t *sm_img = tm_img + 128 * t.tm_cols;
     tc::conv_tc_pack_weights<<<64, 256, 0, st>>>((const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout,
-                                                 (int)d.ksize, t.taps_tmem, tm_img, sm_img);
+                                                 (int)d.ksize, t.taps_tmem, t.tm_cols, tm_img, sm_img);
     BKMA_CUDA_TRY(cudaGetLastError());
     tc::Args a;
     a.x = (const __nv_bfloat16 *)data;
@@ -665,6 +676,8 @@ bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w,
     a.stage_bytes = t.stage_bytes;
     a.stages = t.stages;
     a.taps_tmem = t.taps_tmem;
+    a.nacc = t.nacc;
+    a.tm_cols = t.tm_cols;
     a.wsmem_bytes = t.wsmem_bytes;
     a.wpack_tmem = tm_img;
     a.wpack_smem = reinterpret_cast<const uint4 *>(sm_img);

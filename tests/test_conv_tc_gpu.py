@@ -19,6 +19,8 @@ SHAPES = [
     (3, 64, 1000, 5),
     (2, 128, 1024, 7),
     (1, 128, 8192, 7),
+    (2, 128, 1000, 9),   # taps 0-5 in TMEM (one accumulator), 6-8 in shared memory
+    (2, 96, 512, 11),
 ]
 
 
@@ -114,5 +116,5 @@ def test_tensor_conv_rejects_unsupported(bkma, cuda):
     with pytest.raises(bkma.BkmaError) as e:
         bkma.Conv1dPlan(2, 24, 24, 256, 3, dtype="bf16", impl="tensor")
     assert e.value.status == 2
-    with pytest.raises(bkma.BkmaError):
-        bkma.Conv1dPlan(2, 128, 128, 256, 9, dtype="bf16", impl="tensor")
+    with pytest.raises(bkma.BkmaError):  # 7 taps of shared-memory weights leave no stages
+        bkma.Conv1dPlan(2, 128, 128, 256, 13, dtype="bf16", impl="tensor")
