@@ -236,6 +236,17 @@ bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const voi
 bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream);
 bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan);
 
+/* fill_buffer_conv1d (src/tools/init.hpp:50-72): `count` elements of a
+ * device buffer of `dtype` (F32, F64 or BF16) set to `value`. */
+bkma_status bkma_fill(void *data, int64_t count, int32_t dtype, double value, void *stream);
+/* sum_and_normalize_conv1d + validate_conv1d (src/tools/validation.hpp:
+ * 84-156) in one pass over the device field (n0, n1, n2): *mean = the mean of
+ * the values (i0, i1 < nw, i2), summed in FP64 in a fixed order; *equal = 1
+ * when every value at a given i1 < nw is the same for all (i0, i2) (a NaN
+ * counts as different), else 0. Synchronizes `stream`. */
+bkma_status bkma_conv_check(const void *data, int32_t dtype, int64_t n0, int64_t n1, int64_t n2,
+                            int64_t nw, double *mean, int32_t *equal, void *stream);
+
 /* In-place BF16 tensor-core conv1d (torch semantics, cin = cout = channels,
  * data (batch, channels, length), weight (channels, channels, ksize), bias
  * (channels) or NULL) that allocates nothing. No counterpart in the

@@ -48,6 +48,23 @@ def shard_lines(n0: int, rank: int, world: int) -> tuple[int, int]:
     return offset, base + (1 if rank < extra else 0)
 
 
+def fill(data, value: float, stream=None):
+    """fill_buffer_conv1d's constant fill of a CUDA tensor (F32/F64/BF16)."""
+    check(load().bkma_fill(_ptr(data), data.numel(), _DT[_dtype_name(data)], value,
+                           _stream(stream)))
+    return data
+
+
+def conv_check(data, nw: int, stream=None) -> tuple[float, bool]:
+    """sum_and_normalize_conv1d + validate_conv1d on a (n0, n1, n2) CUDA
+    tensor: (mean of the first nw values per line, all equal per i1)."""
+    n0, n1, n2 = data.shape
+    mean, equal = C.c_double(), C.c_int32()
+    check(load().bkma_conv_check(_ptr(data), _DT[_dtype_name(data)], n0, n1, n2, nw,
+                                 C.byref(mean), C.byref(equal), _stream(stream)))
+    return mean.value, bool(equal.value)
+
+
 def impl_from_name(name: str) -> tuple[int, bool]:
     """impl_selector (src/tools/impl_selector.hpp:31-49) over the C ABI."""
     impl, inplace = C.c_int32(), C.c_int32()

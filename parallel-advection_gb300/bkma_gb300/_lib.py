@@ -91,6 +91,9 @@ SIGNATURES = {
     "bkma_conv_run": (_st, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "bkma_conv_plan_status": (_st, [_vp, _vp]),
     "bkma_conv_plan_destroy": (_st, [_vp]),
+    "bkma_fill": (_st, [_vp, C.c_int64, C.c_int32, C.c_double, _vp]),
+    "bkma_conv_check": (_st, [_vp, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64, _dp,
+                              _i32p, _vp]),
     "bkma_conv1d_bf16_inplace_noalloc": (_st, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64,
                                                C.c_int64, _vp]),
     "bkma_mlp_create": (_st, [C.c_uint64, C.POINTER(_vp)]),

@@ -29,17 +29,6 @@ static void cuda_check(cudaError_t e, const char *what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// sum_and_normalize_conv1d (src/tools/validation.hpp:84-110): mean of
-// data(i0, i1, i2) over i1 < nw.
-static double sum_and_normalize(const std::vector<double> &h, size_t n0, size_t n1, size_t n2,
-                                size_t nw) {
-    double sum = 0;
-    for (size_t i0 = 0; i0 < n0; ++i0)
-        for (size_t i1 = 0; i1 < nw; ++i1)
-            for (size_t i2 = 0; i2 < n2; ++i2) sum += h[(i0 * n1 + i1) * n2 + i2];
-    return sum / (double)(n0 * nw * n2);
-}
-
 int main(int argc, char **argv) {
     try {
         const std::string input_file = argc > 1 ? argv[1] : "conv1d.ini";
@@ -53,16 +42,17 @@ int main(int argc, char **argv) {
 
         const size_t n0 = p.n0, n1 = p.n1, n2 = p.n2, k = p.k, cin = p.channel_in;
         const size_t cells = n0 * n1 * n2;
-        std::vector<double> h(cells, 7.3), hw(cells, 1.0), hwt(k * cin * cin, 1.5), hb(cin, 1.0);
+        const size_t nweight = k * cin * cin;
         double *data = nullptr, *warm = nullptr, *weight = nullptr, *bias = nullptr;
         cuda_check(cudaMalloc(&data, cells * 8), "cudaMalloc");
         cuda_check(cudaMalloc(&warm, cells * 8), "cudaMalloc");
-        cuda_check(cudaMalloc(&weight, hwt.size() * 8), "cudaMalloc");
-        cuda_check(cudaMalloc(&bias, hb.size() * 8), "cudaMalloc");
-        cuda_check(cudaMemcpy(data, h.data(), cells * 8, cudaMemcpyHostToDevice), "H2D");
-        cuda_check(cudaMemcpy(warm, hw.data(), cells * 8, cudaMemcpyHostToDevice), "H2D");
-        cuda_check(cudaMemcpy(weight, hwt.data(), hwt.size() * 8, cudaMemcpyHostToDevice), "H2D");
-        cuda_check(cudaMemcpy(bias, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice), "H2D");
+        cuda_check(cudaMalloc(&weight, nweight * 8), "cudaMalloc");
+        cuda_check(cudaMalloc(&bias, cin * 8), "cudaMalloc");
+        // fill_buffer_conv1d (src/tools/init.hpp:50-72), on the device
+        check(bkma_fill(data, (int64_t)cells, BKMA_F64, 7.3, nullptr));
+        check(bkma_fill(warm, (int64_t)cells, BKMA_F64, 1.0, nullptr));
+        check(bkma_fill(weight, (int64_t)nweight, BKMA_F64, 1.5, nullptr));
+        check(bkma_fill(bias, (int64_t)cin, BKMA_F64, 1.0, nullptr));
 
         bkma_conv_desc d{};
         d.batch = (int64_t)n0;
@@ -78,8 +68,13 @@ int main(int argc, char **argv) {
         bkma_conv_plan *plan = nullptr;
         check(bkma_conv_plan_create(&d, &plan));
 
-        std::cout << std::endl
-                  << "Normalized Array before: " << sum_and_normalize(h, n0, n1, n2, n1) << std::endl;
+        // sum_and_normalize_conv1d + validate_conv1d (src/tools/validation.hpp:
+        // 84-156) as one device pass
+        double mean = 0;
+        int32_t equal = 0;
+        check(bkma_conv_check(data, BKMA_F64, (int64_t)n0, (int64_t)n1, (int64_t)n2,
+                              (int64_t)n1, &mean, &equal, nullptr));
+        std::cout << std::endl << "Normalized Array before: " << mean << std::endl;
         for (int i = 0; i < 3; ++i) {  // warm-up
             check(bkma_conv_run(plan, warm, nullptr, weight, bias, nullptr));
             cuda_check(cudaDeviceSynchronize(), "warm-up");
@@ -90,21 +85,10 @@ int main(int argc, char **argv) {
         const auto end = std::chrono::high_resolution_clock::now();
         const double elapsed = std::chrono::duration<double>(end - start).count();
 
-        cuda_check(cudaMemcpy(h.data(), data, cells * 8, cudaMemcpyDeviceToHost), "D2H");
-        std::cout << "Normalized Array after: " << sum_and_normalize(h, n0, n1, n2, p.n_write)
-                  << std::endl
-                  << std::endl;
-        // validate_conv1d (src/tools/validation.hpp:114-156)
-        bool differ = false;
-        for (size_t i0 = 0; i0 < n0 && !differ; ++i0)
-            for (size_t i1 = 0; i1 < p.n_write && !differ; ++i1)
-                for (size_t i2 = 0; i2 + 1 < n2; ++i2)
-                    if (h[(i0 * n1 + i1) * n2 + i2] != h[(i0 * n1 + i1) * n2 + i2 + 1]) differ = true;
-        for (size_t i2 = 0; i2 < n2 && !differ; ++i2)
-            for (size_t i1 = 0; i1 < p.n_write && !differ; ++i1)
-                for (size_t i0 = 0; i0 + 1 < n0; ++i0)
-                    if (h[(i0 * n1 + i1) * n2 + i2] != h[((i0 + 1) * n1 + i1) * n2 + i2]) differ = true;
-        if (differ)
+        check(bkma_conv_check(data, BKMA_F64, (int64_t)n0, (int64_t)n1, (int64_t)n2,
+                              (int64_t)p.n_write, &mean, &equal, nullptr));
+        std::cout << "Normalized Array after: " << mean << std::endl << std::endl;
+        if (!equal)
             std::cout << "WARNING: Values at same position i1 are not equivalent throught the "
                          "batchs. Check implementation."
                       << std::endl;

@@ -92,3 +92,31 @@ def test_torch_semantics_fp32(bkma, cuda, oracle):
 def test_halo_scratch_is_reported(bkma, cuda):
     plan = bkma.Conv1dPlan(2, 8, 8, 512, 7, dtype="f32", impl="plain")
     assert plan.scratch_bytes() == 4 * 2 * ((512 - 7 + 1 + 63) // 64) * 8 * 6
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f64", "bf16"])
+def test_device_fill_and_conv_check(bkma, cuda, dtype):
+    """fill_buffer_conv1d and the conv1d checks (validation.hpp:84-156) on
+    the device: a constant field is all-equal with the constant as mean; a
+    changed value breaks equality; the mean of random data equals numpy's
+    over the first nw values of every line."""
+    import torch
+    tdt = {"f32": torch.float32, "f64": torch.float64, "bf16": torch.bfloat16}[dtype]
+    n0, n1, n2, nw = 5, 300, 7, 250
+    d = torch.empty((n0, n1, n2), dtype=tdt, device=cuda)
+    bkma.fill(d, 7.3)
+    want = float(torch.tensor(7.3, dtype=tdt))
+    assert torch.equal(d, torch.full_like(d, 7.3))
+    mean, equal = bkma.conv_check(d, nw)
+    assert equal and abs(mean - want) <= 1e-12 * abs(want)
+    d[3, nw - 1, 6] = 1.0
+    assert not bkma.conv_check(d, nw)[1]
+    assert bkma.conv_check(d, nw - 1)[1]   # the changed value lies beyond nw - 1
+    d[3, 0, 0] = float("nan")
+    assert not bkma.conv_check(d, 1)[1]
+    r = torch.rand((n0, n1, n2), dtype=torch.float64, device=cuda).to(tdt)
+    mean, equal = bkma.conv_check(r, nw)
+    ref = r[:, :nw, :].double().cpu().numpy().mean()
+    assert not equal and abs(mean - ref) <= 1e-12
+    one = torch.full((1, 4, 1), float("nan"), dtype=tdt, device=cuda)
+    assert bkma.conv_check(one, 4)[1]  # nothing to compare, as in the reference
