@@ -157,6 +157,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
+}  // namespace
+
+void *tensor_map_encoder() { return reinterpret_cast<void *>(encode_fn()); }
+
+namespace {
+
 template <int NT, int WC>
 cudaError_t launch_tma_t(const AdvPlanImpl &p, const CUtensorMap &tm, const AdvTmaArgs &a,
                          int threads, size_t smem, int64_t grid, cudaStream_t st) {

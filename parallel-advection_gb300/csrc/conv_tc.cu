@@ -19,16 +19,27 @@
 //  * Producer warps load the tile from HBM with 16-byte loads along l,
 //    transpose 8x8 BF16 blocks in registers, and store conflict-free (the
 //    odd row count of a chunk spreads the 8 stores of a phase over all
-//    banks). Rows past the tile come from the halo snapshot (conv.cu), so
-//    tiles of one row can be overwritten in place concurrently.
+//    banks). A warp covers 8 consecutive channel chunks x 4 consecutive row
+//    blocks, so one load instruction touches 8 lines of 64 bytes. Rows past
+//    the tile come from the halo snapshot (conv.cu), so tiles of one row can
+//    be overwritten in place concurrently.
 //  * One thread issues the MMAs of a 128-position item (K taps x Cin/16
-//    K-steps) into one of two alternating TMEM accumulators; four epilogue
-//    warps drain the other (tcgen05.ld), add the bias, round to BF16 and store.
+//    K-steps) into a TMEM accumulator; four epilogue warps drain it
+//    (tcgen05.ld), add the bias and round to BF16. When the output rows are
+//    16-byte strided, each warp writes its 32 channels x 64 positions into a
+//    128-byte-swizzled shared tile (conflict-free) and one lane stores it
+//    with a TMA tensor store; otherwise lanes store their own rows.
+//    The shared-memory data path is the limit of this kernel (every N = 128
+//    MMA reads a 4 KB B tile: half its bandwidth at the tensor rate), so
+//    every other access is shaped for few wavefronts.
 //  * Every mbarrier wait is bounded; on timeout the CTA raises a status word,
 //    stops, drains its MMAs with a bounded wait and frees TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "conv.cuh"
 
@@ -49,7 +60,11 @@ constexpr int PROD_GROUP = 128;    // threads per producer group
 constexpr int THREADS = 32 * (NUM_EPI_WARPS + NUM_PROD_WARPS + 1);
 constexpr uint32_t kSpinLimit = 1u << 22;  // x ~ 0.25 us backoff: ~1 s
 
+constexpr int EPI_TILE_BYTES = 4096;  // 32 channels x 64 positions BF16
+constexpr int EPI_BYTES = NUM_EPI_WARPS * 2 * EPI_TILE_BYTES + 1024;  // + alignment slack
+
 struct Args {
+    CUtensorMap out_map;      // (lout, cout, B) view of out, 64 x 32 x 1 boxes, 128-B swizzle
     const __nv_bfloat16 *x;   // (B, Cin, L)
     __nv_bfloat16 *out;       // (B, Cout, out_stride)
     const __nv_bfloat16 *w;   // (Cout, Cin, K)
@@ -68,6 +83,8 @@ struct Args {
     int nacc;        // FP32 accumulators in TMEM (1 or 2)
     int tm_cols;     // TMEM columns of the weight image: 512 - 128 * nacc
     int wsmem_bytes; // shared-memory weights, placed before the stages
+    int epi_tma;     // 1: the epilogue stores through out_map
+    int epi_off;     // offset of the epilogue tiles (after the stages)
     int *status;     // device status word (0 ok, 4 timeout)
 };
 
@@ -209,6 +226,25 @@ __device__ __forceinline__ void load_block(const Args &a, int b, int tile, int c
     for (int j = 0; j < 8; ++j) v[j] = make_uint4(0, 0, 0, 0);
 }
 
+// Block p of an item's (channel chunk, row block) pairs. With a multiple of 8
+// chunks, 32 consecutive p cover chunks 8g..8g+7 x row blocks 4m..4m+3 of the
+// tile body (one 64-byte segment of 8 channel rows per load instruction; the
+// chunk residues 0..7 keep the transposed stores conflict-free), then the
+// halo blocks; otherwise chunks vary fastest.
+__device__ __forceinline__ void block_of(int p, int nchunks, int &c, int &q) {
+    const int body = nchunks * (TILE / 8);
+    if ((nchunks & 7) == 0 && p < body) {
+        c = (p & 7) + 8 * ((p >> 3) / (TILE / 8));
+        q = (p >> 3) % (TILE / 8);
+    } else if ((nchunks & 7) == 0) {
+        c = (p - body) % nchunks;
+        q = TILE / 8 + (p - body) / nchunks;
+    } else {
+        c = p % nchunks;
+        q = p / nchunks;
+    }
+}
+
 // Transpose an 8x8 BF16 block (v[j] = channel j, 8 positions) into 8 rows of
 // 8 channels and store them at dst + 16*i.
 __device__ __forceinline__ void store_block(unsigned char *dst, const uint4 (&v)[8]) {
@@ -271,7 +307,7 @@ __global__ void conv_tc_pack_weights(const __nv_bfloat16 *w, int cin, int cout, 
 }
 
 template <int KC>  // K16 steps per tap: Cin / 16
-__global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
+__global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_constant__ Args a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t full_bar[STAGES_MAX], empty_bar[STAGES_MAX];
     __shared__ __align__(8) uint64_t accf_bar[2], acce_bar[2];
@@ -367,18 +403,18 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
             // for Cin = 128: 16 chunks x 17 row blocks = 272 blocks / 128 threads)
             for (int p = pt; p < pairs; p += 3 * PROD_GROUP) {
                 uint4 v[3][8];
+                int bc[3], bq[3];
 #pragma unroll
                 for (int h = 0; h < 3; ++h) {
                     const int ph2 = p + h * PROD_GROUP;
-                    if (ph2 < pairs) load_block(a, b, tile, ph2 % nchunks, ph2 / nchunks, v[h]);
+                    block_of(ph2, nchunks, bc[h], bq[h]);
+                    if (ph2 < pairs) load_block(a, b, tile, bc[h], bq[h], v[h]);
                 }
 #pragma unroll
                 for (int h = 0; h < 3; ++h) {
                     const int ph2 = p + h * PROD_GROUP;
                     if (ph2 < pairs)
-                        store_block(stage + ((size_t)(ph2 % nchunks) * a.chunk_rows +
-                                             8 * (ph2 / nchunks)) * 16,
-                                    v[h]);
+                        store_block(stage + ((size_t)bc[h] * a.chunk_rows + 8 * bq[h]) * 16, v[h]);
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -433,6 +469,10 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
         const int co = threadIdx.x;
         const float bias = (a.bias && co < a.cout) ? __bfloat162float(a.bias[co]) : 0.0f;
         const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)a.tm_cols;
+        // this warp's two 4 KB swizzled output tiles (one per half item)
+        const uint32_t epi_tile =
+            ((smem_base + (uint32_t)a.epi_off + 1023u) & ~1023u) + (uint32_t)warp * 2u * EPI_TILE_BYTES;
+        const bool warp_rows = 32 * warp < a.cout;
         int it = 0;
         for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
             const int b = (int)(item / a.ntiles);
@@ -454,8 +494,53 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
                     fence_before();
                     mbar_arrive(&acce_bar[acc]);
                 }
-                if (co < a.cout) {
-                    const int64_t lh = l0 + 64 * half;
+                const int64_t lh = l0 + 64 * half;
+                if (a.epi_tma) {
+                    if (!warp_rows || lh >= a.lout) continue;
+                    uint32_t pk[32];
+#pragma unroll
+                    for (int e = 0; e < 32; ++e) {
+                        const float f0 = __uint_as_float(v[e / 16][(2 * e) % 32]) + bias;
+                        const float f1 = __uint_as_float(v[e / 16][(2 * e + 1) % 32]) + bias;
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
+                        pk[e] = *reinterpret_cast<const uint32_t *>(&h);
+                    }
+                    // The tensor map ends at lt = lout rounded down to 8 positions
+                    // (a tensor store clips in 16-byte units); lanes store the
+                    // last lout - lt values of their rows themselves.
+                    const int64_t lt = a.lout & ~(int64_t)7;
+                    if (lt < a.lout && lt < lh + 64 && co < a.cout) {
+                        __nv_bfloat16 *dst = a.out + ((int64_t)b * a.cout + co) * a.out_stride + lh;
+#pragma unroll
+                        for (int e = 0; e < 64; ++e)
+                            if (lh + e >= lt && lh + e < a.lout)
+                                dst[e] = __ushort_as_bfloat16(
+                                    (uint16_t)((pk[e / 2] >> (16 * (e & 1))) & 0xFFFFu));
+                    }
+                    if (lh >= lt) continue;
+                    // the store issued from this tile one item ago has read it
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                    __syncwarp();
+                    const uint32_t tile_addr = epi_tile + (uint32_t)half * EPI_TILE_BYTES;
+                    const uint32_t row_addr = tile_addr + (uint32_t)lane * 128u;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(
+                                         row_addr + ((uint32_t)(e ^ (lane & 7)) << 4)),
+                                     "r"(pk[4 * e]), "r"(pk[4 * e + 1]), "r"(pk[4 * e + 2]),
+                                     "r"(pk[4 * e + 3])
+                                     : "memory");
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) {
+                        asm volatile(
+                            "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], "
+                            "[%1];" ::"l"(reinterpret_cast<uint64_t>(&a.out_map)),
+                            "r"(tile_addr), "r"((int)lh), "r"(32 * warp), "r"(b)
+                            : "memory");
+                        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                    }
+                } else if (co < a.cout) {
                     uint32_t pk[32];
 #pragma unroll
                     for (int e = 0; e < 32; ++e) {
@@ -482,6 +567,8 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
                 }
             }
         }
+        // every tensor store of this warp has completed before teardown
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
 
     // Drain: the MMA thread's last commit covers every MMA it issued.
@@ -506,9 +593,13 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(Args a) {
 namespace {
 struct TcLayout {
     int taps_tmem, nacc, tm_cols, wsmem_bytes, halo_rows, chunk_rows, stage_bytes, stages;
+    int epi_tma, epi_off;
+    size_t smem;
 };
 
-TcLayout tc_layout(const bkma_conv_desc &d) {
+// On-chip layout of one launch. epi_tma asks for the tensor-store epilogue;
+// it is granted when at least 3 activation stages still fit beside its tiles.
+TcLayout tc_layout(const bkma_conv_desc &d, bool epi_tma = false) {
     TcLayout t;
     const int cin = (int)d.cin, K = (int)d.ksize;
     // one accumulator when that moves more weight taps into TMEM
@@ -521,8 +612,98 @@ TcLayout tc_layout(const bkma_conv_desc &d) {
     t.halo_rows = std::max(8, (K - 1 + 7) / 8 * 8);
     t.chunk_rows = tc::TILE + t.halo_rows + 1;
     t.stage_bytes = ((cin / 8) * t.chunk_rows * 16 + 1023) / 1024 * 1024;
-    t.stages = std::min(tc::STAGES_MAX, (tc::SMEM_LIMIT - t.wsmem_bytes) / t.stage_bytes);
+    const int avail = tc::SMEM_LIMIT - t.wsmem_bytes;
+    t.stages = std::min(tc::STAGES_MAX, avail / t.stage_bytes);
+    t.epi_tma = 0;
+    if (epi_tma) {
+        const int st_epi = std::min(tc::STAGES_MAX, (avail - tc::EPI_BYTES) / t.stage_bytes);
+        if (avail > tc::EPI_BYTES && st_epi >= 3) {
+            t.stages = st_epi;
+            t.epi_tma = 1;
+        }
+    }
+    t.epi_off = t.wsmem_bytes + t.stages * t.stage_bytes;
+    t.smem = (size_t)t.epi_off + (t.epi_tma ? tc::EPI_BYTES : 0);
     return t;
+}
+
+// Encode the output view (lt, cout, B), lt = L-K+1 rounded down to 8
+// positions (tensor stores clip the inner dimension in 16-byte units), with
+// 64 x 32 x 1 boxes and the 128-byte swizzle the epilogue writes. Needs a row
+// stride that is a multiple of 16 bytes.
+bool encode_out_map(CUtensorMap *map, const bkma_conv_desc &d, void *out, int64_t out_stride) {
+    auto fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tensor_map_encoder());
+    const int64_t lt = (d.length - d.ksize + 1) & ~(int64_t)7;
+    if (!fn || (out_stride % 8) != 0 || ((uintptr_t)out % 16) != 0 || lt < 64 || d.cout < 32)
+        return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)lt, (cuuint64_t)d.cout, (cuuint64_t)d.batch};
+    const cuuint64_t strides[2] = {(cuuint64_t)out_stride * 2, (cuuint64_t)(d.cout * out_stride * 2)};
+    const cuuint32_t box[3] = {64, 32, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, out, dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Pack the weights and launch the tensor kernel: data is read (in place when
+// out == data), halo is the snapshot of the rows past each tile (null out of
+// place), grid is capped by the number of items.
+bkma_status tc_launch(const bkma_conv_desc &d, const void *data, void *out, int64_t out_stride,
+                      const void *w, const void *bias, const void *halo, void *wpack, int *status,
+                      int64_t ntiles, int sms, cudaStream_t st) {
+    TcLayout t = tc_layout(d, true);
+    tc::Args a;
+    memset(&a, 0, sizeof(a));
+    if (t.epi_tma && !encode_out_map(&a.out_map, d, out, out_stride)) t = tc_layout(d, false);
+    uint32_t *tm_img = (uint32_t *)wpack;
+    uint32_t *sm_img = tm_img + 128 * t.tm_cols;
+    tc::conv_tc_pack_weights<<<64, 256, 0, st>>>((const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout,
+                                                 (int)d.ksize, t.taps_tmem, t.tm_cols, tm_img, sm_img);
+    BKMA_CUDA_TRY(cudaGetLastError());
+    a.x = (const __nv_bfloat16 *)data;
+    a.out = (__nv_bfloat16 *)out;
+    a.w = (const __nv_bfloat16 *)w;
+    a.bias = (const __nv_bfloat16 *)bias;
+    a.halo = (const __nv_bfloat16 *)halo;
+    a.B = (int)d.batch;
+    a.cin = (int)d.cin;
+    a.cout = (int)d.cout;
+    a.K = (int)d.ksize;
+    a.L = d.length;
+    a.lout = d.length - d.ksize + 1;
+    a.out_stride = out_stride;
+    a.ntiles = (int)ntiles;
+    a.halo_rows = t.halo_rows;
+    a.chunk_rows = t.chunk_rows;
+    a.stage_bytes = t.stage_bytes;
+    a.stages = t.stages;
+    a.taps_tmem = t.taps_tmem;
+    a.nacc = t.nacc;
+    a.tm_cols = t.tm_cols;
+    a.wsmem_bytes = t.wsmem_bytes;
+    a.epi_tma = t.epi_tma;
+    a.epi_off = t.epi_off;
+    a.wpack_tmem = tm_img;
+    a.wpack_smem = reinterpret_cast<const uint4 *>(sm_img);
+    a.status = status;
+    void (*kern)(const tc::Args) = nullptr;
+    switch (a.cin / 16) {
+    case 1: kern = tc::conv_tc_kernel<1>; break;
+    case 2: kern = tc::conv_tc_kernel<2>; break;
+    case 3: kern = tc::conv_tc_kernel<3>; break;
+    case 4: kern = tc::conv_tc_kernel<4>; break;
+    case 5: kern = tc::conv_tc_kernel<5>; break;
+    case 6: kern = tc::conv_tc_kernel<6>; break;
+    case 7: kern = tc::conv_tc_kernel<7>; break;
+    case 8: kern = tc::conv_tc_kernel<8>; break;
+    default: return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be 16..128");
+    }
+    BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t.smem));
+    const int64_t items = (int64_t)a.B * a.ntiles;
+    const int grid = (int)std::min<int64_t>(sms, items);
+    kern<<<grid, tc::THREADS, t.smem, st>>>(a);
+    BKMA_CUDA_TRY(cudaGetLastError());
+    return BKMA_OK;
 }
 }  // namespace
 
@@ -566,56 +747,9 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
         bkma_status s = conv_halo_prepass(p, data, st);
         if (s != BKMA_OK) return s;
     }
-    const TcLayout t = tc_layout(d);
-    uint32_t *tm_img = (uint32_t *)p.d_wpack;
-    uint32_t *sm_img = tm_img + 128 * t.tm_cols;
-    tc::conv_tc_pack_weights<<<64, 256, 0, st>>>((const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout,
-                                                 (int)d.ksize, t.taps_tmem, t.tm_cols, tm_img, sm_img);
-    BKMA_CUDA_TRY(cudaGetLastError());
-    tc::Args a;
-    a.x = (const __nv_bfloat16 *)data;
-    a.out = (__nv_bfloat16 *)(inplace ? data : out);
-    a.w = (const __nv_bfloat16 *)w;
-    a.bias = (const __nv_bfloat16 *)bias;
-    a.halo = (inplace && d.ksize > 1) ? (const __nv_bfloat16 *)p.d_halo : nullptr;
-    a.B = (int)d.batch;
-    a.cin = (int)d.cin;
-    a.cout = (int)d.cout;
-    a.K = (int)d.ksize;
-    a.L = d.length;
-    a.lout = d.length - d.ksize + 1;
-    a.out_stride = inplace ? d.length : a.lout;
-    a.ntiles = (int)p.ntiles;
-    a.halo_rows = t.halo_rows;
-    a.chunk_rows = t.chunk_rows;
-    a.stage_bytes = t.stage_bytes;
-    a.stages = t.stages;
-    a.taps_tmem = t.taps_tmem;
-    a.nacc = t.nacc;
-    a.tm_cols = t.tm_cols;
-    a.wsmem_bytes = t.wsmem_bytes;
-    a.wpack_tmem = tm_img;
-    a.wpack_smem = reinterpret_cast<const uint4 *>(sm_img);
-    a.status = (int *)p.d_status;
-    const size_t smem = (size_t)t.wsmem_bytes + (size_t)t.stages * t.stage_bytes;
-    void (*kern)(tc::Args) = nullptr;
-    switch (a.cin / 16) {
-    case 1: kern = tc::conv_tc_kernel<1>; break;
-    case 2: kern = tc::conv_tc_kernel<2>; break;
-    case 3: kern = tc::conv_tc_kernel<3>; break;
-    case 4: kern = tc::conv_tc_kernel<4>; break;
-    case 5: kern = tc::conv_tc_kernel<5>; break;
-    case 6: kern = tc::conv_tc_kernel<6>; break;
-    case 7: kern = tc::conv_tc_kernel<7>; break;
-    case 8: kern = tc::conv_tc_kernel<8>; break;
-    default: return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be 16..128");
-    }
-    BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t items = (int64_t)a.B * a.ntiles;
-    const int grid = (int)std::min<int64_t>(p.grid, items);
-    kern<<<grid, tc::THREADS, smem, st>>>(a);
-    BKMA_CUDA_TRY(cudaGetLastError());
-    return BKMA_OK;
+    return tc_launch(d, data, inplace ? data : out, inplace ? d.length : d.length - d.ksize + 1, w,
+                     bias, (inplace && d.ksize > 1) ? p.d_halo : nullptr, p.d_wpack,
+                     (int *)p.d_status, p.ntiles, p.grid, st);
 }
 
 }  // namespace bkma
@@ -652,58 +786,11 @@ bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w,
         bkma_status s = conv_halo_bf16_into(d, data, halo, tc::TILE, ntiles, t.halo_rows, st);
         if (s != BKMA_OK) return s;
     }
-    uint32_t *tm_img = (uint32_t *)wpack;
-    uint32_t *sm_img = tm_img + 128 * t.tm_cols;
-    tc::conv_tc_pack_weights<<<64, 256, 0, st>>>((const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout,
-                                                 (int)d.ksize, t.taps_tmem, t.tm_cols, tm_img, sm_img);
-    BKMA_CUDA_TRY(cudaGetLastError());
-    tc::Args a;
-    a.x = (const __nv_bfloat16 *)data;
-    a.out = (__nv_bfloat16 *)data;
-    a.w = (const __nv_bfloat16 *)w;
-    a.bias = (const __nv_bfloat16 *)bias;
-    a.halo = d.ksize > 1 ? (const __nv_bfloat16 *)halo : nullptr;
-    a.B = (int)d.batch;
-    a.cin = (int)d.cin;
-    a.cout = (int)d.cout;
-    a.K = (int)d.ksize;
-    a.L = d.length;
-    a.lout = d.length - d.ksize + 1;
-    a.out_stride = d.length;
-    a.ntiles = (int)ntiles;
-    a.halo_rows = t.halo_rows;
-    a.chunk_rows = t.chunk_rows;
-    a.stage_bytes = t.stage_bytes;
-    a.stages = t.stages;
-    a.taps_tmem = t.taps_tmem;
-    a.nacc = t.nacc;
-    a.tm_cols = t.tm_cols;
-    a.wsmem_bytes = t.wsmem_bytes;
-    a.wpack_tmem = tm_img;
-    a.wpack_smem = reinterpret_cast<const uint4 *>(sm_img);
-    a.status = status;
-    const size_t smem = (size_t)t.wsmem_bytes + (size_t)t.stages * t.stage_bytes;
-    void (*kern)(tc::Args) = nullptr;
-    switch (a.cin / 16) {
-    case 1: kern = tc::conv_tc_kernel<1>; break;
-    case 2: kern = tc::conv_tc_kernel<2>; break;
-    case 3: kern = tc::conv_tc_kernel<3>; break;
-    case 4: kern = tc::conv_tc_kernel<4>; break;
-    case 5: kern = tc::conv_tc_kernel<5>; break;
-    case 6: kern = tc::conv_tc_kernel<6>; break;
-    case 7: kern = tc::conv_tc_kernel<7>; break;
-    case 8: kern = tc::conv_tc_kernel<8>; break;
-    default: return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be 16..128");
-    }
-    BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, sms = 0;
     BKMA_CUDA_TRY(cudaGetDevice(&dev));
     BKMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int64_t items = (int64_t)a.B * a.ntiles;
-    const int grid = (int)std::min<int64_t>(sms, items);
-    kern<<<grid, tc::THREADS, smem, st>>>(a);
-    BKMA_CUDA_TRY(cudaGetLastError());
-    return BKMA_OK;
+    return tc_launch(d, data, data, d.length, w, bias, d.ksize > 1 ? halo : nullptr, wpack, status,
+                     ntiles, sms, st);
 }
 
 }  // namespace bkma

@@ -4,7 +4,11 @@ FP64 oracle evaluated on the same BF16-rounded inputs.
 Tolerance: max |out - ref| <= 1e-2 * max |ref| (the BF16 output rounding alone
 is 2^-9 relative); the tests also bound the mean error far tighter, at
 3e-3 * max|ref|, to catch layout mistakes that only touch some elements.
-Shapes run smallest first.
+Shapes run smallest first. In place (row stride L, a multiple of 8) the
+epilogue stores through a TMA tensor map when cout >= 32 and L-K+1 >= 64;
+out of place it does so only when L-K+1 is a multiple of 8, so the cases
+below cover both epilogues, partial and empty last half-tiles and output
+channel boxes clipped at cout.
 """
 import numpy as np
 import pytest
@@ -15,6 +19,7 @@ SHAPES = [
     # B, C, L, K
     (1, 16, 256, 3),
     (1, 16, 136, 1),
+    (1, 32, 136, 1),     # last tile: 8 positions, its second half-tile is empty
     (2, 32, 512, 7),
     (3, 64, 1000, 5),
     (2, 128, 1024, 7),
@@ -63,7 +68,8 @@ def test_tensor_conv_inplace(bkma, cuda, oracle, shape):
     assert np.array_equal(got[:, :, L - K + 1:], orig.double().cpu().numpy()[:, :, L - K + 1:])
 
 
-@pytest.mark.parametrize("shape", [(2, 32, 512, 7), (2, 128, 1024, 7)])
+@pytest.mark.parametrize("shape", [(2, 32, 512, 7), (2, 128, 1024, 7), (2, 128, 1032, 9),
+                                   (2, 64, 520, 1)])
 def test_tensor_conv_out_of_place_and_bias_none(bkma, cuda, oracle, shape):
     import torch
     B, C, L, K = shape
@@ -79,9 +85,10 @@ def test_tensor_conv_out_of_place_and_bias_none(bkma, cuda, oracle, shape):
     assert torch.equal(xd, before)
 
 
-def test_tensor_conv_fewer_out_channels(bkma, cuda, oracle):
+@pytest.mark.parametrize("L,K", [(512, 3), (520, 9)])
+def test_tensor_conv_fewer_out_channels(bkma, cuda, oracle, L, K):
     import torch
-    B, cin, cout, L, K = 2, 64, 48, 512, 3
+    B, cin, cout = 2, 64, 48
     rng = np.random.default_rng(5)
     x = rng.uniform(-1, 1, (B, cin, L))
     w = rng.uniform(-1, 1, (cout, cin, K)) / np.sqrt(cin * K)
