@@ -469,7 +469,8 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
         const int co = threadIdx.x;
         const float bias = (a.bias && co < a.cout) ? __bfloat162float(a.bias[co]) : 0.0f;
         const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)a.tm_cols;
-        // this warp's two 4 KB swizzled output tiles (one per half item)
+        // this warp's two 4 KB swizzled output tiles (one per half item),
+        // stored by one bulk group per item
         const uint32_t epi_tile =
             ((smem_base + (uint32_t)a.epi_off + 1023u) & ~1023u) + (uint32_t)warp * 2u * EPI_TILE_BYTES;
         const bool warp_rows = 32 * warp < a.cout;
@@ -482,7 +483,16 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             if (!mbar_wait(&accf_bar[acc], aph, &abort_flag, a.status)) break;
             fence_after();
             const int64_t l0 = (int64_t)tile * TILE;
-            __nv_bfloat16 *row = a.out + ((int64_t)b * a.cout + co) * a.out_stride;
+            // The tensor map ends at lt = lout rounded down to 8 positions (a
+            // tensor store clips in 16-byte units); lanes store the last
+            // lout - lt values of their rows themselves.
+            const int64_t lt = a.lout & ~(int64_t)7;
+            const bool tma_rows = a.epi_tma && warp_rows;
+            // both tiles of this warp are free once the previous item's stores read them
+            if (tma_rows) {
+                if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                __syncwarp();
+            }
 #pragma unroll 1
             for (int half = 0; half < 2; ++half) {
                 uint32_t v[2][32];
@@ -495,22 +505,18 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
                     mbar_arrive(&acce_bar[acc]);
                 }
                 const int64_t lh = l0 + 64 * half;
-                if (a.epi_tma) {
-                    if (!warp_rows || lh >= a.lout) continue;
-                    uint32_t pk[32];
+                if (lh >= a.lout || (a.epi_tma && !warp_rows)) continue;
+                uint32_t pk[32];
 #pragma unroll
-                    for (int e = 0; e < 32; ++e) {
-                        const float f0 = __uint_as_float(v[e / 16][(2 * e) % 32]) + bias;
-                        const float f1 = __uint_as_float(v[e / 16][(2 * e + 1) % 32]) + bias;
-                        const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
-                        pk[e] = *reinterpret_cast<const uint32_t *>(&h);
-                    }
-                    // The tensor map ends at lt = lout rounded down to 8 positions
-                    // (a tensor store clips in 16-byte units); lanes store the
-                    // last lout - lt values of their rows themselves.
-                    const int64_t lt = a.lout & ~(int64_t)7;
+                for (int e = 0; e < 32; ++e) {
+                    const float f0 = __uint_as_float(v[e / 16][(2 * e) % 32]) + bias;
+                    const float f1 = __uint_as_float(v[e / 16][(2 * e + 1) % 32]) + bias;
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
+                    pk[e] = *reinterpret_cast<const uint32_t *>(&h);
+                }
+                __nv_bfloat16 *dst = a.out + ((int64_t)b * a.cout + co) * a.out_stride + lh;
+                if (a.epi_tma) {
                     if (lt < a.lout && lt < lh + 64 && co < a.cout) {
-                        __nv_bfloat16 *dst = a.out + ((int64_t)b * a.cout + co) * a.out_stride + lh;
 #pragma unroll
                         for (int e = 0; e < 64; ++e)
                             if (lh + e >= lt && lh + e < a.lout)
@@ -518,11 +524,8 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
                                     (uint16_t)((pk[e / 2] >> (16 * (e & 1))) & 0xFFFFu));
                     }
                     if (lh >= lt) continue;
-                    // the store issued from this tile one item ago has read it
-                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-                    __syncwarp();
-                    const uint32_t tile_addr = epi_tile + (uint32_t)half * EPI_TILE_BYTES;
-                    const uint32_t row_addr = tile_addr + (uint32_t)lane * 128u;
+                    const uint32_t row_addr =
+                        epi_tile + (uint32_t)half * EPI_TILE_BYTES + (uint32_t)lane * 128u;
 #pragma unroll
                     for (int e = 0; e < 8; ++e)
                         asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(
@@ -530,40 +533,36 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
                                      "r"(pk[4 * e]), "r"(pk[4 * e + 1]), "r"(pk[4 * e + 2]),
                                      "r"(pk[4 * e + 3])
                                      : "memory");
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    __syncwarp();
-                    if (lane == 0) {
-                        asm volatile(
-                            "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], "
-                            "[%1];" ::"l"(reinterpret_cast<uint64_t>(&a.out_map)),
-                            "r"(tile_addr), "r"((int)lh), "r"(32 * warp), "r"(b)
-                            : "memory");
-                        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-                    }
                 } else if (co < a.cout) {
-                    uint32_t pk[32];
-#pragma unroll
-                    for (int e = 0; e < 32; ++e) {
-                        const float f0 = __uint_as_float(v[e / 16][(2 * e) % 32]) + bias;
-                        const float f1 = __uint_as_float(v[e / 16][(2 * e + 1) % 32]) + bias;
-                        const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
-                        pk[e] = *reinterpret_cast<const uint32_t *>(&h);
-                    }
-                    __nv_bfloat16 *dst = row + lh;
                     if (lh + 64 <= a.lout && (a.out_stride % 8) == 0) {
                         uint4 *d4 = reinterpret_cast<uint4 *>(dst);
 #pragma unroll
                         for (int e = 0; e < 8; ++e)
                             d4[e] = make_uint4(pk[4 * e], pk[4 * e + 1], pk[4 * e + 2], pk[4 * e + 3]);
                     } else {
-                        for (int e = 0; e < 64; ++e) {
-                            if (lh + e < a.lout) {
-                                const uint16_t bits =
-                                    (uint16_t)((pk[e / 2] >> (16 * (e & 1))) & 0xFFFFu);
-                                dst[e] = __ushort_as_bfloat16(bits);
-                            }
-                        }
+#pragma unroll
+                        for (int e = 0; e < 64; ++e)
+                            if (lh + e < a.lout)
+                                dst[e] = __ushort_as_bfloat16(
+                                    (uint16_t)((pk[e / 2] >> (16 * (e & 1))) & 0xFFFFu));
                     }
+                }
+            }
+            if (tma_rows) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) {
+                    for (int half = 0; half < 2; ++half) {
+                        const int64_t lh = l0 + 64 * half;
+                        if (lh >= lt) break;
+                        asm volatile(
+                            "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], "
+                            "[%1];" ::"l"(reinterpret_cast<uint64_t>(&a.out_map)),
+                            "r"(epi_tile + (uint32_t)half * EPI_TILE_BYTES), "r"((int)lh),
+                            "r"(32 * warp), "r"(b)
+                            : "memory");
+                    }
+                    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                 }
             }
         }
