@@ -427,7 +427,7 @@ def conv_block(bkma_gb300, dev, batch: int = 256, with_fp64: bool = True):
                                  "unit": "TFLOP/s", "frac": tflops / bf16_peak,
                                  "peak_kind": f"{kind} cuBLAS bf16 burst",
                                  "algorithmic_flops": flops,
-                                 "note": "time includes the halo pre-pass kernel"}})
+                                 "note": "time includes the prologue kernel (weight images + halo snapshot of each CTA's last tile)"}})
         if not with_fp64:
             raise StopIteration
         # FP64 plain form on the same BF16 inputs: error reference and speed baseline

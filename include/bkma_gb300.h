@@ -255,10 +255,10 @@ bkma_status bkma_conv_check(const void *data, int32_t dtype, int64_t n0, int64_t
  * device memory to their own pool at start-up, and loops that cannot afford
  * an allocation's implicit synchronization. Its scratch is one 16 MiB device
  * array inside the library (held by every GPU that loads it until exit):
- * 512 KiB for packed weights and 15.5 MiB for the halo snapshot, so
- * batch * ceil((length-ksize+1)/128) * channels * 2 * max(8, round_up(ksize-1, 8))
- * bytes must stay within 16252672; larger shapes get BKMA_ERR_INVALID_ARG
- * (split the batch, or use bkma_conv_run). The first call on a device looks the array's address up,
+ * 512 KiB for packed weights and 15.5 MiB for the halo snapshot, which keeps
+ * one slot per chunk of consecutive tiles (at most 3840 slots of
+ * channels * 2 * max(8, round_up(ksize-1, 8)) bytes: at most 15 MiB for every
+ * shape the tensor path takes), so no batch or length is limited by it. The first call on a device looks the array's address up,
  * so make it before any stream capture. Calls share the array: calls that
  * overlap on the GPU race, and a device-side wait timeout is not reported. */
 bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *weight, const void *bias,

@@ -15,7 +15,8 @@
 //    scratch; the compute kernel then reads its halo from there, so tiles of
 //    one row run concurrently with no ordering between CTAs.
 //
-// The BF16 tensor-core path (conv_tc.cu) shares the halo pre-pass.
+// The BF16 tensor-core path (conv_tc.cu) runs each CTA's tiles in order and
+// snapshots only the rows past each CTA's last tile.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -90,32 +91,6 @@ __global__ void conv_halo_kernel(const T *x, T *halo, int64_t B, int64_t cin, in
     }
 }
 
-// 16-bit halo copy for halo rows padded to a multiple of 8 values: one
-// 16-byte load and store per (row, tile, channel, 8 columns).
-__global__ void conv_halo_kernel_v8(const uint16_t *x, uint16_t *halo, int64_t B, int64_t cin,
-                                    int64_t L, int K, int TL, int64_t ntiles, int hw) {
-    const int nch = hw / 8;
-    const int64_t total = B * ntiles * cin * nch;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % nch);
-        const int64_t rest = i / nch;  // (b, t, ci)
-        const int64_t ci = rest % cin;
-        const int64_t bt = rest / cin;
-        const int64_t t = bt % ntiles;
-        const int64_t b = bt / ntiles;
-        const int64_t col = (t + 1) * TL + 8 * ch;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (col + 8 <= L) v = *reinterpret_cast<const uint4 *>(x + (b * cin + ci) * L + col);
-        uint32_t *w = reinterpret_cast<uint32_t *>(&v);
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            if (8 * ch + e >= K - 1) w[e / 2] &= (e & 1) ? 0x0000FFFFu : 0xFFFF0000u;
-        }
-        reinterpret_cast<uint4 *>(halo)[i] = v;
-    }
-}
-
 template <typename T>
 __device__ __forceinline__ T mac(T acc, T a, T b);
 template <>
@@ -172,23 +147,6 @@ using namespace bkma;
 
 namespace bkma {
 
-// 16-bit halo snapshot into caller-provided memory (no plan): the same
-// kernels as conv_halo_prepass, for the allocation-free conv1d entry point.
-bkma_status conv_halo_bf16_into(const bkma_conv_desc &d, const void *x, void *halo, int TL,
-                                int64_t ntiles, int hw, cudaStream_t st) {
-    const int blocks = 152 * 4;
-    if (hw % 8 == 0 && TL % 8 == 0 && d.length % 8 == 0 && (uintptr_t)x % 16 == 0 &&
-        (uintptr_t)halo % 16 == 0)
-        conv_halo_kernel_v8<<<blocks, 256, 0, st>>>((const uint16_t *)x, (uint16_t *)halo, d.batch,
-                                                    d.cin, d.length, (int)d.ksize, TL, ntiles, hw);
-    else
-        conv_halo_kernel<uint16_t><<<blocks, 256, 0, st>>>((const uint16_t *)x, (uint16_t *)halo,
-                                                          d.batch, d.cin, d.length, (int)d.ksize,
-                                                          TL, ntiles, hw);
-    BKMA_CUDA_TRY(cudaGetLastError());
-    return BKMA_OK;
-}
-
 bkma_status conv_halo_prepass(ConvPlanImpl &p, const void *x, cudaStream_t st) {
     const bkma_conv_desc &d = p.desc;
     const int blocks = 152 * 4;
@@ -200,15 +158,8 @@ bkma_status conv_halo_prepass(ConvPlanImpl &p, const void *x, cudaStream_t st) {
         conv_halo_kernel<float><<<blocks, 256, 0, st>>>((const float *)x, (float *)p.d_halo,
                                                        d.batch, d.cin, d.length, (int)d.ksize,
                                                        p.TL, p.ntiles, p.halo_width);
-    else if (p.halo_width % 8 == 0 && p.TL % 8 == 0 && d.length % 8 == 0 &&
-             (uintptr_t)x % 16 == 0)
-        conv_halo_kernel_v8<<<blocks, 256, 0, st>>>((const uint16_t *)x, (uint16_t *)p.d_halo,
-                                                    d.batch, d.cin, d.length, (int)d.ksize, p.TL,
-                                                    p.ntiles, p.halo_width);
     else
-        conv_halo_kernel<uint16_t><<<blocks, 256, 0, st>>>((const uint16_t *)x, (uint16_t *)p.d_halo,
-                                                          d.batch, d.cin, d.length, (int)d.ksize,
-                                                          p.TL, p.ntiles, p.halo_width);
+        return fail(BKMA_ERR_UNSUPPORTED, "halo pre-pass: F32 or F64 only (BF16 runs on the tensor path)");
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
 }

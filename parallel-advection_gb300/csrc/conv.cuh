@@ -42,7 +42,7 @@ struct ConvPlanImpl {
     int64_t ntiles = 0;   // tiles per row
     void *d_halo = nullptr;
     size_t halo_bytes = 0;
-    int halo_width = 0;       // halo values kept per (row, tile, channel) >= K-1
+    int halo_width = 0;       // halo values kept per channel of a snapshot slot >= K-1
     void *d_wpack = nullptr;  // weights packed for the tensor path
     size_t wpack_bytes = 0;
     void *d_status = nullptr; // device status word of the tensor kernel
@@ -55,8 +55,6 @@ struct ConvPlanImpl {
 };
 
 bkma_status conv_halo_prepass(ConvPlanImpl &p, const void *x, cudaStream_t st);
-bkma_status conv_halo_bf16_into(const bkma_conv_desc &d, const void *x, void *halo, int TL,
-                                int64_t ntiles, int hw, cudaStream_t st);
 bkma_status conv_tc_scratch_need(const bkma_conv_desc &d, size_t *halo_bytes, size_t *wpack_bytes);
 bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w, const void *bias,
                              void *halo, void *wpack, int *status, cudaStream_t st);

@@ -88,9 +88,8 @@ extern "C" bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *
                         std::to_string(wpack_bytes) + " of packed weights; the fixed device array "
                         "holds at most " + std::to_string(kHaloMax) + " and " +
                         std::to_string(kWpackMax) +
-                        " (halo = batch * ceil((length-ksize+1)/128) * channels * 2 * "
-                        "max(8, round_up(ksize-1, 8)) bytes); "
-                        "split the batch or use bkma_conv_run");
+                        " (halo <= 3840 * channels * 2 * max(8, round_up(ksize-1, 8)) bytes); "
+                        "use bkma_conv_run");
     unsigned char *base = nullptr;
     s = scratch_address(&base);
     if (s != BKMA_OK) return s;

@@ -20,9 +20,17 @@
 //    transpose 8x8 BF16 blocks in registers, and store conflict-free (the
 //    odd row count of a chunk spreads the 8 stores of a phase over all
 //    banks). A warp covers 8 consecutive channel chunks x 4 consecutive row
-//    blocks, so one load instruction touches 8 lines of 64 bytes. Rows past
-//    the tile come from the halo snapshot (conv.cu), so tiles of one row can
-//    be overwritten in place concurrently.
+//    blocks, so one load instruction touches 8 lines of 64 bytes.
+//  * Items ((row, tile) pairs) are grouped in chunks of `chunk` consecutive
+//    tiles; CTAs take chunks round-robin (the CTAs of one round read
+//    neighbouring stretches of every channel row) and run a chunk's tiles in
+//    order. The items left after the full rounds are split evenly, one
+//    shorter chunk per CTA, so every CTA runs the same number of items (+-1). In place, the rows past a tile (the next tile's first K-1
+//    positions) are then still unwritten when its producer reads them: the
+//    next tile's epilogue waits for its MMAs, which wait for this tile's
+//    stage. Only the rows past a chunk's last tile belong to another CTA; the
+//    prologue kernel snapshots them (one slot per chunk) before the main
+//    kernel starts.
 //  * One thread issues the MMAs of a 128-position item (K taps x Cin/16
 //    K-steps) into a TMEM accumulator; four epilogue warps drain it
 //    (tcgen05.ld), add the bias and round to BF16. When the output rows are
@@ -59,6 +67,9 @@ constexpr int NUM_PROD_WARPS = 8;  // two groups of 4 warps, alternate items
 constexpr int PROD_GROUP = 128;    // threads per producer group
 constexpr int THREADS = 32 * (NUM_EPI_WARPS + NUM_PROD_WARPS + 1);
 constexpr uint32_t kSpinLimit = 1u << 22;  // x ~ 0.25 us backoff: ~1 s
+constexpr int MAX_CTAS = 1024;             // grid cap
+constexpr int CHUNK_TILES = 32;            // preferred tiles per chunk
+constexpr int MAX_SLOTS = 3840;            // halo snapshot slots (chunks) per call: <= 15 MiB
 
 constexpr int EPI_TILE_BYTES = 4096;  // 32 channels x 64 positions BF16
 constexpr int EPI_BYTES = NUM_EPI_WARPS * 2 * EPI_TILE_BYTES + 1024;  // + alignment slack
@@ -69,12 +80,13 @@ struct Args {
     __nv_bfloat16 *out;       // (B, Cout, out_stride)
     const __nv_bfloat16 *w;   // (Cout, Cin, K)
     const __nv_bfloat16 *bias;  // (Cout) or null
-    const __nv_bfloat16 *halo;  // [B][ntiles][Cin][halo_rows] or null (out of place)
+    const __nv_bfloat16 *halo;  // [chunk slots][Cin][halo_rows]: rows past each chunk, or null
     const uint32_t *wpack_tmem;  // [128][tm_cols] BF16 pairs: TMEM image of taps 0..taps_tmem-1
     const uint4 *wpack_smem;     // shared-memory image of taps taps_tmem..K-1
     int B, cin, cout, K;
     int64_t L, lout, out_stride;
     int ntiles;
+    int chunk;       // items per chunk (the last chunk may be shorter)
     int halo_rows;   // rows after the tile: round_up(K-1, 8)
     int chunk_rows;  // TILE + halo_rows + 1 (odd, spreads banks)
     int stage_bytes;
@@ -198,16 +210,21 @@ __device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat16 h) {
 }
 
 // Load the 8x8 block (ci = 8c..8c+7) x (rows 8q..8q+7 of the tile) into v[j]
-// (row j = ci 8c+j, 8 positions). Rows past the tile come from the halo
-// snapshot when running in place (16-byte rows, halo_rows values per channel).
-__device__ __forceinline__ void load_block(const Args &a, int b, int tile, int c, int q,
+// (row j = ci 8c+j, 8 positions). slot >= 0 (in place, the last item of
+// chunk `slot`): the rows past the tile come from that halo slot (16-byte
+// rows, halo_rows values per channel).
+__device__ __forceinline__ void load_block(const Args &a, int b, int tile, int c, int q, int64_t slot,
                                            uint4 (&v)[8]) {
     const int64_t l0 = (int64_t)tile * TILE;
     const int r0 = 8 * q;
     const int64_t col = l0 + r0;
-    if (a.halo != nullptr && r0 >= TILE) {
-        const __nv_bfloat16 *h =
-            a.halo + (((int64_t)b * a.ntiles + tile) * a.cin + 8 * c) * a.halo_rows + (r0 - TILE);
+    if (r0 >= TILE + a.K - 1) {  // rows no output reads (K = 1): never touch the next tile
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = make_uint4(0, 0, 0, 0);
+        return;
+    }
+    if (slot >= 0 && r0 >= TILE) {
+        const __nv_bfloat16 *h = a.halo + (slot * a.cin + 8 * c) * a.halo_rows + (r0 - TILE);
 #pragma unroll
         for (int j = 0; j < 8; ++j) v[j] = *reinterpret_cast<const uint4 *>(h + (int64_t)j * a.halo_rows);
         return;
@@ -224,6 +241,26 @@ __device__ __forceinline__ void load_block(const Args &a, int b, int tile, int c
     // either fully inside or fully outside)
 #pragma unroll
     for (int j = 0; j < 8; ++j) v[j] = make_uint4(0, 0, 0, 0);
+}
+
+// Chunk k of a launch with `grid` CTAs over `items` items: rounds of grid
+// chunks of `chunk` items, then one last chunk per CTA that splits the rest
+// evenly (possibly empty). Sets [*begin, *end); slot k = r * grid + c.
+__host__ __device__ __forceinline__ void chunk_range(int64_t k, int64_t items, int grid, int chunk,
+                                                     int64_t *begin, int64_t *end) {
+    const int64_t per_round = (int64_t)grid * chunk;
+    const int64_t rounds = items / per_round;
+    if (k < rounds * grid) {
+        *begin = k * chunk;
+        *end = *begin + chunk;
+    } else {
+        const int64_t base = rounds * per_round, rem = items - base, c = k - rounds * grid;
+        *begin = base + (c * rem) / grid;
+        *end = base + ((c + 1) * rem) / grid;
+    }
+}
+__host__ __device__ __forceinline__ int64_t chunk_slots(int64_t items, int grid, int chunk) {
+    return (items / ((int64_t)grid * chunk) + 1) * grid;
 }
 
 // Block p of an item's (channel chunk, row block) pairs. With a multiple of 8
@@ -262,20 +299,45 @@ __device__ __forceinline__ void store_block(unsigned char *dst, const uint4 (&v)
     }
 }
 
-// Weight pre-pack: the TMEM image (taps 0..taps_tmem-1 as BF16 pairs per
-// output channel) and the shared-memory image of the other taps
-// ([tap][ci-chunk][co][8 ci], K-major no-swizzle A tiles of 128 rows).
-__global__ void conv_tc_pack_weights(const __nv_bfloat16 *w, int cin, int cout, int K,
-                                     int taps_tmem, int tm_cols, uint32_t *tm_img,
-                                     uint32_t *sm_img) {
+// Prologue of one call (one launch, before the main kernel). Words
+// [0, nA + nB): the weight images - the TMEM image of taps 0..taps_tmem-1 (BF16
+// pairs (ci, ci+1) per output channel) and the shared-memory image of the
+// other taps ([tap][ci-chunk][co][8 ci], K-major no-swizzle A tiles of 128
+// rows). Then, in place (halo != null), 16-byte pieces of the halo snapshot:
+// slot c = x[b][ci][(t+1)*TILE + j], j < halo_rows, for the last item (b, t)
+// of chunk c (chunk_range), zero past L; empty chunks have no slot content.
+__global__ void conv_tc_prologue(const __nv_bfloat16 *w, int cin, int cout, int K, int taps_tmem,
+                                 int tm_cols, uint32_t *tm_img, uint32_t *sm_img,
+                                 const __nv_bfloat16 *x, __nv_bfloat16 *halo, int64_t items,
+                                 int grid, int chunk, int ntiles, int64_t L, int halo_rows) {
     const int wcols = taps_tmem * cin / 2;
     const int nA = 128 * tm_cols;
     const int nB = (K - taps_tmem) * (cin / 8) * 128 * 4;  // 32-bit words
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA + nB; i += gridDim.x * blockDim.x) {
+    const int pieces = halo_rows / 8;
+    const int64_t nS = halo ? chunk_slots(items, grid, chunk) * cin * pieces : 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nA + nB + nS;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i >= nA + nB) {
+            int64_t r = i - nA - nB;
+            const int piece = (int)(r % pieces);
+            r /= pieces;
+            const int ci = (int)(r % cin);
+            const int64_t c = r / cin;
+            int64_t first, end;
+            chunk_range(c, items, grid, chunk, &first, &end);
+            if (end == first) continue;
+            const int64_t last = end - 1;
+            const int64_t b = last / ntiles;
+            const int64_t col = (last % ntiles + 1) * TILE + 8 * piece;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (col + 8 <= L) v = *reinterpret_cast<const uint4 *>(x + (b * cin + ci) * L + col);
+            *reinterpret_cast<uint4 *>(halo + (c * cin + ci) * halo_rows + 8 * piece) = v;
+            continue;
+        }
         int co, k, ci;
         if (i < nA) {
-            co = i / tm_cols;
-            const int col = i % tm_cols;
+            co = (int)(i / tm_cols);
+            const int col = (int)(i % tm_cols);
             if (col >= wcols || co >= cout) {
                 tm_img[i] = 0;
                 continue;
@@ -283,7 +345,7 @@ __global__ void conv_tc_pack_weights(const __nv_bfloat16 *w, int cin, int cout, 
             k = (2 * col) / cin;
             ci = (2 * col) % cin;
         } else {
-            int r = i - nA;
+            int r = (int)(i - nA);
             const int e = r % 4;
             r /= 4;
             co = r % 128;
@@ -381,17 +443,23 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
     fence_after();
 
     const int64_t items = (int64_t)a.B * a.ntiles;
+    const int64_t chunk_ids = chunk_slots(items, gridDim.x, a.chunk);
     const uint32_t smem_base = smem_u32(smem);
+    // Every role walks the same item sequence: chunks blockIdx.x, +gridDim.x,
+    // ..., the items of a chunk in order.
+#define BKMA_TC_FOR_ITEMS                                                              \
+    for (int64_t ch = blockIdx.x, item = 0, iend = 0; ch < chunk_ids; ch += gridDim.x) \
+        for (chunk_range(ch, items, gridDim.x, a.chunk, &item, &iend); item < iend; ++item, ++it)
 
     if (is_prod) {
         const int pidx = threadIdx.x - 32 * NUM_EPI_WARPS;  // 0..255
         const int grp = pidx / PROD_GROUP;                 // items it with it % 2 == grp
         const int pt = pidx % PROD_GROUP;
-        const int nchunks = cin / 8;
+        const int cchunks = cin / 8;  // 8-channel chunks
         const int qblocks = (TILE + a.halo_rows) / 8;
-        const int pairs = nchunks * qblocks;
+        const int pairs = cchunks * qblocks;
         int it = 0;
-        for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
+        BKMA_TC_FOR_ITEMS {
             if ((it & 1) != grp) continue;
             const int s = it % stages;
             const uint32_t ph = (uint32_t)(it / stages) & 1u;
@@ -399,6 +467,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
             unsigned char *stage = stages_sm + (size_t)s * a.stage_bytes;
+            const int64_t slot = (a.halo != nullptr && item == iend - 1) ? ch : -1;
             // up to three 8x8 blocks per thread in flight at once (one round trip
             // for Cin = 128: 16 chunks x 17 row blocks = 272 blocks / 128 threads)
             for (int p = pt; p < pairs; p += 3 * PROD_GROUP) {
@@ -407,8 +476,8 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
 #pragma unroll
                 for (int h = 0; h < 3; ++h) {
                     const int ph2 = p + h * PROD_GROUP;
-                    block_of(ph2, nchunks, bc[h], bq[h]);
-                    if (ph2 < pairs) load_block(a, b, tile, bc[h], bq[h], v[h]);
+                    block_of(ph2, cchunks, bc[h], bq[h]);
+                    if (ph2 < pairs) load_block(a, b, tile, bc[h], bq[h], slot, v[h]);
                 }
 #pragma unroll
                 for (int h = 0; h < 3; ++h) {
@@ -432,7 +501,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             const uint32_t tap16 = (uint32_t)(cin * 256) >> 4;
             const uint32_t stage0 = smem_base + (uint32_t)a.wsmem_bytes;
             int it = 0;
-            for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
+            BKMA_TC_FOR_ITEMS {
                 const int s = it % stages;
                 const uint32_t ph = (uint32_t)(it / stages) & 1u;
                 if (!mbar_wait(&full_bar[s], ph, &abort_flag, a.status)) break;
@@ -475,7 +544,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             ((smem_base + (uint32_t)a.epi_off + 1023u) & ~1023u) + (uint32_t)warp * 2u * EPI_TILE_BYTES;
         const bool warp_rows = 32 * warp < a.cout;
         int it = 0;
-        for (int64_t item = blockIdx.x; item < items; item += gridDim.x, ++it) {
+        BKMA_TC_FOR_ITEMS {
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
             const int acc = a.nacc == 2 ? (it & 1) : 0;
@@ -570,6 +639,8 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
         if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
 
+#undef BKMA_TC_FOR_ITEMS
+
     // Drain: the MMA thread's last commit covers every MMA it issued.
     if (threadIdx.x == 32 * (NUM_EPI_WARPS + NUM_PROD_WARPS)) {
         for (uint32_t i = 0; i < kSpinLimit; ++i) {
@@ -644,21 +715,58 @@ bool encode_out_map(CUtensorMap *map, const bkma_conv_desc &d, void *out, int64_
               CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Pack the weights and launch the tensor kernel: data is read (in place when
-// out == data), halo is the snapshot of the rows past each tile (null out of
-// place), grid is capped by the number of items.
+int64_t tc_items(const bkma_conv_desc &d) {
+    return d.batch * ((d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE);
+}
+
+// CTAs of a launch: min(SMs, items, MAX_CTAS).
+int tc_grid(int64_t items, int sms) {
+    return (int)std::min<int64_t>(std::min<int64_t>(sms, items), tc::MAX_CTAS);
+}
+
+// Items per chunk: CHUNK_TILES, or more so that the chunks (slots) stay
+// within MAX_SLOTS for any grid up to MAX_CTAS.
+int tc_chunk(int64_t items) {
+    return (int)std::max<int64_t>(tc::CHUNK_TILES,
+                                  (items + tc::MAX_SLOTS - tc::MAX_CTAS - 1) /
+                                      (tc::MAX_SLOTS - tc::MAX_CTAS));
+}
+
+// Halo snapshot bytes: one slot per chunk; for any grid the chunks number at
+// most items / chunk + min(items, MAX_CTAS) <= MAX_SLOTS.
+size_t tc_halo_bytes(const bkma_conv_desc &d, int halo_rows) {
+    const int64_t items = tc_items(d);
+    const int64_t slots = items / tc_chunk(items) + std::min<int64_t>(items, tc::MAX_CTAS);
+    return (size_t)slots * (size_t)d.cin * (size_t)halo_rows * 2;
+}
+
+// Launch the prologue (weight images; in place, the halo snapshot) and the
+// tensor kernel: data is read (in place when out == data, then halo holds
+// one slot per chunk), grid = min(sms, items, MAX_CTAS).
 bkma_status tc_launch(const bkma_conv_desc &d, const void *data, void *out, int64_t out_stride,
-                      const void *w, const void *bias, const void *halo, void *wpack, int *status,
+                      const void *w, const void *bias, void *halo, void *wpack, int *status,
                       int64_t ntiles, int sms, cudaStream_t st) {
     TcLayout t = tc_layout(d, true);
     tc::Args a;
     memset(&a, 0, sizeof(a));
     if (t.epi_tma && !encode_out_map(&a.out_map, d, out, out_stride)) t = tc_layout(d, false);
+    const int64_t items = d.batch * ntiles;
+    const int chunk = tc_chunk(items);
+    const int grid = tc_grid(items, sms);
     uint32_t *tm_img = (uint32_t *)wpack;
     uint32_t *sm_img = tm_img + 128 * t.tm_cols;
-    tc::conv_tc_pack_weights<<<64, 256, 0, st>>>((const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout,
-                                                 (int)d.ksize, t.taps_tmem, t.tm_cols, tm_img, sm_img);
-    BKMA_CUDA_TRY(cudaGetLastError());
+    {
+        const int64_t words = (int64_t)128 * t.tm_cols +
+                              (int64_t)(d.ksize - t.taps_tmem) * (d.cin / 8) * 128 * 4;
+        const int64_t total =
+            words + (halo ? tc::chunk_slots(items, grid, chunk) * d.cin * (t.halo_rows / 8) : 0);
+        const int blocks = (int)std::min<int64_t>(4 * 152, (total + 255) / 256);
+        tc::conv_tc_prologue<<<blocks, 256, 0, st>>>(
+            (const __nv_bfloat16 *)w, (int)d.cin, (int)d.cout, (int)d.ksize, t.taps_tmem, t.tm_cols,
+            tm_img, sm_img, (const __nv_bfloat16 *)data, (__nv_bfloat16 *)halo, items, grid,
+            chunk, (int)ntiles, d.length, t.halo_rows);
+        BKMA_CUDA_TRY(cudaGetLastError());
+    }
     a.x = (const __nv_bfloat16 *)data;
     a.out = (__nv_bfloat16 *)out;
     a.w = (const __nv_bfloat16 *)w;
@@ -672,6 +780,7 @@ bkma_status tc_launch(const bkma_conv_desc &d, const void *data, void *out, int6
     a.lout = d.length - d.ksize + 1;
     a.out_stride = out_stride;
     a.ntiles = (int)ntiles;
+    a.chunk = chunk;
     a.halo_rows = t.halo_rows;
     a.chunk_rows = t.chunk_rows;
     a.stage_bytes = t.stage_bytes;
@@ -698,8 +807,6 @@ bkma_status tc_launch(const bkma_conv_desc &d, const void *data, void *out, int6
     default: return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be 16..128");
     }
     BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t.smem));
-    const int64_t items = (int64_t)a.B * a.ntiles;
-    const int grid = (int)std::min<int64_t>(sms, items);
     kern<<<grid, tc::THREADS, t.smem, st>>>(a);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
@@ -722,14 +829,14 @@ bkma_status conv_tc_plan_init(ConvPlanImpl &p) {
     p.TL = tc::TILE;
     p.ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
     p.halo_width = t.halo_rows;
-    p.halo_bytes = 2 * (size_t)(d.batch * p.ntiles * d.cin * p.halo_width);
+    p.halo_bytes = tc_halo_bytes(d, t.halo_rows);
     p.wpack_bytes = (size_t)128 * t.tm_cols * 4 + (size_t)t.wsmem_bytes;
     BKMA_CUDA_TRY(cudaMalloc(&p.d_wpack, p.wpack_bytes));
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
         sms = 148;
-    p.grid = sms;
+    p.grid = std::min(sms, tc::MAX_CTAS);
     BKMA_CUDA_TRY(cudaMalloc(&p.d_status, sizeof(int)));
     BKMA_CUDA_TRY(cudaMemset(p.d_status, 0, sizeof(int)));
     return BKMA_OK;
@@ -742,10 +849,6 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
     const auto misaligned = [](const void *q) { return q && ((uintptr_t)q % 16) != 0; };
     if (misaligned(data) || misaligned(out) || misaligned(w))
         return fail(BKMA_ERR_INVALID_ARG, "tensor path: data, out and weight must be 16-byte aligned");
-    if (inplace && d.ksize > 1) {
-        bkma_status s = conv_halo_prepass(p, data, st);
-        if (s != BKMA_OK) return s;
-    }
     return tc_launch(d, data, inplace ? data : out, inplace ? d.length : d.length - d.ksize + 1, w,
                      bias, (inplace && d.ksize > 1) ? p.d_halo : nullptr, p.d_wpack,
                      (int *)p.d_status, p.ntiles, p.grid, st);
@@ -756,7 +859,7 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
 namespace bkma {
 
 // Scratch needs of the tensor path for one in-place call: the halo snapshot
-// and the packed weights (bytes, each rounded to 256).
+// (one slot per CTA) and the packed weights (bytes, each rounded to 256).
 bkma_status conv_tc_scratch_need(const bkma_conv_desc &d, size_t *halo_bytes, size_t *wpack_bytes) {
     if (d.cout > 128 || d.cin > 128 || d.cin % 16 != 0 || d.length % 8 != 0)
         return fail(BKMA_ERR_UNSUPPORTED,
@@ -765,26 +868,20 @@ bkma_status conv_tc_scratch_need(const bkma_conv_desc &d, size_t *halo_bytes, si
     if (t.stages < 2)
         return fail(BKMA_ERR_UNSUPPORTED,
                     "tensor path: ksize*cin too large for on-chip weights (TMEM + shared memory)");
-    const int64_t ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
-    *halo_bytes = ((size_t)2 * (size_t)(d.batch * ntiles * d.cin * t.halo_rows) + 255) / 256 * 256;
+    *halo_bytes = (tc_halo_bytes(d, t.halo_rows) + 255) / 256 * 256;
     *wpack_bytes = ((size_t)128 * t.tm_cols * 4 + (size_t)t.wsmem_bytes + 255) / 256 * 256;
     return BKMA_OK;
 }
 
 // In-place BF16 tensor-core conv1d with caller-provided scratch (halo
-// snapshot, packed weights, status word): the same three kernels as
+// snapshot, packed weights, status word): the same two kernels as
 // conv_tc_run, launched without a plan and without allocating.
 bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w, const void *bias,
                              void *halo, void *wpack, int *status, cudaStream_t st) {
     const auto misaligned = [](const void *q) { return q && ((uintptr_t)q % 16) != 0; };
     if (misaligned(data) || misaligned(w) || misaligned(halo) || misaligned(wpack))
         return fail(BKMA_ERR_INVALID_ARG, "tensor path: data, weight and scratch must be 16-byte aligned");
-    const TcLayout t = tc_layout(d);
     const int64_t ntiles = (d.length - d.ksize + 1 + tc::TILE - 1) / tc::TILE;
-    if (d.ksize > 1) {
-        bkma_status s = conv_halo_bf16_into(d, data, halo, tc::TILE, ntiles, t.halo_rows, st);
-        if (s != BKMA_OK) return s;
-    }
     int dev = 0, sms = 0;
     BKMA_CUDA_TRY(cudaGetDevice(&dev));
     BKMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

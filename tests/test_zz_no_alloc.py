@@ -58,14 +58,19 @@ def test_noalloc_matches_plan_entry_point_twice(bkma, cuda, oracle):
         assert err <= 1e-2 * np.abs(ref).max()
 
 
-def test_noalloc_rejects_shapes_beyond_its_array(bkma, cuda):
+def test_noalloc_large_batch_matches_plan(bkma, cuda):
+    """The halo snapshot keeps one slot per CTA, so a batch whose per-tile
+    snapshot would not have fit the fixed array (160 rows x 64 tiles x 128
+    channels x 16 bytes = 21 MB > 15.5 MiB) runs and equals bkma_conv_run."""
     import torch
     lib = bkma.load()
-    x = torch.zeros(8, 16, 16, dtype=torch.bfloat16, device=cuda)  # pointer only
-    w = torch.zeros(16, 16, 7, dtype=torch.bfloat16, device=cuda)
-    # 1000 rows x 64 tiles x 128 channels x 16 bytes = 131 MB > 15.5 MiB: rejected
-    # before any device work, so the small buffers above are never touched
-    rc = lib.bkma_conv1d_bf16_inplace_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
-                                              None, 1000, 128, 8192, 7, None)
-    assert rc == 1
-    assert "split the batch" in lib.bkma_last_error().decode()
+    stream = torch.cuda.current_stream().cuda_stream
+    B, Ch, L, K = 160, 128, 8192, 7
+    x, w, b = _inputs(cuda, 7, B, Ch, L, K)
+    want = x.clone()
+    plan = bkma.Conv1dPlan(B, Ch, Ch, L, K, dtype="bf16", impl="tensor")
+    plan.run(want, w, b)
+    plan.status()
+    assert _noalloc(lib, x, w, b, stream) == 0, lib.bkma_last_error().decode()
+    torch.cuda.synchronize()
+    assert torch.equal(x, want)
