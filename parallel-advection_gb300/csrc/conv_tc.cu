@@ -68,7 +68,7 @@ constexpr int PROD_GROUP = 128;    // threads per producer group
 constexpr int THREADS = 32 * (NUM_EPI_WARPS + NUM_PROD_WARPS + 1);
 constexpr uint32_t kSpinLimit = 1u << 22;  // x ~ 0.25 us backoff: ~1 s
 constexpr int MAX_CTAS = 1024;             // grid cap
-constexpr int CHUNK_TILES = 32;            // preferred tiles per chunk
+constexpr int CHUNK_TILES = 64;            // preferred tiles per chunk
 constexpr int MAX_SLOTS = 3840;            // halo snapshot slots (chunks) per call: <= 15 MiB
 
 constexpr int EPI_TILE_BYTES = 4096;  // 32 channels x 64 positions BF16
