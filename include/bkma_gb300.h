@@ -130,6 +130,17 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
  * not fit shared memory. No counterpart in the reference, which runs one
  * step per kernel (src/advection.cpp:55-59). */
 bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_launch);
+/* On-chip state of the fused steps (FP32 plans, degree 3, 5 or 9).
+ * BKMA_FUSED_F32 (default): FP32, bit-identical to one step per launch.
+ * BKMA_FUSED_F32X2: each cell is held as an unevaluated sum hi + lo of two
+ * FP32 numbers between the steps of a launch (exact TwoSum renormalisation),
+ * so the field is rounded to FP32 once per launch instead of once per step;
+ * one step per launch still gives the FP32 bits. HBM traffic is unchanged.
+ * BKMA_ERR_UNSUPPORTED for FP64 plans, the plain form, or n1 > 3632 (four
+ * n1 x 4-column FP32 buffers must fit shared memory). No counterpart in the
+ * reference. */
+typedef enum bkma_fused_state { BKMA_FUSED_F32 = 0, BKMA_FUSED_F32X2 = 1 } bkma_fused_state;
+bkma_status bkma_adv_plan_set_fused_state(bkma_adv_plan *plan, int32_t state);
 /* BKMA_W_TABLE: per-line weights, i0_count x (degree+1) floats (host or
  * device pointer), applied on the plan's own departure offsets. */
 bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device);

@@ -131,6 +131,12 @@ class AdvectionPlan:
         """Time steps per kernel launch (shared-memory strips; 1 = off)."""
         check(load().bkma_adv_plan_set_fusion(self._h, steps_per_launch))
 
+    def set_fused_state(self, state: str):
+        """On-chip state of fused steps: "f32" (bit-identical to one step
+        per launch) or "f32x2" (hi + lo FP32 pair, one FP32 rounding per
+        launch)."""
+        check(load().bkma_adv_plan_set_fused_state(self._h, {"f32": 0, "f32x2": 1}[state]))
+
     def autotune(self, field, stream=None):
         check(load().bkma_adv_plan_autotune(self._h, _ptr(field), _stream(stream)))
         return self.info()

@@ -71,6 +71,7 @@ SIGNATURES = {
     "bkma_adv_plan_autotune": (_st, [_vp, _vp, _vp]),
     "bkma_adv_plan_set_tile": (_st, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "bkma_adv_plan_set_fusion": (_st, [_vp, C.c_int32]),
+    "bkma_adv_plan_set_fused_state": (_st, [_vp, C.c_int32]),
     "bkma_adv_plan_set_weights": (_st, [_vp, _vp, C.c_int32]),
     "bkma_adv_plan_line_table": (_st, [_vp, _i32p, _dp]),
     "bkma_adv_plan_status": (_st, [_vp, _vp]),

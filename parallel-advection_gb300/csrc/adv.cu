@@ -644,6 +644,22 @@ bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_laun
     return BKMA_OK;
 }
 
+bkma_status bkma_adv_plan_set_fused_state(bkma_adv_plan *plan, int32_t state) {
+    BKMA_CHECK_ARG(plan && (state == BKMA_FUSED_F32 || state == BKMA_FUSED_F32X2),
+                   "state must be BKMA_FUSED_F32 or BKMA_FUSED_F32X2");
+    AdvPlanImpl &p = plan->impl;
+    if (state == BKMA_FUSED_F32X2) {
+        if (p.desc.dtype != BKMA_F32 || p.desc.impl == BKMA_ADV_PLAIN)
+            return fail(BKMA_ERR_UNSUPPORTED, "the hi + lo fused state is for FP32 staged plans");
+        if (!(p.npts == 4 || p.npts == 6 || p.npts == 10))
+            return fail(BKMA_ERR_UNSUPPORTED, "the hi + lo fused state needs degree 3, 5 or 9");
+        if (adv_fused_x2_smem(p) > kMaxSmem || p.desc.n1 > 3632)
+            return fail(BKMA_ERR_UNSUPPORTED, "lines too long for the hi + lo fused state");
+    }
+    p.fuse_x2 = state == BKMA_FUSED_F32X2 ? 1 : 0;
+    return BKMA_OK;
+}
+
 bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device) {
     BKMA_CHECK_ARG(plan && weights, "null argument");
     AdvPlanImpl &p = plan->impl;

@@ -204,6 +204,148 @@ __global__ void __launch_bounds__(kFuseThreads) adv_fused_f32(AdvStagedArgs<floa
     }
 }
 
+// Extended-precision fused steps: the on-chip state of a cell is the
+// unevaluated sum hi + lo of two FP32 numbers (|lo| <= half an ulp of hi);
+// HBM still holds FP32 (hi is staged with lo = 0, and hi = RN(hi + lo) is
+// written back). Per cell and step, in packed FP32x2:
+//   d_k = (hi_k - hi_c) + (lo_k - lo_c),  s = sum_{k != c} w_k d_k  (the
+//   staged kernel's fma order), t = lo_c + s,
+//   (hi', lo') = TwoSum(hi_c, t)   (Knuth: exact, no magnitude condition).
+// With lo = 0 this is the FP32 kernel's arithmetic bit for bit (d_k is the
+// same difference, t = s exactly, hi' = RN(hi_c + s)), so one step per launch
+// gives the same bits; over k steps the field is rounded to FP32 once
+// instead of k times. Thread map: W = 4 columns (one float4 group), R
+// consecutive rows per thread, hi and lo register rings.
+template <int NT, int R>
+__global__ void __launch_bounds__(kFuseThreads) adv_fused_f32x2(AdvStagedArgs<float> a, int ksteps) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int C = NT / 2 - 1;
+    TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, 1, a.W, a.ncb);
+    const int n1 = (int)a.n1;
+    const int wc = tc.wc;
+    constexpr int ws = 4;
+    float *hi_in = reinterpret_cast<float *>(smem_raw);
+    float *lo_in = hi_in + (size_t)n1 * ws;
+    float *hi_out = lo_in + (size_t)n1 * ws;
+    float *lo_out = hi_out + (size_t)n1 * ws;
+    const int64_t line = tc.line0;
+    stage_tile_elems<float>(hi_in, a.src, a.n1, a.n2, line, 1, tc.c0, wc, ws, 0, n1 * ws);
+    for (int i = threadIdx.x; i < n1 * ws; i += blockDim.x) lo_in[i] = 0.f;
+    __syncthreads();
+    const int exc = a.exc_index[line];
+    const int base = exc < 0 ? a.base[line] : 0;
+    float2 w2[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        const float wk = exc < 0 ? a.w[line * NT + k] : 0.f;
+        w2[k] = make_float2(wk, wk);
+    }
+    const AdvExcCell<float> *cells = exc < 0 ? nullptr : a.exc + (int64_t)exc * n1;
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const int r0 = (int)threadIdx.x * R;
+    const int nr = max(0, min(R, n1 - r0));
+    // one cell pair (columns 2j, 2j+1 of the group): returns (hi', lo')
+    auto pair = [&](const float4 (&h)[NT], const float4 (&l)[NT], const float2 (&wv)[NT], bool upper,
+                    float2 &oh, float2 &ol) {
+        const float2 hc = upper ? make_float2(h[C].z, h[C].w) : make_float2(h[C].x, h[C].y);
+        const float2 lc = upper ? make_float2(l[C].z, l[C].w) : make_float2(l[C].x, l[C].y);
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            if (k == C) continue;
+            const float2 hk = upper ? make_float2(h[k].z, h[k].w) : make_float2(h[k].x, h[k].y);
+            const float2 lk = upper ? make_float2(l[k].z, l[k].w) : make_float2(l[k].x, l[k].y);
+            const float2 dh = __ffma2_rn(hc, m1, hk);
+            const float2 dl = __ffma2_rn(lc, m1, lk);
+            acc = __ffma2_rn(wv[k], __fadd2_rn(dh, dl), acc);
+        }
+        const float2 t = __fadd2_rn(lc, acc);
+        const float2 sum = __fadd2_rn(hc, t);
+        const float2 bb = __ffma2_rn(hc, m1, sum);                 // sum - hc
+        const float2 ab = __ffma2_rn(bb, m1, sum);                 // sum - bb
+        const float2 ea = __ffma2_rn(ab, m1, hc);                  // hc - ab
+        const float2 eb = __ffma2_rn(bb, m1, t);                   // t - bb
+        oh = sum;
+        ol = __fadd2_rn(ea, eb);
+    };
+    auto cell4 = [&](const float4 (&h)[NT], const float4 (&l)[NT], const float2 (&wv)[NT], float *dh,
+                     float *dl) {
+        float2 h0, l0, h1, l1;
+        pair(h, l, wv, false, h0, l0);
+        pair(h, l, wv, true, h1, l1);
+        *reinterpret_cast<float4 *>(dh) = make_float4(h0.x, h0.y, h1.x, h1.y);
+        *reinterpret_cast<float4 *>(dl) = make_float4(l0.x, l0.y, l1.x, l1.y);
+    };
+    for (int step = 0; step < ksteps; ++step) {
+        if (nr > 0 && exc < 0) {
+            int q0 = r0 + base;
+            if (q0 >= n1) q0 -= n1;
+            auto row = [&](const float *b, int i) -> float4 {
+                int q = q0 + i;
+                if (q >= n1) q -= n1;
+                return *reinterpret_cast<const float4 *>(b + q * ws);
+            };
+            float4 rh[NT], rl[NT];
+#pragma unroll
+            for (int i = 0; i < NT - 1; ++i) {
+                rh[i] = row(hi_in, i);
+                rl[i] = row(lo_in, i);
+            }
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                rh[(i + NT - 1) % NT] = row(hi_in, i + NT - 1);
+                rl[(i + NT - 1) % NT] = row(lo_in, i + NT - 1);
+                if (i < nr) {
+                    float4 h[NT], l[NT];
+#pragma unroll
+                    for (int k = 0; k < NT; ++k) {
+                        h[k] = rh[(i + k) % NT];
+                        l[k] = rl[(i + k) % NT];
+                    }
+                    cell4(h, l, w2, hi_out + (r0 + i) * ws, lo_out + (r0 + i) * ws);
+                }
+            }
+        } else if (nr > 0) {
+            for (int i = 0; i < nr; ++i) {
+                const AdvExcCell<float> &e = cells[r0 + i];
+                int q = r0 + i + e.base;
+                if (q >= n1) q -= n1;
+                float4 h[NT], l[NT];
+                float2 wv[NT];
+#pragma unroll
+                for (int k = 0; k < NT; ++k) {
+                    int qk = q + k;
+                    if (qk >= n1) qk -= n1;
+                    h[k] = *reinterpret_cast<const float4 *>(hi_in + qk * ws);
+                    l[k] = *reinterpret_cast<const float4 *>(lo_in + qk * ws);
+                    wv[k] = make_float2(e.w[k], e.w[k]);
+                }
+                cell4(h, l, wv, hi_out + (r0 + i) * ws, lo_out + (r0 + i) * ws);
+            }
+        }
+        __syncthreads();
+        float *t = hi_in;
+        hi_in = hi_out;
+        hi_out = t;
+        t = lo_in;
+        lo_in = lo_out;
+        lo_out = t;
+    }
+    float *Gp = a.dst + line * a.n1 * a.n2 + tc.c0;
+    for (int i = threadIdx.x; i < n1 * wc; i += blockDim.x) {
+        const int r = i / wc, cc = i - r * wc;
+        Gp[(int64_t)r * a.n2 + cc] = hi_in[r * ws + cc];
+    }
+}
+
+// Rows per thread of the extended kernel: the fewest of 3, 5, 9 that cover n1
+// with 512 threads (0: n1 too long).
+int fused_x2_rows(int64_t n1) {
+    for (int r : {3, 5, 9})
+        if ((int64_t)kFuseThreads * r >= n1) return r;
+    return 0;
+}
+
 int fused_f32_w(const AdvPlanImpl &p, size_t max_smem) {
     // 8-column strips (three CTAs per SM for n1 = 1024); narrower for longer
     // lines, so that rowblocks x kRowsF32 covers n1
@@ -239,6 +381,32 @@ cudaError_t launch_fused_f32(const AdvPlanImpl &p, const void *src, void *dst, i
                                          (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<(unsigned)p.tiles(W, 1), kFuseThreads, smem, st>>>(a, ksteps);
+    return cudaGetLastError();
+}
+
+template <int NT, int R>
+cudaError_t launch_fused_x2(const AdvPlanImpl &p, const void *src, void *dst, int ksteps,
+                            cudaStream_t st) {
+    AdvStagedArgs<float> a{};
+    a.src = (const float *)src;
+    a.dst = (float *)dst;
+    a.n1 = p.desc.n1;
+    a.n2 = p.desc.n2;
+    a.lines = p.lines;
+    a.W = 4;
+    a.R = 1;
+    a.ncb = p.ncb(4);
+    a.base = p.d_base;
+    a.w = (const float *)p.d_w;
+    a.exc_index = p.d_exc_index;
+    a.exc = (const AdvExcCell<float> *)p.d_exc;
+    a.line_list = nullptr;
+    const size_t smem = adv_fused_x2_smem(p);
+    auto kern = adv_fused_f32x2<NT, R>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)p.tiles(4, 1), kFuseThreads, smem, st>>>(a, ksteps);
     return cudaGetLastError();
 }
 
@@ -282,7 +450,12 @@ cudaError_t launch_fused_npts(const AdvPlanImpl &p, const void *src, void *dst, 
 
 }  // namespace
 
+size_t adv_fused_x2_smem(const AdvPlanImpl &p) {
+    return 4 * (size_t)p.desc.n1 * 4 * sizeof(float);
+}
+
 int adv_fused_tile_w(const AdvPlanImpl &p, size_t max_smem) {
+    if (p.fuse_x2) return adv_fused_x2_smem(p) <= max_smem && fused_x2_rows(p.desc.n1) ? 4 : 0;
     if (p.desc.dtype == BKMA_F32) {
         const int w = fused_f32_w(p, max_smem);
         if (w) return w;
@@ -301,6 +474,21 @@ int adv_fused_tile_w(const AdvPlanImpl &p, size_t max_smem) {
 
 cudaError_t adv_fused_launch(const AdvPlanImpl &p, const void *src, void *dst, int W, int k,
                              cudaStream_t st) {
+    if (p.fuse_x2) {
+        if (W != 4) return cudaErrorInvalidValue;
+        switch (p.npts * 16 + fused_x2_rows(p.desc.n1)) {
+        case 4 * 16 + 3: return launch_fused_x2<4, 3>(p, src, dst, k, st);
+        case 4 * 16 + 5: return launch_fused_x2<4, 5>(p, src, dst, k, st);
+        case 4 * 16 + 9: return launch_fused_x2<4, 9>(p, src, dst, k, st);
+        case 6 * 16 + 3: return launch_fused_x2<6, 3>(p, src, dst, k, st);
+        case 6 * 16 + 5: return launch_fused_x2<6, 5>(p, src, dst, k, st);
+        case 6 * 16 + 9: return launch_fused_x2<6, 9>(p, src, dst, k, st);
+        case 10 * 16 + 3: return launch_fused_x2<10, 3>(p, src, dst, k, st);
+        case 10 * 16 + 5: return launch_fused_x2<10, 5>(p, src, dst, k, st);
+        case 10 * 16 + 9: return launch_fused_x2<10, 9>(p, src, dst, k, st);
+        default: return cudaErrorInvalidValue;
+        }
+    }
     if (p.desc.dtype == BKMA_F32) {
         if (W == fused_f32_w(p, (size_t)227 * 1024)) {
             switch (p.npts) {

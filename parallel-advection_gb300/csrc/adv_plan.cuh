@@ -38,6 +38,7 @@ struct AdvPlanImpl {
     int W = 16, R = 1, threads = 256, path = 0;
     bool autotuned = false;
     int fuse = 1;  // time steps per launch (adv_fused.cu when > 1)
+    int fuse_x2 = 0;  // fused on-chip state: 0 FP32, 1 FP32 hi + lo pair
     struct TmapCache {
         const void *ptr;
         int W;
@@ -127,6 +128,8 @@ cudaError_t adv_stream_launch_fields(int npts, const StreamField *d_fields, int 
 // Multi-step fused form (adv_fused.cu): strip width for a plan (0 if the
 // plan's lines are too long), and one launch of k fused steps src -> dst.
 int adv_fused_tile_w(const AdvPlanImpl &p, size_t max_smem);
+// Shared memory of the hi + lo fused kernel (four n1 x 4 FP32 buffers).
+size_t adv_fused_x2_smem(const AdvPlanImpl &p);
 cudaError_t adv_fused_launch(const AdvPlanImpl &p, const void *src, void *dst, int W, int k,
                              cudaStream_t st);
 

@@ -546,3 +546,68 @@ def test_fused_steps_limits(bkma, cuda):
         _plan(bkma, long_lines, dtype="f32").set_fusion(4)
     with pytest.raises(bkma.BkmaError):
         _plan(bkma, p, dtype="f32").set_fusion(0)
+
+
+@pytest.mark.parametrize("case,vel", FUSED_CASES)
+@pytest.mark.parametrize("degree", [3, 5, 9])
+def test_fused_x2_one_step_per_launch_is_fp32(bkma, cuda, case, vel, degree):
+    """With the hi + lo state and one step per launch, lo is zero when every
+    step starts, and the arithmetic is the FP32 kernel's: same bits."""
+    import torch
+    p = AdvParams(*case)
+    kw = dict(dtype="f32", degree=degree, weights="reference" if degree == 5 else "lagrange")
+    if vel is not None:
+        kw["velocity"] = vel
+    f0 = _init(p, 41).astype(np.float32).astype(np.float64)
+    ref = _to(cuda, f0, torch.float32)
+    _plan(bkma, p, **kw).step(ref, nsteps=5)
+    plan = _plan(bkma, p, **kw)
+    plan.set_fused_state("f32x2")
+    plan.set_fusion(4)
+    d = _to(cuda, f0, torch.float32)
+    for _ in range(5):
+        plan.step(d, nsteps=1)
+    plan.status()
+    assert torch.equal(d, ref)
+
+
+@pytest.mark.parametrize("case,vel", FUSED_CASES)
+def test_fused_x2_rounds_once_per_launch(bkma, cuda, oracle, case, vel):
+    """50 steps in one launch with the hi + lo state against the FP64 oracle:
+    the error stays near one FP32 rounding (|f| <= 1.01: half an ulp is
+    6e-8), below the error of 50 FP32 steps, each rounded to FP32; out of
+    place the input stays as it was."""
+    import torch
+    p = AdvParams(*case)
+    kw = dict(dtype="f32")
+    if vel is not None:
+        kw["velocity"] = vel
+    f0 = _init(p, 43).astype(np.float32).astype(np.float64)
+    want = oracle.adv_step(p, f0.copy(), 50, velocity=vel)
+    scale = np.abs(want).max()
+    std = _to(cuda, f0, torch.float32)
+    _plan(bkma, p, **kw).step(std, nsteps=50)
+    plan = _plan(bkma, p, inplace=False, **kw)
+    plan.set_fused_state("f32x2")
+    plan.set_fusion(50)
+    src = _to(cuda, f0, torch.float32)
+    out = torch.zeros_like(src)
+    plan.step(src, out=out, nsteps=50)
+    plan.status()
+    assert torch.equal(src, _to(cuda, f0, torch.float32))
+    err_x2 = np.abs(out.cpu().numpy().astype(np.float64) - want).max() / scale
+    err_std = np.abs(std.cpu().numpy().astype(np.float64) - want).max() / scale
+    assert err_x2 <= 2.5e-7, (err_x2, err_std)
+    assert err_x2 < err_std, (err_x2, err_std)
+
+
+def test_fused_x2_limits(bkma, cuda):
+    p = AdvParams(2, 64, 4, 0.001, 0.0, 1.0, -1.0, 1.0)
+    with pytest.raises(bkma.BkmaError):
+        _plan(bkma, p, dtype="f64").set_fused_state("f32x2")
+    long_lines = AdvParams(2, 4096, 4, 0.001, 0.0, 1.0, -1.0, 1.0)
+    with pytest.raises(bkma.BkmaError):
+        _plan(bkma, long_lines, dtype="f32").set_fused_state("f32x2")
+    plan = _plan(bkma, p, dtype="f32")
+    plan.set_fused_state("f32x2")
+    plan.set_fused_state("f32")
