@@ -133,8 +133,9 @@ bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_laun
 /* On-chip state of the fused steps (FP32 plans, degree 3, 5 or 9).
  * BKMA_FUSED_F32 (default): FP32, bit-identical to one step per launch.
  * BKMA_FUSED_F32X2: each cell is held as an unevaluated sum hi + lo of two
- * FP32 numbers between the steps of a launch (exact TwoSum renormalisation),
- * so the field is rounded to FP32 once per launch instead of once per step;
+ * FP32 numbers between the steps of a launch (Fast2Sum renormalisation, exact
+ * wherever the cell's value exceeds its one-step change), so the field is
+ * rounded to FP32 once per launch instead of once per step;
  * one step per launch still gives the FP32 bits. HBM traffic is unchanged.
  * BKMA_ERR_UNSUPPORTED for FP64 plans, the plain form, or n1 > 3632 (four
  * n1 x 4-column FP32 buffers must fit shared memory). No counterpart in the
