@@ -10,7 +10,9 @@
 // stencil window in registers: a ring of 4 blocks holds rows of the ORIGINAL
 // field from r0+d on (d = the line's signed tap-0 offset); the loads of the
 // block three ahead are issued before the current block's stores, so two
-// blocks of loads are always in flight. Output row r0+i is the incremental
+// blocks of loads are always in flight; an L2 prefetch runs kPrefetch blocks
+// further ahead, so that those loads find their rows in L2 (the registers
+// bound the bytes in flight, and with them the HBM rate at DRAM latency). Output row r0+i is the incremental
 // form f_c + sum_k w_k (f_k - f_c) over the npts rows from r0+d+i, the same
 // operations in the same order as the staged kernels (identical bits).
 //
@@ -41,6 +43,10 @@ constexpr int kU = 8;         // output rows per block
 constexpr int kWarps = 8;     // warps per CTA
 constexpr int kSeamRows = kStreamSeam + kStreamBack;
 constexpr int kPitch = 32;    // shared-memory row pitch (floats) of a warp's seams
+// L2 prefetch distance in blocks beyond the register ring's loads (batched
+// workload: 681 GCells/s without, 702 at 4, 716 at 8, 665 at 12, 643 at 16;
+// 727 with the start-of-segment burst)
+constexpr int kPrefetch = 8;
 
 template <int NT>
 __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group, int seg,
@@ -105,6 +111,9 @@ __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group
     // of block t. At block t the loads of block t+3 are issued (into the
     // slot block t-1 used), and block t's outputs read slots t and t+1, so
     // two blocks of loads stay in flight behind the one being computed.
+    // rows the steady-state prefetch would have covered before the first block
+    for (int j = max(a, a + d + 3 * kU); j < min(b, a + d + (3 + kPrefetch) * kU); ++j)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(src + (int64_t)j * n2));
     float B[4 * kU];
 #pragma unroll
     for (int i = 0; i < 3 * kU; ++i) B[i] = ld(a + d + i);
@@ -114,6 +123,15 @@ __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group
         constexpr int ph = decltype(ph_c)::value;  // t % 4
         constexpr int ld_slot = (ph + 3) % 4;
         const int j0 = r0 + d + 3 * kU;
+        {  // L2 prefetch of the rows kPrefetch blocks beyond this load
+            const int jp = j0 + kPrefetch * kU;
+            if (jp >= a && jp + kU <= b) {
+                const float *pp = pn + (int64_t)kPrefetch * kU * n2;
+#pragma unroll
+                for (int i = 0; i < kU; ++i)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(pp + (int64_t)i * n2));
+            }
+        }
         if (j0 >= a && j0 + kU <= b) {
 #pragma unroll
             for (int i = 0; i < kU; ++i) {
