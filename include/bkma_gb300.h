@@ -91,7 +91,8 @@ typedef struct bkma_adv_plan_info {
     int32_t npts;              /* stencil points (degree + 1) */
     int32_t autotuned;         /* 1 once bkma_adv_plan_autotune picked the tile */
     int64_t tiles;             /* CTAs per step */
-    int32_t path;              /* 0: cp.async staging, 1: TMA (cp.async.bulk.tensor) staging */
+    int32_t path;              /* 0: cp.async staging, 1: TMA (cp.async.bulk.tensor) staging,
+                                  2: streamed columns, 3: contiguous lines (n2 = 1) */
     int32_t reserved;
 } bkma_adv_plan_info;
 
@@ -118,7 +119,9 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * or path 2: streamed columns (FP32, every line's per-step shift within the
  * streamed window, n1 >= 64), where R is the row-segment mode (0 = from the
  * field's size, k = up to k segments per 32-column group, k <= 8) and W the
- * tile width of the staged pass over exception lines. */
+ * tile width of the staged pass over exception lines, or path 3: contiguous
+ * lines (FP32, n2 = 1, n1 % 4 == 0, n1 >= 16; W = 1, R whole lines per CTA,
+ * `threads` ignored: 256). R <= 1024 on paths 0, 1 and 3. */
 bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
                                    int32_t path);
 /* Multi-step fusion: bkma_adv_step runs `steps_per_launch` time steps per

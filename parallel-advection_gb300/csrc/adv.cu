@@ -166,17 +166,29 @@ void default_tile(AdvPlanImpl &p) {
     while (p.R > 1 && p.smem_bytes(p.W, p.R) > kMaxSmem) p.R /= 2;
     while (p.W > 1 && p.smem_bytes(p.W, p.R) > kMaxSmem) p.W /= 2;
     p.threads = 256;
-    // TMA staging for FP32 column tiles; launch_once falls back per call when
-    // a field pointer is not 16-byte aligned.
+    // TMA staging for FP32 column tiles (512 threads: 4-5 % faster than 256
+    // on the reference's n1 = 1024 shapes); launch_once falls back per call
+    // when a field pointer is not 16-byte aligned.
     const void *aligned_probe = reinterpret_cast<const void *>(uintptr_t(256));
     p.path = (p.R == 1 && adv_tma_eligible(p, aligned_probe, p.W) &&
               adv_tma_smem(p, p.W) <= kMaxSmem) ? 1 : 0;
-    if (p.path == 0 && p.stream_ok && n2 >= 8) {
+    if (p.path == 1) p.threads = 512;
+    // Streaming beats TMA tiles when a tile leaves one CTA per SM (n1 >= 2048:
+    // 534 vs 760 GCells/s at 1024 x 2048 x 1024) or when rows are 1 MB or
+    // more apart (1 x 1024 x 2^21: 400 vs 699, every box row a new page).
+    const bool tma_poor = adv_tma_smem(p, p.W) > 100 * 1024 || n2 * p.esize >= (1 << 20);
+    if (p.stream_ok && n2 >= 8 && (p.path == 0 || tma_poor)) {
         // rows that are not 16-byte aligned, or tiles too tall for the TMA
         // form: stream the columns (row segments chosen from the size)
         p.path = 2;
         p.R = 0;
         p.W = (int)std::min<int64_t>(16, n2);
+    }
+    if (adv_rows_shape_ok(p) && adv_rows_smem(p, adv_rows_default_r(p)) <= kMaxSmem) {
+        // n2 = 1: runs of whole contiguous lines
+        p.path = 3;
+        p.W = 1;
+        p.R = adv_rows_default_r(p);
     }
 }
 
@@ -304,6 +316,12 @@ cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R
         return launch_staged_npts<float>(p, src, dst, p.exc_tile_w(kMaxSmem), 1, 256, st,
                                          p.d_exc_lines, p.n_exc);
     }
+    if (path == 3) {
+        if (adv_rows_eligible(p, src, dst, R)) return adv_rows_launch(p, src, dst, R, st);
+        // unaligned field: the generic staged kernel on whole rows
+        W = 1;
+        while (R > 1 && p.smem_bytes(W, R) > kMaxSmem) R /= 2;
+    }
     if (p.desc.impl == BKMA_ADV_PLAIN)
         return launch_plain(p, (const double *)src, (double *)dst, W, R, threads, st);
     if (p.desc.dtype == BKMA_F32) return launch_staged_npts<float>(p, src, dst, W, R, threads, st);
@@ -430,7 +448,9 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
             return BKMA_OK;
         }
     }
-    std::vector<TuneVal> cands;
+    // The plan's own tile is the first candidate, so tuning never ends on a
+    // tile slower than the default.
+    std::vector<TuneVal> cands{{p.W, p.R, p.threads, p.path}};
     const int64_t n2 = p.desc.n2;
     const int ths[2] = {256, 512};
     if (n2 >= 8) {
@@ -443,9 +463,12 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     }
     if (p.stream_ok)
         for (int segs : {0, 1, 2, 4, 8}) cands.push_back({(int)std::min<int64_t>(16, n2), segs, 256, 2});
-    for (int R : {1, 2, 4, 8, 16})
-        if (n2 < 32 && R <= p.lines)
+    for (int R : {1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024})
+        if (n2 < 32 && R <= p.lines && p.smem_bytes((int)n2, R) <= kMaxSmem)
             for (int t : ths) cands.push_back({(int)n2, R, t, 0});
+    if (adv_rows_shape_ok(p))
+        for (int R = 1; R <= 4096 && R <= p.lines; R *= 2)
+            if (adv_rows_eligible(p, field, field, R)) cands.push_back({1, R, 256, 3});
     cudaEvent_t e0, e1;
     BKMA_CUDA_TRY(cudaEventCreate(&e0));
     BKMA_CUDA_TRY(cudaEventCreate(&e1));
@@ -453,7 +476,8 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     TuneVal bestv{p.W, p.R, p.threads, p.path};
     for (const TuneVal &c : cands) {
         const size_t need = c.path == 1 ? adv_tma_smem(p, c.W)
-                            : c.path == 2 ? 0 : p.smem_bytes(c.W, c.R);
+                            : c.path == 2 ? 0
+                            : c.path == 3 ? adv_rows_smem(p, c.R) : p.smem_bytes(c.W, c.R);
         if (need > kMaxSmem) continue;
         cudaError_t err = launch_once(p, field, field, c.W, c.R, c.threads, c.path, st);  // warm-up
         if (err != cudaSuccess) {
@@ -582,10 +606,11 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
     info->threads = p.threads;
     info->smem_bytes = (int32_t)(p.path == 1   ? adv_tma_smem(p, p.W)
                                  : p.path == 2 ? adv_stream_smem()
+                                 : p.path == 3 ? adv_rows_smem(p, p.R)
                                                : p.smem_bytes(p.W, p.R));
     info->npts = p.npts;
     info->autotuned = p.autotuned ? 1 : 0;
-    info->tiles = p.tiles(p.W, p.R);
+    info->tiles = p.path == 3 ? (p.lines + p.R - 1) / p.R : p.tiles(p.W, p.R);
     info->path = p.path;
     return BKMA_OK;
 }
@@ -610,12 +635,12 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                                    int32_t path) {
     BKMA_CHECK_ARG(plan, "null argument");
     AdvPlanImpl &p = plan->impl;
-    BKMA_CHECK_ARG(W >= 1 && W <= 1024 && R >= (path == 2 ? 0 : 1) && R <= 64,
-                   "W must be in [1,1024], R in [1,64] (path 2: row-segment mode 0..8)");
+    BKMA_CHECK_ARG(W >= 1 && W <= 1024 && R >= (path == 2 ? 0 : 1) && R <= 1024,
+                   "W must be in [1,1024], R in [1,1024] (path 2: row-segment mode 0..8)");
     BKMA_CHECK_ARG(threads == 128 || threads == 256 || threads == 512, "threads must be 128, 256 or 512");
-    BKMA_CHECK_ARG(path >= 0 && path <= 2, "path must be 0, 1 or 2");
+    BKMA_CHECK_ARG(path >= 0 && path <= 3, "path must be 0, 1, 2 or 3");
     BKMA_CHECK_ARG(path != 2 || p.stream_ok, "streamed form not available for this plan");
-    BKMA_CHECK_ARG(path == 2 || R == 1 || W >= p.desc.n2, "R > 1 needs whole-row tiles (W >= n2)");
+    BKMA_CHECK_ARG(path >= 2 || R == 1 || W >= p.desc.n2, "R > 1 needs whole-row tiles (W >= n2)");
     BKMA_CHECK_ARG(path != 2 || R <= 8, "path 2: R is the row-segment mode, 0 (auto) to 8");
     if (path == 1) {
         const void *probe = reinterpret_cast<const void *>(uintptr_t(256));
@@ -623,6 +648,10 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
         BKMA_CHECK_ARG(adv_tma_smem(p, W) <= kMaxSmem, "tile does not fit shared memory");
     } else if (path == 0) {
         BKMA_CHECK_ARG(p.smem_bytes(W, R) <= kMaxSmem, "tile does not fit shared memory");
+    } else if (path == 3) {
+        BKMA_CHECK_ARG(adv_rows_shape_ok(p) && W == 1 && adv_rows_smem(p, R) <= kMaxSmem,
+                       "path 3 needs an FP32 plan with n2 = 1, n1 % 4 == 0, n1 >= 16, "
+                       "W = 1 and R lines that fit shared memory");
     }
     p.W = W;
     p.R = R;

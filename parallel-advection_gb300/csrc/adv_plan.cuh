@@ -34,7 +34,8 @@ struct AdvPlanImpl {
     // every non-exception line can stream (FP32 tables, see stream_line_ok)
     bool stream_ok = false;
     // launch shape: path 0 = cp.async staging (any shape), 1 = TMA staging,
-    // 2 = streamed columns (+ staged exception lines)
+    // 2 = streamed columns (+ staged exception lines), 3 = contiguous lines
+    // (n2 = 1, R lines per CTA)
     int W = 16, R = 1, threads = 256, path = 0;
     bool autotuned = false;
     int fuse = 1;  // time steps per launch (adv_fused.cu when > 1)
@@ -119,6 +120,14 @@ int64_t adv_stream_groups(const AdvPlanImpl &p);
 int64_t adv_stream_ctas(const AdvPlanImpl &p, int segs);
 // Device descriptor of a plan's field for the streamed kernel.
 StreamField adv_stream_field(const AdvPlanImpl &p, const void *src, void *dst, int segs);
+// Contiguous-line form (adv_rows.cu, FP32, n2 = 1, n1 % 4 == 0, n1 >= 16):
+// R whole lines per CTA.
+bool adv_rows_shape_ok(const AdvPlanImpl &p);
+bool adv_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R);
+size_t adv_rows_smem(const AdvPlanImpl &p, int R);
+int adv_rows_default_r(const AdvPlanImpl &p);
+cudaError_t adv_rows_launch(const AdvPlanImpl &p, const void *src, void *dst, int R,
+                            cudaStream_t st);
 size_t adv_stream_smem();  // static shared memory per CTA of the streamed kernel
 // All fields of `d_fields` (device array, ascending cta0) have npts taps;
 // nctas = the sum of their CTA counts.

@@ -611,3 +611,60 @@ def test_fused_x2_limits(bkma, cuda):
     plan = _plan(bkma, p, dtype="f32")
     plan.set_fused_state("f32x2")
     plan.set_fused_state("f32")
+
+
+ROWS_CASES = [
+    # (n0, n1, n2, dt, minX, maxX, minVx, maxVx), velocity or None
+    ((300, 16, 1, 0.001, 0.0, 1.0, -1.0, 1.0), None),     # the reference's 16-cell lines
+    ((7, 1024, 1, 0.002, 0.0, 1.0, -2.0, 2.0), None),
+    ((3, 4096, 1, 0.0007, 0.0, 1.0, -1.0, 1.0), None),
+    ((5, 20, 1, 0.004, 0.0, 1.0, -3.0, 3.0), None),      # n1 not a power of two, shifts > 1 cell
+    ((6, 1000, 1, 0.001, 0.0, 1.0, -2.0, 3.0), EXC_VEL),  # exception lines
+]
+
+
+@pytest.mark.parametrize("case,vel", ROWS_CASES)
+@pytest.mark.parametrize("degree", [3, 5, 9])
+def test_rows_path_bit_identical(bkma, cuda, case, vel, degree):
+    """Contiguous-line kernel (n2 = 1, path 3) against the generic staged
+    kernel on whole rows: same bits, for several lines per CTA (R that does
+    not divide n0 leaves a partial last CTA)."""
+    import torch
+    p = AdvParams(*case)
+    kw = dict(dtype="f32", degree=degree, weights="reference" if degree == 5 else "lagrange")
+    if vel is not None:
+        kw["velocity"] = vel
+    f0 = _init(p, 51).astype(np.float32).astype(np.float64)
+    ref = _to(cuda, f0, torch.float32)
+    staged = _plan(bkma, p, **kw)
+    staged.set_tile(1, 1, 256, 0)
+    staged.step(ref, nsteps=3)
+    plan = _plan(bkma, p, **kw)
+    assert plan.info()["path"] == 3
+    for R in (1, 2, 64):
+        plan.set_tile(1, min(R, p.n0), 256, 3)
+        d = _to(cuda, f0, torch.float32)
+        plan.step(d, nsteps=3)
+        plan.status()
+        assert torch.equal(d, ref), R
+
+
+def test_rows_path_misaligned_field_falls_back(bkma, cuda, oracle):
+    """A field 4 bytes off the 16-byte grid runs the staged kernel instead
+    (same bits), and both match the oracle within the FP32 bound."""
+    import torch
+    p = AdvParams(9, 64, 1, 0.003, 0.0, 1.0, -1.0, 1.0)
+    f0 = _init(p, 52).astype(np.float32).astype(np.float64)
+    plan = _plan(bkma, p, dtype="f32")
+    assert plan.info()["path"] == 3
+    aligned = _to(cuda, f0, torch.float32)
+    plan.step(aligned, nsteps=2)
+    buf = torch.zeros(f0.size + 4, dtype=torch.float32, device=cuda)
+    off = buf[1:1 + f0.size].view(p.n0, p.n1, p.n2)
+    off.copy_(_to(cuda, f0, torch.float32))
+    plan.step(off, nsteps=2)
+    plan.status()
+    assert torch.equal(off, aligned)
+    want = oracle.adv_step(p, f0.copy(), 2)
+    err = np.abs(aligned.cpu().numpy().astype(np.float64) - want).max() / np.abs(want).max()
+    assert err <= 3e-7 * 2 + 2e-7, err
