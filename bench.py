@@ -29,7 +29,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "parallel-advection_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-N0, N1, N2 = 2048, 1024, 512  # --n0 shrinks N0 for profiling captures only
+N0, N1, N2 = 2048, 1024, 512  # --n0/--n1/--n2 change the field for profiling captures only
 DT, MINX, MAXX = 0.001, 0.0, 1.0
 NOISE, SEED = 0.01, 12345
 CFG_STEPS = 50
@@ -253,8 +253,8 @@ def run_gpu(args):
     avg_launch_s = statistics.mean(launch_ms) / 1e3
     achieved = cells * 8 / avg_launch_s / 1e9
     info = plan.info()
-    kernel = {1: f"adv_tma_f32<6,{info['tile_cols']}>", 2: "adv_stream_f32<6>"}.get(
-        info["path"], "adv_staged<float,6>")
+    kernel = {1: f"adv_tma_f32<6,{info['tile_cols']}>", 2: "adv_stream_f32<6>",
+              3: "adv_rows_f32<6>"}.get(info["path"], "adv_staged<float,6>")
     traffic = None
     try:
         with open(PROFILE_JSON[info["path"]]) as fp:
@@ -340,9 +340,9 @@ def fused_block(bkma_gb300, dev, f, plan, vel, kw, cells):
         del a2
     del a1, fz
     return {"steps_per_launch": fused, "steps": CFG_STEPS,
-            "kernel": "adv_fused_f32<6> (512 threads, 8-column strips, two shared buffers)",
+            "kernel": "adv_fused_f32<6> (256 threads for n1 = 1024, 8-column strips, two shared buffers)",
             "hi_lo_state": {"steps_per_launch": x2,
-                            "kernel": "adv_fused_f32x2<6,3> (4-column strips, hi + lo FP32 pair)"},
+                            "kernel": "adv_fused_f32x2<6,3> (352 threads for n1 = 1024, 4-column strips, hi + lo FP32 pair)"},
             "note": "not the metric: state stays in shared memory between steps"}
 
 
@@ -672,15 +672,24 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip error/e2e/cpu/conv blocks")
     ap.add_argument("--n0", type=int, default=None, help="smaller field for profiling captures")
+    ap.add_argument("--n1", type=int, default=None, help="other line length (profiling captures)")
+    ap.add_argument("--n2", type=int, default=None, help="other column count (profiling captures)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="advection", choices=["advection", "conv", "batched", "learned", "fused"],
                     help="conv: only the conv1d block, as its own JSON line")
     ap.add_argument("--conv-batch", type=int, default=256, help="smaller batch for captures")
     ap.add_argument("--fields", type=int, default=64, help="batched workload: field count")
     args = ap.parse_args()
+    global N0, N1, N2
     if args.n0:
-        global N0
         N0 = args.n0
+    if args.n1:
+        N1 = args.n1
+    if args.n2:
+        N2 = args.n2
+    if args.n0 or args.n1 or args.n2:
+        global WORKLOAD
+        WORKLOAD = f"single advection FP32 {N0}x{N1}x{N2}, degree 5 (profiling shape)"
     if args.warmup < 3:
         args.warmup = 3
     if args.workload in ("batched", "learned", "fused") and args.impl != "reference":
