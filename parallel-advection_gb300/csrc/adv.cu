@@ -159,13 +159,17 @@ void default_tile(AdvPlanImpl &p) {
     } else {
         p.W = (int)n2;
         const size_t per = p.smem_bytes(p.W, 1);
-        int r = (int)std::max<size_t>(1, (48 * 1024) / std::max<size_t>(per, 1));
+        // very short lines: smaller CTAs (1048576 x 16 x 128: 2 slabs of
+        // 10.8 KB and 128 threads run at 744 GCells/s, 4 slabs and 256
+        // threads at 600)
+        const size_t target = p.desc.n1 <= 64 ? 24 * 1024 : 48 * 1024;
+        int r = (int)std::max<size_t>(1, target / std::max<size_t>(per, 1));
         r = (int)std::min<int64_t>(r, p.lines);
         p.R = std::max(1, r);
     }
     while (p.R > 1 && p.smem_bytes(p.W, p.R) > kMaxSmem) p.R /= 2;
     while (p.W > 1 && p.smem_bytes(p.W, p.R) > kMaxSmem) p.W /= 2;
-    p.threads = 256;
+    p.threads = (short_lines && p.desc.n1 <= 64) ? 128 : 256;
     // TMA staging for FP32 column tiles (512 threads: 4-5 % faster than 256
     // on the reference's n1 = 1024 shapes); launch_once falls back per call
     // when a field pointer is not 16-byte aligned.
@@ -189,6 +193,7 @@ void default_tile(AdvPlanImpl &p) {
         p.path = 3;
         p.W = 1;
         p.R = adv_rows_default_r(p);
+        p.threads = 256;  // the contiguous-line kernel's fixed CTA
     }
 }
 
@@ -452,7 +457,7 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     // tile slower than the default.
     std::vector<TuneVal> cands{{p.W, p.R, p.threads, p.path}};
     const int64_t n2 = p.desc.n2;
-    const int ths[2] = {256, 512};
+    const int ths[3] = {128, 256, 512};
     if (n2 >= 8) {
         for (int W : {8, 16, 32, 64})
             if (W <= n2 || W == 8)
@@ -465,6 +470,10 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
         for (int segs : {0, 1, 2, 4, 8}) cands.push_back({(int)std::min<int64_t>(16, n2), segs, 256, 2});
     for (int R : {1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024})
         if (n2 < 32 && R <= p.lines && p.smem_bytes((int)n2, R) <= kMaxSmem)
+            for (int t : ths) cands.push_back({(int)n2, R, t, 0});
+    // whole-row tiles of a few slabs for wider rows of short lines
+    for (int R : {1, 2, 4, 8, 16})
+        if (n2 >= 32 && n2 <= 256 && R <= p.lines && p.smem_bytes((int)n2, R) <= 96 * 1024)
             for (int t : ths) cands.push_back({(int)n2, R, t, 0});
     if (adv_rows_shape_ok(p))
         for (int R = 1; R <= 4096 && R <= p.lines; R *= 2)
