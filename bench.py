@@ -661,7 +661,7 @@ def e2e(plan, dev, cells):
             "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
             "time_steps_per_transfer": CFG_STEPS, "pinned_copy": link,
             "note": "one e2e step = H2D of the field + 50 advection steps + D2H, "
-                    "slab chunks pipelined on three streams"}
+                    "slab chunks pipelined: copies in on one stream, steps on two, copies out on one"}
 
 
 def main():

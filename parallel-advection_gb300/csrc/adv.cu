@@ -142,7 +142,7 @@ namespace bkma {
 namespace {
 
 constexpr size_t kMaxSmem = 227 * 1024;
-constexpr int kRunHostChunks = 16;  // slab chunks of bkma_adv_run_host's copy/compute pipeline
+constexpr int kRunHostChunks = 32;  // slab chunks of bkma_adv_run_host's copy/compute pipeline (8: 759, 16: 784, 32: 788, 64: 781 GCells/s e2e)
 
 // Default tile: columns of one slab when n2 is wide enough for 64-byte row
 // segments, otherwise whole slabs; about 32-64 KB of shared memory per CTA.
@@ -753,9 +753,9 @@ bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nste
         BKMA_CUDA_TRY(cudaStreamSynchronize(st));
         return BKMA_OK;
     }
-    // Pipeline over slab chunks: chunk c = copy in, nsteps steps, copy out, on
-    // stream c % 3; each chunk is a sub-plan of the same lines (same tables,
-    // bit-identical results), so copies of one chunk overlap steps of others.
+    // Pipeline over slab chunks: chunk c = copy in, nsteps steps, copy out;
+    // each chunk is a sub-plan of the same lines (same tables, bit-identical
+    // results), so copies of one chunk overlap steps of others.
     if ((int)p.chunks.size() != nch) {
         for (auto *c : p.chunks) bkma_adv_plan_destroy(c);
         p.chunks.clear();
@@ -777,8 +777,16 @@ bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nste
         if (!q) BKMA_CUDA_TRY(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
     for (auto &e : p.pipe_ev)
         if (!e) BKMA_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    BKMA_CUDA_TRY(cudaEventRecord(p.pipe_ev[3], st));
-    for (auto &q : p.pipe) BKMA_CUDA_TRY(cudaStreamWaitEvent(q, p.pipe_ev[3], 0));
+    while ((int)p.chunk_ev.size() < 2 * nch) {
+        cudaEvent_t e = nullptr;
+        BKMA_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        p.chunk_ev.push_back(e);
+    }
+    BKMA_CUDA_TRY(cudaEventRecord(p.pipe_ev[4], st));
+    for (auto &q : p.pipe) BKMA_CUDA_TRY(cudaStreamWaitEvent(q, p.pipe_ev[4], 0));
+    // Copies in run back to back on one stream, so the first chunk arrives
+    // at the link's full rate and the steps start early; each chunk's steps
+    // wait for its copy, each copy out for its steps.
     for (int c = 0; c < nch; ++c) {
         AdvPlanImpl &sp = plan_impl(p.chunks[(size_t)c]);
         sp.W = p.W;  // the parent's tile choice (set or autotuned)
@@ -790,13 +798,18 @@ bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nste
         const size_t nb = (size_t)sp.lines * slab;
         char *dev = (char *)p.d_host_buf + (size_t)l0 * slab;
         char *host = (char *)host_data + (size_t)l0 * slab;
-        cudaStream_t q = p.pipe[c % 3];
-        BKMA_CUDA_TRY(cudaMemcpyAsync(dev, host, nb, cudaMemcpyHostToDevice, q));
+        cudaEvent_t in_done = p.chunk_ev[2 * (size_t)c], stepped = p.chunk_ev[2 * (size_t)c + 1];
+        BKMA_CUDA_TRY(cudaMemcpyAsync(dev, host, nb, cudaMemcpyHostToDevice, p.pipe[0]));
+        BKMA_CUDA_TRY(cudaEventRecord(in_done, p.pipe[0]));
+        cudaStream_t q = p.pipe[1 + (c & 1)];
+        BKMA_CUDA_TRY(cudaStreamWaitEvent(q, in_done, 0));
         bkma_status s = adv_launch(sp, dev, nullptr, nsteps, q);
         if (s != BKMA_OK) return s;
-        BKMA_CUDA_TRY(cudaMemcpyAsync(host, dev, nb, cudaMemcpyDeviceToHost, q));
+        BKMA_CUDA_TRY(cudaEventRecord(stepped, q));
+        BKMA_CUDA_TRY(cudaStreamWaitEvent(p.pipe[3], stepped, 0));
+        BKMA_CUDA_TRY(cudaMemcpyAsync(host, dev, nb, cudaMemcpyDeviceToHost, p.pipe[3]));
     }
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
         BKMA_CUDA_TRY(cudaEventRecord(p.pipe_ev[k], p.pipe[k]));
         BKMA_CUDA_TRY(cudaStreamWaitEvent(st, p.pipe_ev[k], 0));
     }

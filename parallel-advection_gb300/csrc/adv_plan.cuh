@@ -48,14 +48,18 @@ struct AdvPlanImpl {
     std::vector<TmapCache> tmaps;  // TMA descriptors of recently used fields
     int *d_status = nullptr;       // device status word of the bounded waits
     // host-run buffer, and bkma_adv_run_host's pipeline: sub-plans over slab
-    // chunks (lines are independent) on three streams, so the copies of one
+    // chunks (lines are independent) on four streams, so the copies of one
     // chunk overlap the time steps of another
     void *d_host_buf = nullptr;
     size_t host_buf_bytes = 0;
     std::vector<bkma_adv_plan *> chunks;
     std::vector<int64_t> chunk_l0;
-    cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t pipe_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // pipe[0]: copies in (one after another), pipe[1..2]: steps of alternate
+    // chunks, pipe[3]: copies out; chunk_ev[2c] = chunk c copied in,
+    // chunk_ev[2c+1] = chunk c stepped
+    cudaStream_t pipe[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t pipe_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> chunk_ev;
     double *d_partials = nullptr;
     int device = 0;
 
@@ -64,6 +68,8 @@ struct AdvPlanImpl {
         for (auto &q : pipe)
             if (q) cudaStreamDestroy(q);
         for (auto &e : pipe_ev)
+            if (e) cudaEventDestroy(e);
+        for (auto &e : chunk_ev)
             if (e) cudaEventDestroy(e);
         cudaFree(d_base);
         cudaFree(d_w);
