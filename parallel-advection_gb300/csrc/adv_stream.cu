@@ -7,17 +7,18 @@
 // `segs` row segments, one warp each; a CTA of 8 warps holds 8/segs groups.
 //
 // A warp walks its segment [a, b) in blocks of U = 8 rows, keeping the
-// stencil window in registers: a ring of 4 blocks holds rows of the ORIGINAL
-// field from r0+d on (d = the line's signed tap-0 offset); the loads of the
-// block three ahead are issued before the current block's stores, so two
-// blocks of loads are always in flight; an L2 prefetch runs kPrefetch blocks
-// further ahead, so that those loads find their rows in L2 (the registers
-// bound the bytes in flight, and with them the HBM rate at DRAM latency). Output row r0+i is the incremental
-// form f_c + sum_k w_k (f_k - f_c) over the npts rows from r0+d+i, the same
+// stencil window in registers: a ring of kRing blocks holds rows of the
+// ORIGINAL field from r0+d on (d = the line's signed tap-0 offset); the loads
+// of the block kRing-1 ahead are issued before the current block's stores,
+// so kRing-2 blocks of loads are always in flight; an L2 prefetch runs
+// kPrefetch blocks further ahead, so that those loads find their rows in L2
+// (the registers bound the bytes in flight, and with them the HBM rate at
+// DRAM latency). Output row r0+i is the incremental form
+// f_c + sum_k w_k (f_k - f_c) over the npts rows from r0+d+i, the same
 // operations in the same order as the staged kernels (identical bits).
 //
 // In place: inside its segment a lane reads every row before it overwrites
-// it (loads at block r0 reach rows >= r0 + d + 24 >= r0 when d >= -24, and a
+// it (loads at block r0 reach rows >= r0 + d + 8 (kRing-1) >= r0 when d >= -24, and a
 // lane's loads are ordered before its later stores). Rows outside the
 // segment belong to other warps, which overwrite them: before any store,
 // each warp saves in shared memory the first d+npts-1 rows of its segment
@@ -40,6 +41,10 @@ namespace bkma {
 namespace {
 
 constexpr int kU = 8;         // output rows per block
+// register ring of kRing blocks: kRing - 1 blocks of loads ahead (batched
+// workload: 4 blocks 727, 5 blocks 735, 6 blocks 730, 8 blocks 666 GCells/s;
+// up to 8 blocks the kernel keeps two CTAs per SM)
+constexpr int kRing = 5;
 constexpr int kWarps = 8;     // warps per CTA
 constexpr int kSeamRows = kStreamSeam + kStreamBack;
 constexpr int kPitch = 32;    // shared-memory row pitch (floats) of a warp's seams
@@ -107,22 +112,23 @@ __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group
         if (j < a) return below[(kStreamSeam + (j - a) - d) * kPitch + lane];
         return src[(int64_t)j * n2];
     };
-    // Ring of 4 blocks of kU rows: slot (t % 4) holds rows r0(t)+d .. +kU-1
-    // of block t. At block t the loads of block t+3 are issued (into the
-    // slot block t-1 used), and block t's outputs read slots t and t+1, so
-    // two blocks of loads stay in flight behind the one being computed.
-    // rows the steady-state prefetch would have covered before the first block
-    for (int j = max(a, a + d + 3 * kU); j < min(b, a + d + (3 + kPrefetch) * kU); ++j)
+    // Ring of kRing blocks of kU rows: slot (t % kRing) holds rows r0(t)+d ..
+    // +kU-1 of block t. At block t the loads of block t+kRing-1 are issued
+    // (into the slot block t-1 used), and block t's outputs read slots t and
+    // t+1, so kRing-2 blocks of loads stay in flight behind the one being
+    // computed. Before the first block: the rows the steady-state prefetch
+    // would have covered.
+    for (int j = max(a, a + d + (kRing - 1) * kU); j < min(b, a + d + (kRing - 1 + kPrefetch) * kU); ++j)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(src + (int64_t)j * n2));
-    float B[4 * kU];
+    float B[kRing * kU];
 #pragma unroll
-    for (int i = 0; i < 3 * kU; ++i) B[i] = ld(a + d + i);
-    const float *pn = src + (int64_t)(a + d + 3 * kU) * n2;  // first row of block t+3
+    for (int i = 0; i < (kRing - 1) * kU; ++i) B[i] = ld(a + d + i);
+    const float *pn = src + (int64_t)(a + d + (kRing - 1) * kU) * n2;  // first row of block t+kRing-1
     float *po = dst + (int64_t)a * n2;
     auto block = [&](auto ph_c, int r0) {
-        constexpr int ph = decltype(ph_c)::value;  // t % 4
-        constexpr int ld_slot = (ph + 3) % 4;
-        const int j0 = r0 + d + 3 * kU;
+        constexpr int ph = decltype(ph_c)::value;  // t % kRing
+        constexpr int ld_slot = (ph + kRing - 1) % kRing;
+        const int j0 = r0 + d + (kRing - 1) * kU;
         {  // L2 prefetch of the rows kPrefetch blocks beyond this load
             const int jp = j0 + kPrefetch * kU;
             if (jp >= a && jp + kU <= b) {
@@ -147,17 +153,17 @@ __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group
 #pragma unroll
         for (int i = 0; i < kU; ++i) {
             if (i < nr) {
-                const float fc = B[(ph * kU + i + C) % (4 * kU)];
+                const float fc = B[(ph * kU + i + C) % (kRing * kU)];
                 float acc = 0.f;
 #pragma unroll
                 for (int k = 0; k < NT; ++k)
-                    if (k != C) acc = fmaf(w[k], B[(ph * kU + i + k) % (4 * kU)] - fc, acc);
+                    if (k != C) acc = fmaf(w[k], B[(ph * kU + i + k) % (kRing * kU)] - fc, acc);
                 *po = fc + acc;
             }
             po += n2;
         }
     };
-    for (int r0 = a; r0 < b; r0 += 4 * kU) {
+    for (int r0 = a; r0 < b; r0 += kRing * kU) {
         block(std::integral_constant<int, 0>{}, r0);
         if (r0 + kU >= b) break;
         block(std::integral_constant<int, 1>{}, r0 + kU);
@@ -165,6 +171,22 @@ __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group
         block(std::integral_constant<int, 2>{}, r0 + 2 * kU);
         if (r0 + 3 * kU >= b) break;
         block(std::integral_constant<int, 3>{}, r0 + 3 * kU);
+        if constexpr (kRing > 4) {
+            if (r0 + 4 * kU >= b) break;
+            block(std::integral_constant<int, 4 % kRing>{}, r0 + 4 * kU);
+        }
+        if constexpr (kRing > 5) {
+            if (r0 + 5 * kU >= b) break;
+            block(std::integral_constant<int, 5 % kRing>{}, r0 + 5 * kU);
+        }
+        if constexpr (kRing > 6) {
+            if (r0 + 6 * kU >= b) break;
+            block(std::integral_constant<int, 6 % kRing>{}, r0 + 6 * kU);
+        }
+        if constexpr (kRing > 7) {
+            if (r0 + 7 * kU >= b) break;
+            block(std::integral_constant<int, 7 % kRing>{}, r0 + 7 * kU);
+        }
     }
 }
 

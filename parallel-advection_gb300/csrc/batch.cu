@@ -88,6 +88,8 @@ struct BatchImpl {
     size_t cap = 48 * 1024;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t cs = nullptr;
+    cudaStream_t par[2] = {nullptr, nullptr};  // capture branches of the streamed launches
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
 
     void free_lists() {
         cudaFree(d_fields);
@@ -100,6 +102,11 @@ struct BatchImpl {
     ~BatchImpl() {
         if (exec) cudaGraphExecDestroy(exec);
         if (cs) cudaStreamDestroy(cs);
+        for (auto &q : par)
+            if (q) cudaStreamDestroy(q);
+        if (fork) cudaEventDestroy(fork);
+        for (auto &e : join)
+            if (e) cudaEventDestroy(e);
         free_lists();
         cudaFree(d_counter);
         for (auto *p : plans) bkma_adv_plan_destroy(p);
@@ -226,21 +233,39 @@ bkma_status build_batch(BatchImpl &b, cudaStream_t st) {
         b.exec = nullptr;
     }
     if (!b.cs) BKMA_CUDA_TRY(cudaStreamCreateWithFlags(&b.cs, cudaStreamNonBlocking));
+    for (auto &q : b.par)
+        if (!q) BKMA_CUDA_TRY(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+    if (!b.fork) BKMA_CUDA_TRY(cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming));
+    for (auto &e : b.join)
+        if (!e) BKMA_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     (void)st;
     cudaGraph_t g = nullptr;
     b.launches = 0;
+    // the launches touch disjoint lines: capture them as parallel branches,
+    // so the last wave of one overlaps the others
     BKMA_CUDA_TRY(cudaStreamBeginCapture(b.cs, cudaStreamCaptureModeThreadLocal));
+    cudaEventRecord(b.fork, b.cs);
+    for (auto &q : b.par) cudaStreamWaitEvent(q, b.fork, 0);
+    cudaStream_t branch[3] = {b.cs, b.par[0], b.par[1]};
+    int nb = 0;
     if (b.ntiles > 0) {
-        cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), b.cs);
-        kern<<<b.grid, b.threads, b.smem, b.cs>>>((const BatchFieldDev<T> *)b.d_fields,
-                                                 b.nstaged, b.ntiles, b.d_counter);
+        cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), branch[nb]);
+        kern<<<b.grid, b.threads, b.smem, branch[nb]>>>((const BatchFieldDev<T> *)b.d_fields,
+                                                       b.nstaged, b.ntiles, b.d_counter);
         ++b.launches;
+        ++nb;
     }
     const int npts_of[3] = {4, 6, 10};
     for (int k = 0; k < 3; ++k) {
         if (b.items[k] == 0) continue;
-        adv_stream_launch_fields(npts_of[k], b.d_stream[k], b.nstream[k], b.items[k], b.cs);
+        adv_stream_launch_fields(npts_of[k], b.d_stream[k], b.nstream[k], b.items[k],
+                                 branch[nb % 3]);
         ++b.launches;
+        ++nb;
+    }
+    for (int k = 0; k < 2; ++k) {
+        cudaEventRecord(b.join[k], b.par[k]);
+        cudaStreamWaitEvent(b.cs, b.join[k], 0);
     }
     cudaError_t e = cudaStreamEndCapture(b.cs, &g);
     if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
