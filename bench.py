@@ -56,18 +56,69 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """SM clock, power and clock-event reasons sampled during the timed
+    region: NVML (the driver's libnvidia-ml, read-only queries) every 5 ms
+    from a thread, the GPU matched by UUID; nvidia-smi every 200 ms when NVML
+    cannot be loaded."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
         self.lines = []
+        self.nv = None
+        self.samples = []
+        self.running = False
+
+    def _nvml_handle(self):
+        import ctypes as C
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = C.c_void_p()
+        uuid = None
+        try:
+            import torch
+            u = getattr(torch.cuda.get_device_properties(self.index), "uuid", None)
+            if u is not None:
+                uuid = "GPU-" + str(u) if not str(u).startswith("GPU-") else str(u)
+        except Exception:
+            uuid = None
+        ok = uuid is not None and lib.nvmlDeviceGetHandleByUUID(uuid.encode(), C.byref(h)) == 0
+        if not ok and lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(h)) != 0:
+            return None
+        return lib, h
+
+    def _poll(self):
+        import ctypes as C
+        lib, h = self.nv
+        sm, mx, pw, rs = C.c_uint(), C.c_uint(), C.c_uint(), C.c_ulonglong()
+        get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx))
+        while self.running:
+            if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(sm)) == 0 and \
+                    get_reasons(h, C.byref(rs)) == 0:
+                lib.nvmlDeviceGetPowerUsage(h, C.byref(pw))
+                self.samples.append((sm.value, mx.value, pw.value / 1000.0, rs.value))
+            time.sleep(0.005)
 
     def start(self):
+        try:
+            self.nv = self._nvml_handle()
+        except Exception:
+            self.nv = None
+        if self.nv is not None:
+            self.running = True
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
@@ -84,6 +135,21 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def stop(self):
+        if self.nv is not None:
+            self.running = False
+            self.t.join(timeout=1)
+            if not self.samples:
+                return None
+            reasons = set()
+            for _, _, _, r in self.samples:
+                for bit, name in self.REASONS.items():
+                    if r & bit:
+                        reasons.add(name)
+            return {"sm_mhz": statistics.median(x[0] for x in self.samples),
+                    "sm_max_mhz": max(x[1] for x in self.samples),
+                    "power_w": statistics.median(x[2] for x in self.samples),
+                    "samples": len(self.samples), "source": "nvml, 5 ms",
+                    "reasons": sorted(reasons)}
         if not self.proc:
             return None
         time.sleep(0.25)
@@ -107,7 +173,7 @@ class ClockSampler:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
-                "reasons": sorted(reasons)}
+                "source": "nvidia-smi, 200 ms", "reasons": sorted(reasons)}
 
 
 def dist_env():
