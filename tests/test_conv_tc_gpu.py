@@ -125,3 +125,34 @@ def test_tensor_conv_rejects_unsupported(bkma, cuda):
     assert e.value.status == 2
     with pytest.raises(bkma.BkmaError):  # 7 taps of shared-memory weights leave no stages
         bkma.Conv1dPlan(2, 128, 128, 256, 13, dtype="bf16", impl="tensor")
+
+
+@pytest.mark.parametrize("B", [640, 611])
+def test_tensor_conv_chunk_rounds_against_torch(bkma, cuda, B):
+    """Sizes with full rounds of 64-tile chunks over the CTAs plus an evenly
+    split remainder (640 and 611 rows x 16 tiles), in place: every chunk
+    boundary reads its halo from the snapshot. Reference: PyTorch's FP32
+    conv1d on the same BF16 inputs (TF32 off)."""
+    import torch
+    C, L, K = 128, 2048, 7
+    g = torch.Generator(device=cuda).manual_seed(B)
+    s = 1.0 / (C * K) ** 0.5
+    x = ((torch.rand((B, C, L), generator=g, device=cuda) * 2 - 1)).to(torch.bfloat16)
+    w = ((torch.rand((C, C, K), generator=g, device=cuda) * 2 - 1) * s).to(torch.bfloat16)
+    b = ((torch.rand((C,), generator=g, device=cuda) * 2 - 1) * s).to(torch.bfloat16)
+    prev = torch.backends.cudnn.allow_tf32
+    torch.backends.cudnn.allow_tf32 = False
+    try:
+        want = torch.nn.functional.conv1d(x.float(), w.float(), b.float())
+    finally:
+        torch.backends.cudnn.allow_tf32 = prev
+    orig_tail = x[:, :, L - K + 1:].clone()
+    plan = bkma.Conv1dPlan(B, C, C, L, K, dtype="bf16", impl="tensor")
+    plan.run(x, w, b)
+    plan.status()
+    got = x[:, :, :L - K + 1].float()
+    err = (got - want).abs()
+    scale = want.abs().max()
+    assert err.max() <= 1e-2 * scale, (err.max().item(), scale.item())
+    assert err.mean() <= 3e-3 * scale, (err.mean().item(), scale.item())
+    assert torch.equal(x[:, :, L - K + 1:], orig_tail)
