@@ -620,6 +620,8 @@ ROWS_CASES = [
     ((3, 4096, 1, 0.0007, 0.0, 1.0, -1.0, 1.0), None),
     ((5, 20, 1, 0.004, 0.0, 1.0, -3.0, 3.0), None),      # n1 not a power of two, shifts > 1 cell
     ((6, 1000, 1, 0.001, 0.0, 1.0, -2.0, 3.0), EXC_VEL),  # exception lines
+    ((70000, 16, 1, 0.001, 0.0, 1.0, -1.0, 1.0), None),   # 274 CTAs of 256 lines
+    ((600, 1024, 1, 0.001, 0.0, 1.0, -1.0, 1.0), None),   # 75 CTAs of 8 lines
 ]
 
 
@@ -641,8 +643,12 @@ def test_rows_path_bit_identical(bkma, cuda, case, vel, degree):
     staged.step(ref, nsteps=3)
     plan = _plan(bkma, p, **kw)
     assert plan.info()["path"] == 3
+    d = _to(cuda, f0, torch.float32)
+    plan.step(d, nsteps=3)  # the default R
+    plan.status()
+    assert torch.equal(d, ref)
     for R in (1, 2, 64):
-        plan.set_tile(1, min(R, p.n0), 256, 3)
+        plan.set_tile(1, max(1, min(R, p.n0, (200 * 1024) // (4 * p.n1))), 256, 3)
         d = _to(cuda, f0, torch.float32)
         plan.step(d, nsteps=3)
         plan.status()
