@@ -242,6 +242,31 @@ __device__ __forceinline__ void rows_f32x4(const float *S, float *G, int n1, int
 // One staged tile: `tc.nslab` slabs x `tc.wc` columns x all n1 rows of the
 // field `a.src` -> `a.dst` (may alias). Shared by the single-field kernel and
 // the batched persistent kernel, so both produce the same bits.
+// One cell from its npts taps p[0], p[ws], ..., p[(NT-1) ws] and weights w.
+// FP32: the incremental form f_c + sum_{k != c} w_k (f_k - f_c), whose
+// rounding scales with the small differences rather than with |f| (and the
+// same operations as the packed FP32 kernels: same bits). FP64: the direct
+// form sum_k w_k f_k, one multiply and NT - 1 FMAs instead of 2 NT - 1
+// operations; FP64 issue bounds these kernels on GB300, and FP64 rounding
+// (~1e-16 |f| per step) stays far below the stencil's own error.
+template <typename T, int NT>
+__device__ __forceinline__ T stencil_cell(const T *p, int ws, const T (&w)[NT]) {
+    constexpr int C = NT / 2 - 1;
+    if constexpr (sizeof(T) == 8) {
+        T acc = w[0] * p[0];
+#pragma unroll
+        for (int k = 1; k < NT; ++k) acc = fma(w[k], p[k * ws], acc);
+        return acc;
+    } else {
+        const T fc = p[C * ws];
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < NT; ++k)
+            if (k != C) acc = fma(w[k], p[k * ws] - fc, acc);
+        return fc + acc;
+    }
+}
+
 template <typename T, int NT>
 __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const TileCoord &tc, T *sm) {
     constexpr int C = NT / 2 - 1;  // centre tap: the left node of the foot cell
@@ -307,13 +332,7 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
                 for (int k = 0; k < NT; ++k) w[k] = ec.w[k];
             }
             if (rr >= n1) rr -= n1;
-            const T *p = S + rr * ws + c;
-            const T fc = p[C * ws];
-            T acc = T(0);
-#pragma unroll
-            for (int k = 0; k < NT; ++k)
-                if (k != C) acc = fma(w[k], p[k * ws] - fc, acc);
-            a.dst[g0 + (int64_t)r * a.n2 + c] = fc + acc;
+            a.dst[g0 + (int64_t)r * a.n2 + c] = stencil_cell<T, NT>(S + rr * ws + c, ws, w);
         }
         return;
     }
@@ -339,13 +358,7 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
             for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
                 int rr = r + base;
                 if (rr >= n1) rr -= n1;
-                const T *p = S + rr * ws + c;
-                const T fc = p[C * ws];
-                T acc = T(0);
-#pragma unroll
-                for (int k = 0; k < NT; ++k)
-                    if (k != C) acc = fma(w[k], p[k * ws] - fc, acc);
-                G[(int64_t)r * a.n2 + c] = fc + acc;
+                G[(int64_t)r * a.n2 + c] = stencil_cell<T, NT>(S + rr * ws + c, ws, w);
                 c += dc;
                 r += dr;
                 if (c >= wc) {
@@ -361,13 +374,10 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
                 const AdvExcCell<T> &e = cells[r];
                 int rr = r + e.base;
                 if (rr >= n1) rr -= n1;
-                const T *p = S + rr * ws + c;
-                const T fc = p[C * ws];
-                T acc = T(0);
+                T we[NT];
 #pragma unroll
-                for (int k = 0; k < NT; ++k)
-                    if (k != C) acc = fma(e.w[k], p[k * ws] - fc, acc);
-                G[(int64_t)r * a.n2 + c] = fc + acc;
+                for (int k = 0; k < NT; ++k) we[k] = e.w[k];
+                G[(int64_t)r * a.n2 + c] = stencil_cell<T, NT>(S + rr * ws + c, ws, we);
                 c += dc;
                 r += dr;
                 if (c >= wc) {

@@ -73,13 +73,7 @@ __global__ void __launch_bounds__(kFuseThreads) adv_fused(AdvStagedArgs<T> a, in
                     for (int k = 0; k < NT; ++k) wk[k] = e.w[k];
                 }
                 if (rr >= n1) rr -= n1;
-                const T *p = S + rr * ws + c;
-                const T fc = p[C * ws];
-                T acc = T(0);
-#pragma unroll
-                for (int k = 0; k < NT; ++k)
-                    if (k != C) acc = fma(wk[k], p[k * ws] - fc, acc);
-                v[j] = fc + acc;
+                v[j] = stencil_cell<T, NT>(S + rr * ws + c, ws, wk);
             }
         }
         __syncthreads();  // every thread has read the old strip
