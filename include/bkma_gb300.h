@@ -130,7 +130,8 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
  * are bit-identical to one step per launch; HBM traffic per cell-step falls
  * by the factor. Out of place, `data` is left unchanged. Not for the plain
  * FP64 form; BKMA_ERR_UNSUPPORTED when a strip of the plan's n1 rows does
- * not fit shared memory. No counterpart in the reference, which runs one
+ * not fit shared memory, and for FP32 lines longer than 4608 rows (the strips
+ * would hold one column: slower than one step per launch). No counterpart in the reference, which runs one
  * step per kernel (src/advection.cpp:55-59). */
 bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_launch);
 /* On-chip state of the fused steps (FP32 plans, degree 3, 5 or 9).

@@ -677,6 +677,13 @@ bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_laun
             return fail(BKMA_ERR_UNSUPPORTED, "the plain FP64 form runs one step per launch");
         if (adv_fused_tile_w(p, kMaxSmem) == 0)
             return fail(BKMA_ERR_UNSUPPORTED, "lines too long for a fused shared-memory strip");
+        // FP32 lines too long for the fast strips would run one column per
+        // CTA: 2x slower than one step per launch (64 x 8192 x 512: 315-382
+        // vs 655 GCells/s), so fusion is refused there
+        if (p.desc.dtype == BKMA_F32 && !p.fuse_x2 && !adv_fused_f32_fast(p, kMaxSmem))
+            return fail(BKMA_ERR_UNSUPPORTED,
+                        "FP32 lines longer than the fused strips hold (4608 rows): one step "
+                        "per launch is faster");
     }
     p.fuse = steps_per_launch;
     return BKMA_OK;

@@ -459,6 +459,10 @@ cudaError_t launch_fused_npts(const AdvPlanImpl &p, const void *src, void *dst, 
 
 }  // namespace
 
+bool adv_fused_f32_fast(const AdvPlanImpl &p, size_t max_smem) {
+    return fused_f32_w(p, max_smem) != 0;
+}
+
 size_t adv_fused_x2_smem(const AdvPlanImpl &p) {
     return 4 * (size_t)p.desc.n1 * 4 * sizeof(float);
 }

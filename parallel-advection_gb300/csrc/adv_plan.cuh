@@ -143,6 +143,9 @@ cudaError_t adv_stream_launch_fields(int npts, const StreamField *d_fields, int 
 // Multi-step fused form (adv_fused.cu): strip width for a plan (0 if the
 // plan's lines are too long), and one launch of k fused steps src -> dst.
 int adv_fused_tile_w(const AdvPlanImpl &p, size_t max_smem);
+// FP32 plans: whether the fast fused strips (two shared buffers, 4 or 8
+// columns) hold the plan's lines.
+bool adv_fused_f32_fast(const AdvPlanImpl &p, size_t max_smem);
 // Shared memory of the hi + lo fused kernel (four n1 x 4 FP32 buffers).
 size_t adv_fused_x2_smem(const AdvPlanImpl &p);
 cudaError_t adv_fused_launch(const AdvPlanImpl &p, const void *src, void *dst, int W, int k,

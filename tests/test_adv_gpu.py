@@ -546,6 +546,12 @@ def test_fused_steps_limits(bkma, cuda):
         _plan(bkma, long_lines, dtype="f32").set_fusion(4)
     with pytest.raises(bkma.BkmaError):
         _plan(bkma, p, dtype="f32").set_fusion(0)
+    # FP32 lines longer than the fast strips hold: refused (slower than one
+    # step per launch); FP64 keeps its one-column strips
+    mid = AdvParams(2, 8192, 4, 0.001, 0.0, 1.0, -1.0, 1.0)
+    with pytest.raises(bkma.BkmaError):
+        _plan(bkma, mid, dtype="f32").set_fusion(4)
+    _plan(bkma, mid, dtype="f64").set_fusion(4)
 
 
 @pytest.mark.parametrize("case,vel", FUSED_CASES)
