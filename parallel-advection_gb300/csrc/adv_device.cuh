@@ -269,7 +269,6 @@ __device__ __forceinline__ T stencil_cell(const T *p, int ws, const T (&w)[NT]) 
 
 template <typename T, int NT>
 __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const TileCoord &tc, T *sm) {
-    constexpr int C = NT / 2 - 1;  // centre tap: the left node of the foot cell
     // Parameters of the first line, loaded before the staging wait so their
     // latency hides behind the copies.
     const int exc0 = a.exc_index[tc.line0];

@@ -34,7 +34,6 @@ template <typename T, int NT>
 __global__ void __launch_bounds__(kFuseThreads) adv_fused(AdvStagedArgs<T> a, int ksteps) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *S = reinterpret_cast<T *>(smem_raw);
-    constexpr int C = NT / 2 - 1;
     TileCoord tc = tile_of(blockIdx.x, a.lines, a.n2, 1, a.W, a.ncb);
     if (a.line_list) tc.line0 = a.line_list[tc.line0];
     const int n1 = (int)a.n1;
