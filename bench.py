@@ -57,7 +57,7 @@ def peaks():
 
 class ClockSampler:
     """SM clock, power and clock-event reasons sampled during the timed
-    region: NVML (the driver's libnvidia-ml, read-only queries) every 5 ms
+    region: NVML (the NVIDIA driver's libnvidia-ml, read-only queries) every 5 ms
     from a thread, the GPU matched by UUID; nvidia-smi every 200 ms when NVML
     cannot be loaded."""
 

@@ -15,7 +15,7 @@ void set_error(const std::string &msg);
 bkma_status fail(bkma_status s, const std::string &msg);
 bkma_status cuda_fail(cudaError_t e, const char *what);
 // The driver's cuTensorMapEncodeTiled (a PFN_cuTensorMapEncodeTiled_v12000),
-// or null when the driver does not provide it.
+// or null when the CUDA driver does not provide it.
 void *tensor_map_encoder();
 
 #define BKMA_CUDA_TRY(expr)                                   \

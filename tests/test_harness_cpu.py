@@ -8,7 +8,7 @@ import pytest
 
 from bkma_gb300 import harness
 
-REF = "/root/reference/benchmark"
+REF = os.path.join(os.environ.get("BKMA_REFERENCE_DIR", "/root/reference"), "benchmark")
 
 
 def test_records_and_aggregates():
