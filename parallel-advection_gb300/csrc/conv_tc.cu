@@ -36,7 +36,9 @@
 //    (tcgen05.ld), add the bias and round to BF16. When the output rows are
 //    16-byte strided, each warp writes its 32 channels x 64 positions into a
 //    128-byte-swizzled shared tile (conflict-free) and one lane stores it
-//    with a TMA tensor store; otherwise lanes store their own rows.
+//    with a TMA tensor store (two tiles per warp stored together after the
+//    accumulator is released, or one tile stored per half, by shape);
+//    otherwise lanes store their own rows.
 //    The shared-memory data path is the limit of this kernel (every N = 128
 //    MMA reads a 4 KB B tile: half its bandwidth at the tensor rate), so
 //    every other access is shaped for few wavefronts.
@@ -72,7 +74,9 @@ constexpr int CHUNK_TILES = 64;            // preferred tiles per chunk
 constexpr int MAX_SLOTS = 3840;            // halo snapshot slots (chunks) per call: <= 15 MiB
 
 constexpr int EPI_TILE_BYTES = 4096;  // 32 channels x 64 positions BF16
-constexpr int EPI_BYTES = NUM_EPI_WARPS * 2 * EPI_TILE_BYTES + 1024;  // + alignment slack
+// epilogue tiles per warp: 2 (one per half item, both stored after the
+// accumulator is released) or 1 (each half stored as soon as it is staged)
+constexpr int epi_bytes(int tiles) { return NUM_EPI_WARPS * tiles * EPI_TILE_BYTES + 1024; }
 
 struct Args {
     CUtensorMap out_map;      // (lout, cout, B) view of out, 64 x 32 x 1 boxes, 128-B swizzle
@@ -95,7 +99,7 @@ struct Args {
     int nacc;        // FP32 accumulators in TMEM (1 or 2)
     int tm_cols;     // TMEM columns of the weight image: 512 - 128 * nacc
     int wsmem_bytes; // shared-memory weights, placed before the stages
-    int epi_tma;     // 1: the epilogue stores through out_map
+    int epi_tma;     // 1 or 2: the epilogue stores through out_map from 1 or 2 tiles per warp
     int epi_off;     // offset of the epilogue tiles (after the stages)
     int *status;     // device status word (0 ok, 4 timeout)
 };
@@ -538,10 +542,11 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
         const int co = threadIdx.x;
         const float bias = (a.bias && co < a.cout) ? __bfloat162float(a.bias[co]) : 0.0f;
         const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)a.tm_cols;
-        // this warp's two 4 KB swizzled output tiles (one per half item),
-        // stored by one bulk group per item
-        const uint32_t epi_tile =
-            ((smem_base + (uint32_t)a.epi_off + 1023u) & ~1023u) + (uint32_t)warp * 2u * EPI_TILE_BYTES;
+        // this warp's 4 KB swizzled output tiles: with two, one per half item,
+        // stored by one bulk group per item; with one, one bulk group per half
+        const uint32_t epi_tile = ((smem_base + (uint32_t)a.epi_off + 1023u) & ~1023u) +
+                                  (uint32_t)(warp * a.epi_tma * EPI_TILE_BYTES);
+        const bool one_tile = a.epi_tma == 1;
         const bool warp_rows = 32 * warp < a.cout;
         int it = 0;
         BKMA_TC_FOR_ITEMS {
@@ -558,7 +563,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             const int64_t lt = a.lout & ~(int64_t)7;
             const bool tma_rows = a.epi_tma && warp_rows;
             // both tiles of this warp are free once the previous item's stores read them
-            if (tma_rows) {
+            if (tma_rows && !one_tile) {
                 if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
                 __syncwarp();
             }
@@ -593,8 +598,12 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
                                     (uint16_t)((pk[e / 2] >> (16 * (e & 1))) & 0xFFFFu));
                     }
                     if (lh >= lt) continue;
-                    const uint32_t row_addr =
-                        epi_tile + (uint32_t)half * EPI_TILE_BYTES + (uint32_t)lane * 128u;
+                    if (one_tile) {  // the tile is free once its last store read it
+                        if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                        __syncwarp();
+                    }
+                    const uint32_t tile_addr = epi_tile + (one_tile ? 0u : (uint32_t)half * EPI_TILE_BYTES);
+                    const uint32_t row_addr = tile_addr + (uint32_t)lane * 128u;
 #pragma unroll
                     for (int e = 0; e < 8; ++e)
                         asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(
@@ -602,6 +611,18 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
                                      "r"(pk[4 * e]), "r"(pk[4 * e + 1]), "r"(pk[4 * e + 2]),
                                      "r"(pk[4 * e + 3])
                                      : "memory");
+                    if (one_tile) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        __syncwarp();
+                        if (lane == 0) {
+                            asm volatile(
+                                "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, "
+                                "%3, %4}], [%1];" ::"l"(reinterpret_cast<uint64_t>(&a.out_map)),
+                                "r"(tile_addr), "r"((int)lh), "r"(32 * warp), "r"(b)
+                                : "memory");
+                            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                        }
+                    }
                 } else if (co < a.cout) {
                     if (lh + 64 <= a.lout && (a.out_stride % 8) == 0) {
                         uint4 *d4 = reinterpret_cast<uint4 *>(dst);
@@ -617,7 +638,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
                     }
                 }
             }
-            if (tma_rows) {
+            if (tma_rows && !one_tile) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) {
@@ -667,8 +688,13 @@ struct TcLayout {
     size_t smem;
 };
 
-// On-chip layout of one launch. epi_tma asks for the tensor-store epilogue;
-// it is granted when at least 3 activation stages still fit beside its tiles.
+// On-chip layout of one launch. epi_tma asks for the tensor-store epilogue:
+// two tiles per warp when an item has more than 40 MMAs (stores after the
+// accumulator is released: K = 7 at Cin = 128 1453 vs 1404 TFLOP/s, K = 11 at
+// Cin = 96 1093 vs 965), one tile per warp below that (each half stored at
+// once: K = 1/3/5 +11/13/14 %) or when two tiles leave fewer than 3
+// activation stages (K = 9 at Cin = 128: 1605 vs 1222 with per-lane stores);
+// none when even one tile leaves fewer than 3.
 TcLayout tc_layout(const bkma_conv_desc &d, bool epi_tma = false) {
     TcLayout t;
     const int cin = (int)d.cin, K = (int)d.ksize;
@@ -686,14 +712,20 @@ TcLayout tc_layout(const bkma_conv_desc &d, bool epi_tma = false) {
     t.stages = std::min(tc::STAGES_MAX, avail / t.stage_bytes);
     t.epi_tma = 0;
     if (epi_tma) {
-        const int st_epi = std::min(tc::STAGES_MAX, (avail - tc::EPI_BYTES) / t.stage_bytes);
-        if (avail > tc::EPI_BYTES && st_epi >= 3) {
-            t.stages = st_epi;
-            t.epi_tma = 1;
+        const int mmas = K * cin / 16;
+        for (int tiles : {2, 1}) {
+            if (tiles == 2 && mmas <= 40) continue;
+            const int bytes = tc::epi_bytes(tiles);
+            const int st_epi = std::min(tc::STAGES_MAX, (avail - bytes) / t.stage_bytes);
+            if (avail > bytes && st_epi >= 3) {
+                t.stages = st_epi;
+                t.epi_tma = tiles;
+                break;
+            }
         }
     }
     t.epi_off = t.wsmem_bytes + t.stages * t.stage_bytes;
-    t.smem = (size_t)t.epi_off + (t.epi_tma ? tc::EPI_BYTES : 0);
+    t.smem = (size_t)t.epi_off + (t.epi_tma ? tc::epi_bytes(t.epi_tma) : 0);
     return t;
 }
 
