@@ -1,15 +1,20 @@
-// advection [file.ini] [--fp32]: the reference's advection driver
+// advection [file.ini] [--fp32] [--fused K] [--hi-lo]: the reference's advection driver
 // (src/advection.cpp:14-71) over the C ABI. Same .ini keys, same printed
 // blocks (runtime parameters, RESULTS_VALIDATION, PERF_DIAGS).
 //
 // kernelImpl selects the strategy like impl_selector: NDRange / AdaptiveWg /
 // GB300 run in place, BasicRange out of place into a second buffer (the
 // reference's global scratch), Plain runs the per-cell FP64 reference math.
-// The field is FP64 like the reference unless --fp32 is given.
+// The field is FP64 like the reference unless --fp32 is given. --fused K
+// runs K time steps per kernel launch on shared-memory strips (same bits, one
+// call for all maxIter steps instead of a wait after each); --hi-lo (FP32,
+// with --fused) keeps each cell as an FP32 hi + lo pair between the steps of
+// a launch, rounding to FP32 once per launch.
 #include <cuda_runtime.h>
 
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <iostream>
 #include <stdexcept>
@@ -34,11 +39,15 @@ static void cuda_check(cudaError_t e, const char *what) {
 int main(int argc, char **argv) {
     try {
         std::string input_file = "advection.ini";
-        bool fp32 = false;
+        bool fp32 = false, hi_lo = false;
+        int fused = 1;
         for (int i = 1; i < argc; ++i) {
             if (std::strcmp(argv[i], "--fp32") == 0) fp32 = true;
+            else if (std::strcmp(argv[i], "--hi-lo") == 0) hi_lo = true;
+            else if (std::strcmp(argv[i], "--fused") == 0 && i + 1 < argc) fused = std::atoi(argv[++i]);
             else input_file = argv[i];
         }
+        if (fused < 1) throw std::invalid_argument("--fused needs K >= 1");
         ConfigMap cm(input_file);
         AdvParams p;
         p.setup(cm);
@@ -72,11 +81,18 @@ int main(int argc, char **argv) {
         d.maxVx = p.maxRealVx;
         bkma_adv_plan *plan = nullptr;
         check(bkma_adv_plan_create(&d, &plan));
+        if (hi_lo) check(bkma_adv_plan_set_fused_state(plan, BKMA_FUSED_F32X2));
+        if (fused > 1) check(bkma_adv_plan_set_fusion(plan, fused));
         check(bkma_adv_fill(plan, data, 0, 0.0, 0, nullptr));  // fill_buffer_adv
         cuda_check(cudaDeviceSynchronize(), "fill");
 
         const auto start = std::chrono::high_resolution_clock::now();
-        for (size_t t = 0; t < p.maxIter; ++t) {
+        if (fused > 1) {  // every step in one call, K per launch
+            check(bkma_adv_step(plan, data, inplace ? nullptr : scratch, (int32_t)p.maxIter, nullptr));
+            if (!inplace && p.maxIter > 0) std::swap(data, scratch);
+            cuda_check(cudaDeviceSynchronize(), "steps");
+        }
+        for (size_t t = 0; fused == 1 && t < p.maxIter; ++t) {
             if (inplace) {
                 check(bkma_adv_step(plan, data, nullptr, 1, nullptr));
             } else {

@@ -50,6 +50,26 @@ def test_advection_driver(apps, tmp_path, impl, extra):
     assert "PERF_DIAGS:" in r.stdout and "upd_cells_per_sec" in r.stdout
 
 
+def _l1(apps, tmp_path, impl, extra):
+    ini = tmp_path / "adv.ini"
+    ini.write_text(ADV_INI.format(impl=impl))
+    r = subprocess.run([apps["advection"], str(ini)] + extra, capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    return re.search(r"Highest L1 error found: (\S+) \(lowest is (\S+)\)", r.stdout).groups()
+
+
+@pytest.mark.parametrize("impl,extra", [("AdaptiveWg", ["--fp32"]), ("AdaptiveWg", []),
+                                        ("BasicRange", ["--fp32"])])
+def test_advection_driver_fused_same_result(apps, tmp_path, impl, extra):
+    """--fused K gives the bits of one step per launch, so the printed
+    validation errors are the same; --hi-lo stays within the check."""
+    assert _l1(apps, tmp_path, impl, extra + ["--fused", "4"]) == _l1(apps, tmp_path, impl, extra)
+    if "--fp32" in extra:
+        hi, _ = _l1(apps, tmp_path, impl, extra + ["--fused", "10", "--hi-lo"])
+        assert float(hi) < 1e-6
+
+
 def test_advection_driver_unknown_impl(apps, tmp_path):
     ini = tmp_path / "adv.ini"
     ini.write_text(ADV_INI.format(impl="Hierarchical"))
