@@ -1,0 +1,105 @@
+"""Seeded random shapes through the default plans.
+
+Advection: each plan's own kernel choice (TMA tiles, streamed columns,
+contiguous lines, staged whole rows) against the generic staged kernel on
+the same field: identical bits after three steps, in place; fields small
+enough for the oracle also stay within the FP32 bound of the FP64 oracle.
+Conv1d (tensor path, BF16): random batch, channels, length and kernel size
+against PyTorch's FP32 conv1d on the same BF16 inputs (TF32 off), in place
+and out of place."""
+import numpy as np
+import pytest
+
+from oracle import AdvParams
+
+pytestmark = pytest.mark.gpu
+
+
+def _adv_cases(n=24, seed=2026):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        n1 = int(rng.choice([16, 20, 64, 100, 256, 333, 1024, 2048, 3000]))
+        n2 = int(rng.choice([1, 1, 2, 3, 4, 7, 8, 13, 16, 32, 37, 64, 100]))
+        n0 = int(rng.integers(1, max(2, min(64, 400000 // (n1 * n2)) + 1)))
+        deg = int(rng.choice([3, 5, 9]))
+        vmax = float(rng.choice([0.5, 1.0, 3.0, 20.0]))
+        dt = float(rng.choice([1e-4, 1e-3, 4e-3]))
+        out.append((n0, n1, n2, deg, vmax, dt))
+    return out
+
+
+@pytest.mark.parametrize("case", _adv_cases())
+def test_fuzz_advection_paths_agree(bkma, cuda, oracle, case):
+    import torch
+    n0, n1, n2, deg, vmax, dt = case
+    p = AdvParams(n0, n1, n2, dt, 0.0, 1.0, -vmax, vmax)
+    kw = dict(dtype="f32", degree=deg, weights="reference" if deg == 5 else "lagrange",
+              dt=dt, minX=0.0, maxX=1.0, minVx=-vmax, maxVx=vmax)
+    rng = np.random.default_rng(n0 * 7919 + n1 * 31 + n2)
+    x = np.arange(n1) / n1
+    f0 = (np.sin(2 * np.pi * x)[None, :, None]
+          + 0.01 * rng.uniform(-1, 1, (n0, n1, n2))).astype(np.float32)
+    auto = bkma.AdvectionPlan(n0, n1, n2, **kw)
+    staged = bkma.AdvectionPlan(n0, n1, n2, **kw)
+    staged.set_tile(min(16, n2), 1, 256, 0)
+    a = torch.tensor(f0, device=cuda)
+    s = torch.tensor(f0, device=cuda)
+    auto.step(a, nsteps=3)
+    staged.step(s, nsteps=3)
+    auto.status()
+    staged.status()
+    assert torch.equal(a, s), auto.info()
+    if n0 * n1 * n2 <= 200000:
+        want = oracle.adv_step(p, f0.astype(np.float64), 3, degree=deg, ref_weights=deg == 5)
+        err = np.abs(a.cpu().numpy().astype(np.float64) - want).max() / np.abs(want).max()
+        assert err <= 3e-7 * 3 + 2e-7 + (1e-6 if deg == 9 else 0.0), (err, auto.info())
+
+
+def _conv_cases(n=10, seed=77):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        c = int(rng.choice([16, 32, 48, 64, 96, 128]))
+        k = int(rng.integers(1, 10))
+        length = int(8 * rng.integers(max(2, (k + 7) // 8 + 1), 400))
+        b = int(rng.integers(1, 9))
+        out.append((b, c, length, k, bool(rng.integers(0, 2))))
+    return out
+
+
+@pytest.mark.parametrize("case", _conv_cases())
+def test_fuzz_tensor_conv_against_torch(bkma, cuda, case):
+    import torch
+    B, C, L, K, inplace = case
+    g = torch.Generator(device=cuda).manual_seed(B * 1000 + C * 10 + K)
+    s = 1.0 / (C * K) ** 0.5
+    x = (torch.rand((B, C, L), generator=g, device=cuda) * 2 - 1).to(torch.bfloat16)
+    w = ((torch.rand((C, C, K), generator=g, device=cuda) * 2 - 1) * s).to(torch.bfloat16)
+    b = ((torch.rand((C,), generator=g, device=cuda) * 2 - 1) * s).to(torch.bfloat16)
+    prev = torch.backends.cudnn.allow_tf32
+    torch.backends.cudnn.allow_tf32 = False
+    try:
+        want = torch.nn.functional.conv1d(x.float(), w.float(), b.float())
+    finally:
+        torch.backends.cudnn.allow_tf32 = prev
+    try:
+        plan = bkma.Conv1dPlan(B, C, C, L, K, dtype="bf16", impl="tensor", inplace=inplace)
+    except bkma.BkmaError as e:  # shapes the tensor path does not take
+        assert e.status == 2
+        pytest.skip(str(e))
+    if inplace:
+        tail = x[:, :, L - K + 1:].clone()
+        plan.run(x, w, b)
+        plan.status()
+        got = x[:, :, :L - K + 1].float()
+        assert torch.equal(x[:, :, L - K + 1:], tail)
+    else:
+        out = torch.empty((B, C, L - K + 1), dtype=torch.bfloat16, device=cuda)
+        plan.run(x, w, b, out=out)
+        plan.status()
+        got = out.float()
+    err = (got - want).abs()
+    scale = want.abs().max()
+    assert err.max() <= 1e-2 * scale, (err.max().item(), scale.item())
+    assert err.mean() <= 3e-3 * scale
