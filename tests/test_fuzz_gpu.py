@@ -3,7 +3,8 @@
 Advection: each plan's own kernel choice (TMA tiles, streamed columns,
 contiguous lines, staged whole rows) against the generic staged kernel on
 the same field: identical bits after three steps, in place; fields small
-enough for the oracle also stay within the FP32 bound of the FP64 oracle.
+enough for the oracle also stay within the FP32 bound of the FP64 oracle;
+degree-5 FP64 plans stay within 1e-11 max|f| of the plain FP64 form.
 Conv1d (tensor path, BF16): random batch, channels, length and kernel size
 against PyTorch's FP32 conv1d on the same BF16 inputs (TF32 off), in place
 and out of place."""
@@ -54,6 +55,15 @@ def test_fuzz_advection_paths_agree(bkma, cuda, oracle, case):
         want = oracle.adv_step(p, f0.astype(np.float64), 3, degree=deg, ref_weights=deg == 5)
         err = np.abs(a.cpu().numpy().astype(np.float64) - want).max() / np.abs(want).max()
         assert err <= 3e-7 * 3 + 2e-7 + (1e-6 if deg == 9 else 0.0), (err, auto.info())
+    if deg == 5:
+        # FP64: the default plan (direct stencil sum) against the plain form
+        # (the reference's per-cell arithmetic, bit-exact with the oracle)
+        kw64 = dict(kw, dtype="f64")
+        d = torch.tensor(f0.astype(np.float64), device=cuda)
+        r = d.clone()
+        bkma.AdvectionPlan(n0, n1, n2, **kw64).step(d, nsteps=3)
+        bkma.AdvectionPlan(n0, n1, n2, impl="plain", **kw64).step(r, nsteps=3)
+        assert ((d - r).abs().max() <= 1e-11 * r.abs().max()).item()
 
 
 def _conv_cases(n=10, seed=77):
