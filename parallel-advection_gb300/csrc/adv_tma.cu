@@ -164,8 +164,8 @@ void *tensor_map_encoder() { return reinterpret_cast<void *>(encode_fn()); }
 namespace {
 
 template <int NT, int WC>
-cudaError_t launch_tma_t(const AdvPlanImpl &p, const CUtensorMap &tm, const AdvTmaArgs &a,
-                         int threads, size_t smem, int64_t grid, cudaStream_t st) {
+cudaError_t launch_tma_t(const CUtensorMap &tm, const AdvTmaArgs &a, int threads, size_t smem,
+                         int64_t grid, cudaStream_t st) {
     auto kern = adv_tma_f32<NT, WC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -231,13 +231,13 @@ cudaError_t adv_tma_launch(AdvPlanImpl &p, const void *src, void *dst, int W, in
     const size_t smem = adv_tma_smem(p, W);
     const int64_t grid = p.lines * a.ncb;
     if (p.npts == 6) {
-        if (W == 16) return launch_tma_t<6, 16>(p, *tm, a, threads, smem, grid, st);
-        if (W == 8) return launch_tma_t<6, 8>(p, *tm, a, threads, smem, grid, st);
-        return launch_tma_t<6, 32>(p, *tm, a, threads, smem, grid, st);
+        if (W == 16) return launch_tma_t<6, 16>(*tm, a, threads, smem, grid, st);
+        if (W == 8) return launch_tma_t<6, 8>(*tm, a, threads, smem, grid, st);
+        return launch_tma_t<6, 32>(*tm, a, threads, smem, grid, st);
     }
-    if (W == 16) return launch_tma_t<4, 16>(p, *tm, a, threads, smem, grid, st);
-    if (W == 8) return launch_tma_t<4, 8>(p, *tm, a, threads, smem, grid, st);
-    return launch_tma_t<4, 32>(p, *tm, a, threads, smem, grid, st);
+    if (W == 16) return launch_tma_t<4, 16>(*tm, a, threads, smem, grid, st);
+    if (W == 8) return launch_tma_t<4, 8>(*tm, a, threads, smem, grid, st);
+    return launch_tma_t<4, 32>(*tm, a, threads, smem, grid, st);
 }
 
 }  // namespace bkma
