@@ -113,3 +113,69 @@ def test_fuzz_tensor_conv_against_torch(bkma, cuda, case):
     scale = want.abs().max()
     assert err.max() <= 1e-2 * scale, (err.max().item(), scale.item())
     assert err.mean() <= 3e-3 * scale
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_fuzz_batch_equals_single_plans(bkma, cuda, seed):
+    """A random uneven batch (streamed, staged and exception-line fields of
+    degree 3 and 5, n2 from 1 up) gives, after the batch autotuner, the bits
+    of every field advanced alone by its own plan."""
+    import torch
+    rng = np.random.default_rng(seed)
+    fields, singles = [], []
+    for _ in range(int(rng.integers(3, 9))):
+        n0 = int(rng.integers(1, 40))
+        n1 = int(rng.choice([64, 100, 256, 512, 1024, 2048]))
+        n2 = int(rng.integers(1, 80))
+        deg = int(rng.choice([3, 5]))
+        vel = rng.uniform(-3.0, 3.0, n0)
+        if rng.integers(0, 3) == 0:  # a few lines with shifts of whole cells
+            vel[: max(1, n0 // 4)] = np.round(vel[: max(1, n0 // 4)])
+        f0 = (rng.uniform(-1, 1, (n0, n1, n2))).astype(np.float32)
+        kw = dict(degree=deg, weights="reference" if deg == 5 else "lagrange", dt=1.0 / n1,
+                  minX=0.0, maxX=1.0, minVx=-3.0, maxVx=3.0, velocity=vel)
+        fields.append(dict(data=torch.tensor(f0, device=cuda), **kw))
+        singles.append((torch.tensor(f0, device=cuda), kw))
+    batch = bkma.AdvectionBatch(fields, dtype="f32")
+    batch.autotune()
+    for f, (s, _) in zip(fields, singles):  # the autotuner steps the fields: reset
+        f["data"].copy_(s)
+    batch.step(3)
+    torch.cuda.synchronize()
+    for f, (s, kw) in zip(fields, singles):
+        n0, n1, n2 = s.shape
+        bkma.AdvectionPlan(n0, n1, n2, dtype="f32", **kw).step(s, nsteps=3)
+        assert torch.equal(f["data"], s)
+
+
+@pytest.mark.parametrize("case", _adv_cases(n=8, seed=4040))
+def test_fuzz_fused_steps(bkma, cuda, case):
+    """Random shapes: k fused steps per launch give the bits of one step per
+    launch, and the hi + lo state at one step per launch gives the FP32 bits."""
+    import torch
+    n0, n1, n2, deg, vmax, dt = case
+    kw = dict(dtype="f32", degree=deg, weights="reference" if deg == 5 else "lagrange",
+              dt=dt, minX=0.0, maxX=1.0, minVx=-vmax, maxVx=vmax)
+    rng = np.random.default_rng(n0 + n1 + n2)
+    f0 = rng.uniform(-1, 1, (n0, n1, n2)).astype(np.float32)
+    ref = torch.tensor(f0, device=cuda)
+    bkma.AdvectionPlan(n0, n1, n2, **kw).step(ref, nsteps=5)
+    fz = bkma.AdvectionPlan(n0, n1, n2, **kw)
+    try:
+        fz.set_fusion(3)
+    except bkma.BkmaError:  # lines the fused strips cannot hold
+        pytest.skip("no fused strip for this shape")
+    d = torch.tensor(f0, device=cuda)
+    fz.step(d, nsteps=5)
+    fz.status()
+    assert torch.equal(d, ref)
+    x2 = bkma.AdvectionPlan(n0, n1, n2, **kw)
+    try:
+        x2.set_fused_state("f32x2")
+    except bkma.BkmaError:
+        return
+    x2.set_fusion(2)
+    e = torch.tensor(f0, device=cuda)
+    for _ in range(5):
+        x2.step(e, nsteps=1)
+    assert torch.equal(e, ref)
