@@ -49,9 +49,10 @@ constexpr int kWarps = 8;     // warps per CTA
 constexpr int kSeamRows = kStreamSeam + kStreamBack;
 constexpr int kPitch = 32;    // shared-memory row pitch (floats) of a warp's seams
 // L2 prefetch distance in blocks beyond the register ring's loads (batched
-// workload: 681 GCells/s without, 702 at 4, 716 at 8, 665 at 12, 643 at 16;
-// 727 with the start-of-segment burst)
-constexpr int kPrefetch = 8;
+// workload, 4-block ring: 681 GCells/s without, 702 at 4, 716 at 8, 665 at
+// 12, 643 at 16, 727 at 8 with the start-of-segment burst; 5-block ring: 744
+// at 6, 738 at 8, 729 at 10)
+constexpr int kPrefetch = 6;
 
 template <int NT>
 __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group, int seg,
