@@ -40,7 +40,9 @@ typedef enum bkma_status {
     BKMA_ERR_UNSUPPORTED = 2, /* reference: std::runtime_error (impl_selector.hpp:44-47) */
     BKMA_ERR_CUDA = 3,        /* a CUDA runtime error (message holds cudaGetErrorString) */
     BKMA_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
-    BKMA_ERR_NO_DEVICE = 5    /* no CUDA device visible */
+    BKMA_ERR_NO_DEVICE = 5,   /* no CUDA device visible */
+    BKMA_ERR_HOST = 6         /* a host-side failure (out of host memory): no C++ exception
+                                 ever leaves an entry point */
 } bkma_status;
 
 typedef enum bkma_dtype { BKMA_F32 = 0, BKMA_F64 = 1, BKMA_BF16 = 2 } bkma_dtype;

@@ -14,7 +14,8 @@ LIB_PATH = _build.LIB
 
 BKMA_OK = 0
 STATUS_NAMES = {0: "BKMA_OK", 1: "BKMA_ERR_INVALID_ARG", 2: "BKMA_ERR_UNSUPPORTED",
-                3: "BKMA_ERR_CUDA", 4: "BKMA_ERR_TIMEOUT", 5: "BKMA_ERR_NO_DEVICE"}
+                3: "BKMA_ERR_CUDA", 4: "BKMA_ERR_TIMEOUT", 5: "BKMA_ERR_NO_DEVICE",
+                6: "BKMA_ERR_HOST"}
 
 BKMA_F32, BKMA_F64, BKMA_BF16 = 0, 1, 2
 BKMA_ADV_AUTO, BKMA_ADV_STAGED, BKMA_ADV_PLAIN = 0, 1, 2

@@ -32,8 +32,10 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -424,8 +426,15 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
         work(0, p.lines);
     } else {
         std::vector<std::thread> pool;
-        for (int t = 0; t < nthr; ++t)
-            pool.emplace_back(work, p.lines * t / nthr, p.lines * (t + 1) / nthr);
+        pool.reserve((size_t)nthr);
+        int started = 0;
+        try {
+            for (; started < nthr; ++started)
+                pool.emplace_back(work, p.lines * started / nthr, p.lines * (started + 1) / nthr);
+        } catch (const std::system_error &) {
+            // a thread that could not start: its share and the rest run here
+        }
+        for (int t = started; t < nthr; ++t) work(p.lines * t / nthr, p.lines * (t + 1) / nthr);
         for (auto &th : pool) th.join();
     }
     for (int64_t l = 0; l < p.lines; ++l)
@@ -525,12 +534,18 @@ using namespace bkma;
 
 extern "C" {
 
-bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan) {
+bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan) try {
     BKMA_CHECK_ARG(desc && plan, "bkma_adv_plan_create: null argument");
     *plan = nullptr;
     const bkma_adv_desc &d = *desc;
     BKMA_CHECK_ARG(d.n0 > 0 && d.n1 > 0 && d.n2 > 0, "n0, n1, n2 must be positive");
     BKMA_CHECK_ARG(d.n1 < (1 << 24) && d.n2 < (1 << 24), "n1 and n2 must be < 2^24");
+    // the velocity index i0 is an int in AdvectionSolver::coord
+    // (src/solvers/AdvectionSolver.hpp:24); 2^50 cells keep every size product
+    // far from int64 overflow
+    BKMA_CHECK_ARG(d.n0 < (int64_t(1) << 31), "n0 must be < 2^31");
+    BKMA_CHECK_ARG((double)d.n0 * (double)d.n1 * (double)d.n2 < 1125899906842624.0,
+                   "n0 * n1 * n2 must be < 2^50");
     BKMA_CHECK_ARG(d.i0_offset >= 0 && d.i0_offset < d.n0, "i0_offset out of range");
     const int64_t count = d.i0_count == 0 ? d.n0 - d.i0_offset : d.i0_count;
     BKMA_CHECK_ARG(count > 0 && d.i0_offset + count <= d.n0, "i0_count out of range");
@@ -550,8 +565,8 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
     BKMA_CHECK_ARG(d.maxX > d.minX, "maxX must exceed minX");
     BKMA_CHECK_ARG(std::isfinite(d.dt), "dt must be finite");
 
-    auto *pl = new (std::nothrow) bkma_adv_plan;
-    if (!pl) return fail(BKMA_ERR_INVALID_ARG, "out of host memory");
+    // owned here until complete: an early return or an exception frees it
+    std::unique_ptr<bkma_adv_plan> pl(new bkma_adv_plan);
     AdvPlanImpl &p = pl->impl;
     p.desc = d;
     p.desc.i0_count = count;
@@ -582,14 +597,12 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
         if (e != cudaSuccess) s = cuda_fail(e, "plan tables");
     }
     if (s != BKMA_OK) {
-        delete pl;
         return s;
     }
     {
         cudaError_t e = cudaMalloc(&p.d_status, sizeof(int));
         if (e == cudaSuccess) e = cudaMemset(p.d_status, 0, sizeof(int));
         if (e != cudaSuccess) {
-            delete pl;
             return cuda_fail(e, "plan status word");
         }
     }
@@ -598,14 +611,13 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
     const bool too_long = p.path == 2 ? (p.n_exc > 0 && p.exc_tile_w(kMaxSmem) == 0)
                                       : p.smem_bytes(p.W, p.R) > kMaxSmem;
     if (too_long) {
-        delete pl;
         return fail(BKMA_ERR_UNSUPPORTED, "n1 too long for a shared-memory line tile");
     }
-    *plan = pl;
+    *plan = pl.release();
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_create")
 
-bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info *info) {
+bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info *info) try {
     BKMA_CHECK_ARG(plan && info, "null argument");
     const AdvPlanImpl &p = plan->impl;
     info->lines = p.lines;
@@ -622,9 +634,9 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
     info->tiles = p.path == 3 ? (p.lines + p.R - 1) / p.R : p.tiles(p.W, p.R);
     info->path = p.path;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_info_get")
 
-bkma_status bkma_adv_plan_status(bkma_adv_plan *plan, void *stream) {
+bkma_status bkma_adv_plan_status(bkma_adv_plan *plan, void *stream) try {
     BKMA_CHECK_ARG(plan, "null argument");
     AdvPlanImpl &p = plan->impl;
     BKMA_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
@@ -633,15 +645,15 @@ bkma_status bkma_adv_plan_status(bkma_adv_plan *plan, void *stream) {
     BKMA_CUDA_TRY(cudaMemset(p.d_status, 0, sizeof(int)));
     if (st != 0) return fail((bkma_status)st, "advection: a bounded device wait timed out");
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_status")
 
-bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *field, void *stream) {
+bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *field, void *stream) try {
     BKMA_CHECK_ARG(plan && field, "null argument");
     return adv_autotune(plan->impl, field, (cudaStream_t)stream);
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_autotune")
 
 bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
-                                   int32_t path) {
+                                   int32_t path) try {
     BKMA_CHECK_ARG(plan, "null argument");
     AdvPlanImpl &p = plan->impl;
     BKMA_CHECK_ARG(W >= 1 && W <= 1024 && R >= (path == 2 ? 0 : 1) && R <= 1024,
@@ -667,9 +679,9 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
     p.threads = threads;
     p.path = path;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_set_tile")
 
-bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_launch) {
+bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_launch) try {
     BKMA_CHECK_ARG(plan && steps_per_launch >= 1, "steps_per_launch must be >= 1");
     AdvPlanImpl &p = plan->impl;
     if (steps_per_launch > 1) {
@@ -687,9 +699,9 @@ bkma_status bkma_adv_plan_set_fusion(bkma_adv_plan *plan, int32_t steps_per_laun
     }
     p.fuse = steps_per_launch;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_set_fusion")
 
-bkma_status bkma_adv_plan_set_fused_state(bkma_adv_plan *plan, int32_t state) {
+bkma_status bkma_adv_plan_set_fused_state(bkma_adv_plan *plan, int32_t state) try {
     BKMA_CHECK_ARG(plan && (state == BKMA_FUSED_F32 || state == BKMA_FUSED_F32X2),
                    "state must be BKMA_FUSED_F32 or BKMA_FUSED_F32X2");
     AdvPlanImpl &p = plan->impl;
@@ -703,9 +715,9 @@ bkma_status bkma_adv_plan_set_fused_state(bkma_adv_plan *plan, int32_t state) {
     }
     p.fuse_x2 = state == BKMA_FUSED_F32X2 ? 1 : 0;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_set_fused_state")
 
-bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device) {
+bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights, int32_t on_device) try {
     BKMA_CHECK_ARG(plan && weights, "null argument");
     AdvPlanImpl &p = plan->impl;
     BKMA_CHECK_ARG(p.desc.weights == BKMA_W_TABLE, "plan was not created with BKMA_W_TABLE");
@@ -714,29 +726,29 @@ bkma_status bkma_adv_plan_set_weights(bkma_adv_plan *plan, const float *weights,
     BKMA_CUDA_TRY(cudaMemcpy(p.d_w, weights, bytes,
                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_set_weights")
 
-bkma_status bkma_adv_plan_line_table(const bkma_adv_plan *plan, int32_t *offsets, double *shifts) {
+bkma_status bkma_adv_plan_line_table(const bkma_adv_plan *plan, int32_t *offsets, double *shifts) try {
     BKMA_CHECK_ARG(plan, "null argument");
     const AdvPlanImpl &p = plan->impl;
     if (offsets) std::memcpy(offsets, p.base.data(), sizeof(int32_t) * (size_t)p.lines);
     if (shifts) std::memcpy(shifts, p.shift.data(), sizeof(double) * (size_t)p.lines);
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_line_table")
 
-bkma_status bkma_adv_plan_destroy(bkma_adv_plan *plan) {
+bkma_status bkma_adv_plan_destroy(bkma_adv_plan *plan) try {
     delete plan;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_plan_destroy")
 
-bkma_status bkma_adv_step(bkma_adv_plan *plan, void *data, void *out, int32_t nsteps, void *stream) {
+bkma_status bkma_adv_step(bkma_adv_plan *plan, void *data, void *out, int32_t nsteps, void *stream) try {
     BKMA_CHECK_ARG(plan && data, "bkma_adv_step: null argument");
     BKMA_CHECK_ARG(nsteps >= 0, "nsteps must be >= 0");
     AdvPlanImpl &p = plan->impl;
     return adv_launch(p, data, out, nsteps, (cudaStream_t)stream);
-}
+} BKMA_ABI_CATCH("bkma_adv_step")
 
-bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nsteps, void *stream) {
+bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nsteps, void *stream) try {
     BKMA_CHECK_ARG(plan && host_data, "bkma_adv_run_host: null argument");
     AdvPlanImpl &p = plan->impl;
     const size_t slab = (size_t)(p.desc.n1 * p.desc.n2) * (size_t)p.esize;
@@ -826,6 +838,6 @@ bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nste
         if (s != BKMA_OK) return s;
     }
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_run_host")
 
 }  // extern "C"

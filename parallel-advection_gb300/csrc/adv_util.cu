@@ -129,7 +129,7 @@ constexpr int kNormBlocks = 1024;
 extern "C" {
 
 bkma_status bkma_adv_fill(const bkma_adv_plan *plan, void *data, int32_t mode, double amp,
-                          uint64_t seed, void *stream) {
+                          uint64_t seed, void *stream) try {
     BKMA_CHECK_ARG(plan && data, "null argument");
     BKMA_CHECK_ARG(mode == 0 || mode == 1, "mode must be 0 or 1");
     const AdvPlanImpl &p = plan_impl(plan);
@@ -146,10 +146,10 @@ bkma_status bkma_adv_fill(const bkma_adv_plan *plan, void *data, int32_t mode, d
                                                            seed);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_fill")
 
 bkma_status bkma_adv_error_norms(const bkma_adv_plan *plan, const void *data, int32_t data_dtype,
-                                 const void *ref, int32_t ref_dtype, double *out, void *stream) {
+                                 const void *ref, int32_t ref_dtype, double *out, void *stream) try {
     BKMA_CHECK_ARG(plan && data && ref && out, "null argument");
     BKMA_CHECK_ARG((data_dtype == BKMA_F32 || data_dtype == BKMA_F64) &&
                        (ref_dtype == BKMA_F32 || ref_dtype == BKMA_F64),
@@ -184,10 +184,10 @@ bkma_status bkma_adv_error_norms(const bkma_adv_plan *plan, const void *data, in
     }
     for (int q = 0; q < 4; ++q) out[q] = r[q];
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_error_norms")
 
 bkma_status bkma_adv_validate(const bkma_adv_plan *plan, const void *data, int64_t max_iter,
-                              double *highest_l1, double *lowest_l1, void *stream) {
+                              double *highest_l1, double *lowest_l1, void *stream) try {
     BKMA_CHECK_ARG(plan && data, "null argument");
     const AdvPlanImpl &p = plan_impl(plan);
     cudaStream_t st = (cudaStream_t)stream;
@@ -225,6 +225,6 @@ bkma_status bkma_adv_validate(const bkma_adv_plan *plan, const void *data, int64
     if (highest_l1) *highest_l1 = hi;
     if (lowest_l1) *lowest_l1 = lo;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_validate")
 
 }  // extern "C"

@@ -15,6 +15,7 @@
 // src/core/bkma_tools.hpp:74-107).
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "adv_device.cuh"
@@ -291,26 +292,26 @@ using namespace bkma;
 extern "C" {
 
 bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields, int32_t dtype,
-                                  bkma_adv_batch **batch) {
+                                  bkma_adv_batch **batch) try {
     BKMA_CHECK_ARG(fields && batch && nfields > 0, "bkma_adv_batch_create: bad arguments");
     BKMA_CHECK_ARG(dtype == BKMA_F32 || dtype == BKMA_F64, "dtype must be BKMA_F32 or BKMA_F64");
     *batch = nullptr;
-    auto *bb = new (std::nothrow) bkma_adv_batch;
-    if (!bb) return fail(BKMA_ERR_INVALID_ARG, "out of host memory");
+    // owned here until complete: an early return or an exception frees it
+    std::unique_ptr<bkma_adv_batch> bb(new bkma_adv_batch);
     BatchImpl &b = bb->impl;
     b.dtype = dtype;
     b.esize = dtype == BKMA_F32 ? 4 : 8;
     b.nfields = nfields;
     b.W.assign((size_t)nfields, 0);
     b.R.assign((size_t)nfields, 1);
+    b.plans.reserve((size_t)nfields);  // push_back below cannot throw: no plan leaks
+    b.data.reserve((size_t)nfields);
     for (int i = 0; i < nfields; ++i) {
         const bkma_adv_field &f = fields[i];
         if (!f.data) {
-            delete bb;
             return fail(BKMA_ERR_INVALID_ARG, "field " + std::to_string(i) + ": null data");
         }
         if (f.degree != 3 && f.degree != 5) {
-            delete bb;
             return fail(BKMA_ERR_INVALID_ARG, "field " + std::to_string(i) + ": degree must be 3 or 5");
         }
         bkma_adv_desc d{};
@@ -332,7 +333,6 @@ bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields,
         bkma_status s = bkma_adv_plan_create(&d, &p);
         if (s != BKMA_OK) {
             const std::string m = bkma_last_error();
-            delete bb;
             return fail(s, "field " + std::to_string(i) + ": " + m);
         }
         b.plans.push_back(p);
@@ -341,26 +341,24 @@ bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields,
     }
     cudaError_t e = cudaMalloc(&b.d_counter, sizeof(unsigned long long));
     if (e != cudaSuccess) {
-        delete bb;
         return cuda_fail(e, "batch counter");
     }
     bkma_status s = rebuild(b, nullptr);
     if (s != BKMA_OK) {
-        delete bb;
         return s;
     }
-    *batch = bb;
+    *batch = bb.release();
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_batch_create")
 
-bkma_status bkma_adv_batch_step(bkma_adv_batch *batch, int32_t nsteps, void *stream) {
+bkma_status bkma_adv_batch_step(bkma_adv_batch *batch, int32_t nsteps, void *stream) try {
     BKMA_CHECK_ARG(batch && nsteps >= 0, "bkma_adv_batch_step: bad arguments");
     BatchImpl &b = batch->impl;
     for (int i = 0; i < nsteps; ++i) BKMA_CUDA_TRY(cudaGraphLaunch(b.exec, (cudaStream_t)stream));
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_batch_step")
 
-bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream) {
+bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream) try {
     BKMA_CHECK_ARG(batch, "null argument");
     BatchImpl &b = batch->impl;
     cudaStream_t st = (cudaStream_t)stream;
@@ -407,17 +405,17 @@ bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream) {
     b.stream = best_stream;
     b.segs_mode = best_segs;
     return rebuild(b, st);
-}
+} BKMA_ABI_CATCH("bkma_adv_batch_autotune")
 
-bkma_status bkma_adv_batch_info(const bkma_adv_batch *batch, int64_t *cells, int32_t *launches_per_step) {
+bkma_status bkma_adv_batch_info(const bkma_adv_batch *batch, int64_t *cells, int32_t *launches_per_step) try {
     BKMA_CHECK_ARG(batch, "null argument");
     if (cells) *cells = batch->impl.cells;
     if (launches_per_step) *launches_per_step = batch->impl.launches;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_batch_info")
 
 bkma_status bkma_adv_batch_tiles(const bkma_adv_batch *batch, int32_t *W, int32_t *R, int64_t *tiles,
-                                 int32_t *threads, int64_t *smem_bytes) {
+                                 int32_t *threads, int64_t *smem_bytes) try {
     BKMA_CHECK_ARG(batch, "null argument");
     const BatchImpl &b = batch->impl;
     for (int i = 0; i < b.nfields; ++i) {
@@ -428,11 +426,11 @@ bkma_status bkma_adv_batch_tiles(const bkma_adv_batch *batch, int32_t *W, int32_
     if (threads) *threads = b.threads;
     if (smem_bytes) *smem_bytes = (int64_t)b.smem;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_batch_tiles")
 
-bkma_status bkma_adv_batch_destroy(bkma_adv_batch *batch) {
+bkma_status bkma_adv_batch_destroy(bkma_adv_batch *batch) try {
     delete batch;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_adv_batch_destroy")
 
 }  // extern "C"

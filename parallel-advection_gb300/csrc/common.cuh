@@ -11,9 +11,13 @@
 
 namespace bkma {
 
-void set_error(const std::string &msg);
-bkma_status fail(bkma_status s, const std::string &msg);
-bkma_status cuda_fail(cudaError_t e, const char *what);
+void set_error(const std::string &msg) noexcept;
+bkma_status fail(bkma_status s, const std::string &msg) noexcept;
+bkma_status cuda_fail(cudaError_t e, const char *what) noexcept;
+// BKMA_ERR_HOST with the message of the C++ exception being handled (a host
+// allocation that failed, a thread that could not start), prefixed by the
+// entry point's name. Call only from a catch handler.
+bkma_status host_fail(const char *fn) noexcept;
 // The driver's cuTensorMapEncodeTiled (a PFN_cuTensorMapEncodeTiled_v12000),
 // or null when the CUDA driver does not provide it.
 void *tensor_map_encoder();
@@ -28,6 +32,13 @@ void *tensor_map_encoder();
     do {                                                                     \
         if (!(cond)) return ::bkma::fail(BKMA_ERR_INVALID_ARG, msg);         \
     } while (0)
+
+// Every entry point of the C ABI is a function-try-block closed by this
+// handler: no C++ exception crosses the ABI, the caller gets BKMA_ERR_HOST.
+#define BKMA_ABI_CATCH(fn) \
+    catch (...) {          \
+        return ::bkma::host_fail(fn); \
+    }
 
 // Non-contracted FP64 operations. On the device the _rn intrinsics are never
 // fused; on the host the library is compiled with -ffp-contract=off.

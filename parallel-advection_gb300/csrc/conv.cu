@@ -19,6 +19,7 @@
 // snapshots only the rows past each CTA's last tile.
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <string>
 
 #include "common.cuh"
@@ -233,7 +234,7 @@ bkma_status run_reference(ConvPlanImpl &p, void *data, void *out, const void *w,
 
 extern "C" {
 
-bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **plan) {
+bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **plan) try {
     BKMA_CHECK_ARG(desc && plan, "bkma_conv_plan_create: null argument");
     *plan = nullptr;
     const bkma_conv_desc &d = *desc;
@@ -255,8 +256,8 @@ bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **p
                        "dtype must be F64, F32 or BF16");
         if (d.inplace) BKMA_CHECK_ARG(d.cin == d.cout, "in place needs cin == cout");
     }
-    auto *pl = new (std::nothrow) bkma_conv_plan;
-    if (!pl) return fail(BKMA_ERR_INVALID_ARG, "out of host memory");
+    // owned here until complete: an early return or an exception frees it
+    std::unique_ptr<bkma_conv_plan> pl(new bkma_conv_plan);
     ConvPlanImpl &p = pl->impl;
     p.desc = d;
     if (p.desc.n2 == 0) p.desc.n2 = 1;
@@ -282,21 +283,20 @@ bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **p
         }
     }
     if (s != BKMA_OK) {
-        delete pl;
         return s;
     }
-    *plan = pl;
+    *plan = pl.release();
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_conv_plan_create")
 
-bkma_status bkma_conv_plan_scratch_bytes(const bkma_conv_plan *plan, int64_t *bytes) {
+bkma_status bkma_conv_plan_scratch_bytes(const bkma_conv_plan *plan, int64_t *bytes) try {
     BKMA_CHECK_ARG(plan && bytes, "null argument");
     *bytes = (int64_t)(plan->impl.halo_bytes + plan->impl.wpack_bytes);
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_conv_plan_scratch_bytes")
 
 bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const void *weight,
-                          const void *bias, void *stream) {
+                          const void *bias, void *stream) try {
     BKMA_CHECK_ARG(plan && data && weight, "bkma_conv_run: null argument");
     ConvPlanImpl &p = plan->impl;
     const bkma_conv_desc &d = p.desc;
@@ -311,9 +311,9 @@ bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const voi
     if (p.tensor) return conv_tc_run(p, data, out, weight, bias, st);
     if (d.dtype == BKMA_F64) return run_torch_plain<double>(p, data, out, weight, bias, st);
     return run_torch_plain<float>(p, data, out, weight, bias, st);
-}
+} BKMA_ABI_CATCH("bkma_conv_run")
 
-bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream) {
+bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream) try {
     BKMA_CHECK_ARG(plan, "null argument");
     ConvPlanImpl &p = plan->impl;
     BKMA_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
@@ -323,11 +323,11 @@ bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream) {
     BKMA_CUDA_TRY(cudaMemset(p.d_status, 0, sizeof(int)));
     if (st != 0) return fail((bkma_status)st, "tensor-core conv1d: a bounded device wait timed out");
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_conv_plan_status")
 
-bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan) {
+bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan) try {
     delete plan;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_conv_plan_destroy")
 
 }  // extern "C"

@@ -62,7 +62,7 @@ using namespace bkma;
 extern "C" bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *weight,
                                                         const void *bias, int64_t batch,
                                                         int64_t channels, int64_t length,
-                                                        int64_t ksize, void *stream) {
+                                                        int64_t ksize, void *stream) try {
     BKMA_CHECK_ARG(data && weight, "bkma_conv1d_bf16_inplace_noalloc: null data or weight");
     BKMA_CHECK_ARG(batch > 0 && channels > 0 && length > 0 && ksize > 0 && ksize <= length,
                    "bkma_conv1d_bf16_inplace_noalloc: need batch, channels, length > 0 and "
@@ -97,4 +97,4 @@ extern "C" bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *
     int *status = reinterpret_cast<int *>(base + kStatusOff);
     BKMA_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
     return conv_tc_run_into(d, data, weight, bias, base + kHaloOff, base + kWpackOff, status, st);
-}
+} BKMA_ABI_CATCH("bkma_conv1d_bf16_inplace_noalloc")

@@ -101,7 +101,7 @@ using namespace bkma;
 
 extern "C" {
 
-bkma_status bkma_fill(void *data, int64_t count, int32_t dtype, double value, void *stream) {
+bkma_status bkma_fill(void *data, int64_t count, int32_t dtype, double value, void *stream) try {
     BKMA_CHECK_ARG(data && count >= 0, "bkma_fill: bad arguments");
     if (count == 0) return BKMA_OK;
     cudaStream_t st = (cudaStream_t)stream;
@@ -117,10 +117,10 @@ bkma_status bkma_fill(void *data, int64_t count, int32_t dtype, double value, vo
     }
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_fill")
 
 bkma_status bkma_conv_check(const void *data, int32_t dtype, int64_t n0, int64_t n1, int64_t n2,
-                            int64_t nw, double *mean, int32_t *equal, void *stream) {
+                            int64_t nw, double *mean, int32_t *equal, void *stream) try {
     BKMA_CHECK_ARG(data && n0 > 0 && n1 > 0 && n2 > 0 && nw > 0 && nw <= n1,
                    "bkma_conv_check: need n0, n1, n2 > 0 and 0 < nw <= n1");
     cudaStream_t st = (cudaStream_t)stream;
@@ -130,6 +130,6 @@ bkma_status bkma_conv_check(const void *data, int32_t dtype, int64_t n0, int64_t
     case BKMA_BF16: return check_t<__nv_bfloat16>(data, n0, n1, n2, nw, mean, equal, st);
     default: return fail(BKMA_ERR_INVALID_ARG, "bkma_conv_check: dtype must be F32, F64 or BF16");
     }
-}
+} BKMA_ABI_CATCH("bkma_conv_check")
 
 }  // extern "C"

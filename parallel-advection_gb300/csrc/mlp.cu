@@ -13,6 +13,7 @@
 //
 // Parameter layout (1252 floats): W1[32] b1[32] W2[32][32] b2[32] W3[4][32] b3[4].
 #include <cmath>
+#include <memory>
 #include <vector>
 
 #include "common.cuh"
@@ -309,11 +310,11 @@ bkma_status launch_grad(MlpImpl &M, const float *alpha, const float *taps4, cons
 
 extern "C" {
 
-bkma_status bkma_mlp_create(uint64_t seed, bkma_mlp **out) {
+bkma_status bkma_mlp_create(uint64_t seed, bkma_mlp **out) try {
     BKMA_CHECK_ARG(out, "null argument");
     *out = nullptr;
-    auto *m = new (std::nothrow) bkma_mlp;
-    if (!m) return fail(BKMA_ERR_INVALID_ARG, "out of host memory");
+    // owned here until complete: an early return or an exception frees it
+    std::unique_ptr<bkma_mlp> m(new bkma_mlp);
     MlpImpl &M = m->impl;
     // hidden layers U[-1,1]*sqrt(6/(fan_in+fan_out)) from the shared generator,
     // output layer zero
@@ -333,14 +334,13 @@ bkma_status bkma_mlp_create(uint64_t seed, bkma_mlp **out) {
     if (e == cudaSuccess) e = cudaMemset(M.d_m, 0, sizeof(float) * mlp::NP);
     if (e == cudaSuccess) e = cudaMemset(M.d_v, 0, sizeof(float) * mlp::NP);
     if (e != cudaSuccess) {
-        delete m;
         return cuda_fail(e, "bkma_mlp_create");
     }
-    *out = m;
+    *out = m.release();
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_mlp_create")
 
-bkma_status bkma_mlp_params(bkma_mlp *mlp, float *host_params, int32_t set) {
+bkma_status bkma_mlp_params(bkma_mlp *mlp, float *host_params, int32_t set) try {
     BKMA_CHECK_ARG(mlp && host_params, "null argument");
     const size_t b = sizeof(float) * mlp::NP;
     if (set)
@@ -348,21 +348,21 @@ bkma_status bkma_mlp_params(bkma_mlp *mlp, float *host_params, int32_t set) {
     else
         BKMA_CUDA_TRY(cudaMemcpy(host_params, mlp->impl.d_params, b, cudaMemcpyDeviceToHost));
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_mlp_params")
 
 bkma_status bkma_mlp_samples(int64_t n, uint64_t seed, int64_t first, float *alpha, float *taps4,
-                             float *target, void *stream) {
+                             float *target, void *stream) try {
     BKMA_CHECK_ARG(n > 0 && alpha && taps4 && target && first >= 0, "bad arguments");
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
     mlp::samples_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(n, seed, first, alpha,
                                                                            taps4, target);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_mlp_samples")
 
 bkma_status bkma_mlp_grad(bkma_mlp *mlp, const float *alpha, const float *taps4,
                           const float *target, int64_t n, float *host_grad, double *host_loss,
-                          void *stream) {
+                          void *stream) try {
     BKMA_CHECK_ARG(mlp && alpha && taps4 && target && n > 0 && host_grad, "bad arguments");
     MlpImpl &M = mlp->impl;
     cudaStream_t st = (cudaStream_t)stream;
@@ -378,11 +378,11 @@ bkma_status bkma_mlp_grad(bkma_mlp *mlp, const float *alpha, const float *taps4,
     BKMA_CUDA_TRY(cudaMemsetAsync(M.d_grad, 0, sizeof(float) * mlp::NP, st));
     if (host_loss) *host_loss = loss / (double)n;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_mlp_grad")
 
 bkma_status bkma_mlp_train(bkma_mlp *mlp, const float *alpha, const float *taps4,
                            const float *target, int64_t n, int32_t steps, int32_t batch,
-                           float lr_max, uint64_t seed, double *host_loss, void *stream) {
+                           float lr_max, uint64_t seed, double *host_loss, void *stream) try {
     BKMA_CHECK_ARG(mlp && alpha && taps4 && target && n > 0 && steps >= 0 && batch > 0 &&
                        lr_max > 0,
                    "bad arguments");
@@ -409,21 +409,21 @@ bkma_status bkma_mlp_train(bkma_mlp *mlp, const float *alpha, const float *taps4
         *host_loss = l / (double)batch;
     }
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_mlp_train")
 
 bkma_status bkma_mlp_infer(const bkma_mlp *mlp, const float *alpha, int64_t n, float *weights,
-                           void *stream) {
+                           void *stream) try {
     BKMA_CHECK_ARG(mlp && alpha && weights && n > 0, "bad arguments");
     const int64_t blocks = std::min<int64_t>((n + 127) / 128, 152 * 8);
     mlp::infer_kernel<<<(unsigned)blocks, 128, 0, (cudaStream_t)stream>>>(mlp->impl.d_params, alpha,
                                                                          n, weights);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_mlp_infer")
 
-bkma_status bkma_mlp_destroy(bkma_mlp *mlp) {
+bkma_status bkma_mlp_destroy(bkma_mlp *mlp) try {
     delete mlp;
     return BKMA_OK;
-}
+} BKMA_ABI_CATCH("bkma_mlp_destroy")
 
 }  // extern "C"

@@ -56,6 +56,8 @@ def test_impl_selector_unknown_name_message(bkma):
     (dict(i0_offset=9), "i0_offset"),
     (dict(i0_count=9), "i0_count"),
     (dict(maxX=-1.0), "maxX"),
+    (dict(n0=2**31), "n0 must be < 2^31"),
+    (dict(n0=2**28, n1=2**16, n2=2**8), "2^50"),
 ])
 def test_adv_descriptor_validation(bkma, kw, msg):
     args = dict(n0=8, n1=64, n2=3)
@@ -89,3 +91,43 @@ def test_null_arguments(bkma):
     assert lib.bkma_adv_step(None, None, None, 1, None) == 1
     assert lib.bkma_conv_run(None, None, None, None, None, None) == 1
     assert lib.bkma_adv_plan_create(None, None) == 1
+
+
+def test_long_error_message_is_truncated(bkma):
+    """The error text lives in a fixed per-thread buffer: an unknown name of
+    5000 characters gives the error status and a message cut to 1023 bytes."""
+    with pytest.raises(bkma.BkmaError) as e:
+        bkma.impl_from_name("x" * 5000)
+    assert e.value.status == 2
+    assert len(bkma.load().bkma_last_error()) == 1023
+
+
+_OOM_CHILD = r"""
+import resource, sys
+sys.path.insert(0, sys.argv[1])
+import bkma_gb300
+from bkma_gb300 import _lib
+bkma_gb300.load()
+vm = [l for l in open("/proc/self/status") if l.startswith("VmSize:")][0].split()[1]
+lim = int(vm) * 1024 + (1 << 30)  # 1 GiB above the current address space
+resource.setrlimit(resource.RLIMIT_AS, (lim, resource.getrlimit(resource.RLIMIT_AS)[1]))
+try:
+    bkma_gb300.AdvectionPlan(2**30, 64, 1, dtype="f32")  # 4 GiB of line tables first
+except bkma_gb300.BkmaError as e:
+    print("STATUS", e.status, str(e))
+    sys.exit(0)
+print("NO ERROR")
+"""
+
+
+def test_host_allocation_failure_is_a_status(bkma):
+    """A plan whose host-side line tables cannot be allocated returns
+    BKMA_ERR_HOST through the C ABI (no C++ exception reaches the caller).
+    The child process caps its address space, so the allocation fails at once
+    and no memory is touched."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-c", _OOM_CHILD, os.path.join(ROOT, "parallel-advection_gb300")],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "STATUS 6 BKMA_ERR_HOST: bkma_adv_plan_create: " in r.stdout, r.stdout + r.stderr[-2000:]
