@@ -20,11 +20,29 @@ _W = {"reference": _lib.BKMA_W_REFERENCE, "lagrange": _lib.BKMA_W_LAGRANGE,
       "table": _lib.BKMA_W_TABLE}
 
 
-def _ptr(t) -> int | None:
-    if t is None:
-        return None
-    if isinstance(t, int):
+def _dev(t, name: str, dtype: str | None = None, numel: int | None = None) -> int | None:
+    """Device address of a tensor argument, after the checks a kernel cannot
+    make on a raw pointer: a CUDA tensor on the current device, contiguous, of
+    `dtype`, with at least `numel` elements (a host, short or mistyped buffer
+    would be read or written out of bounds on the GPU). None stays None; an
+    integer is a raw device address the caller vouches for, as through the C
+    ABI itself."""
+    if t is None or isinstance(t, int):
         return t
+
+    def bad(why):
+        return BkmaError(_lib.BKMA_ERR_INVALID_ARG, f"{name}: {why}")
+    if not getattr(t, "is_cuda", False):
+        raise bad("not a CUDA tensor (the library runs on the GPU only)")
+    import torch
+    if t.device.index != torch.cuda.current_device():
+        raise bad(f"on {t.device}, but the current device is cuda:{torch.cuda.current_device()}")
+    if not t.is_contiguous():
+        raise bad("not contiguous")
+    if dtype is not None and _dtype_name(t) != dtype:
+        raise bad(f"dtype {t.dtype}, the plan computes in {dtype}")
+    if numel is not None and t.numel() < numel:
+        raise bad(f"{t.numel()} elements, {numel} needed")
     return t.data_ptr()
 
 
@@ -50,7 +68,7 @@ def shard_lines(n0: int, rank: int, world: int) -> tuple[int, int]:
 
 def fill(data, value: float, stream=None):
     """fill_buffer_conv1d's constant fill of a CUDA tensor (F32/F64/BF16)."""
-    check(load().bkma_fill(_ptr(data), data.numel(), _DT[_dtype_name(data)], value,
+    check(load().bkma_fill(_dev(data, "data"), data.numel(), _DT[_dtype_name(data)], value,
                            _stream(stream)))
     return data
 
@@ -60,7 +78,7 @@ def conv_check(data, nw: int, stream=None) -> tuple[float, bool]:
     tensor: (mean of the first nw values per line, all equal per i1)."""
     n0, n1, n2 = data.shape
     mean, equal = C.c_double(), C.c_int32()
-    check(load().bkma_conv_check(_ptr(data), _DT[_dtype_name(data)], n0, n1, n2, nw,
+    check(load().bkma_conv_check(_dev(data, "data"), _DT[_dtype_name(data)], n0, n1, n2, nw,
                                  C.byref(mean), C.byref(equal), _stream(stream)))
     return mean.value, bool(equal.value)
 
@@ -110,7 +128,9 @@ class AdvectionPlan:
         return {n: getattr(i, n) for n, _ in i._fields_}
 
     def step(self, data, out=None, nsteps: int = 1, stream=None):
-        check(load().bkma_adv_step(self._h, _ptr(data), _ptr(out), nsteps, _stream(stream)))
+        n = self.lines * self.n1 * self.n2
+        check(load().bkma_adv_step(self._h, _dev(data, "data", self.dtype, n),
+                                   _dev(out, "out", self.dtype, n), nsteps, _stream(stream)))
         return data if out is None else out
 
     def run_host(self, host: np.ndarray, nsteps: int = 1, stream=None) -> np.ndarray:
@@ -118,6 +138,9 @@ class AdvectionPlan:
         assert host.dtype == want and host.flags["C_CONTIGUOUS"] and host.shape == self.shape
         check(load().bkma_adv_run_host(self._h, host.ctypes.data, nsteps, _stream(stream)))
         return host
+
+    def _field(self, t, name: str) -> int | None:
+        return _dev(t, name, self.dtype, self.lines * self.n1 * self.n2)
 
     def set_tile(self, W: int, R: int = 1, threads: int = 256, path: int = 0):
         check(load().bkma_adv_plan_set_tile(self._h, W, R, threads, path))
@@ -138,18 +161,22 @@ class AdvectionPlan:
         check(load().bkma_adv_plan_set_fused_state(self._h, {"f32": 0, "f32x2": 1}[state]))
 
     def autotune(self, field, stream=None):
-        check(load().bkma_adv_plan_autotune(self._h, _ptr(field), _stream(stream)))
+        check(load().bkma_adv_plan_autotune(self._h, self._field(field, "field"),
+                                            _stream(stream)))
         return self.info()
 
     def fill(self, data, mode: int = 0, amp: float = 0.0, seed: int = 0, stream=None):
-        check(load().bkma_adv_fill(self._h, _ptr(data), mode, amp, seed, _stream(stream)))
+        check(load().bkma_adv_fill(self._h, self._field(data, "data"), mode, amp, seed,
+                                   _stream(stream)))
         return data
 
     def error_norms(self, data, ref, stream=None) -> dict:
         out = (C.c_double * 4)()
         dd = _DT[_dtype_name(data)]
         rd = _DT[_dtype_name(ref)]
-        check(load().bkma_adv_error_norms(self._h, _ptr(data), dd, _ptr(ref), rd, out,
+        n = self.lines * self.n1 * self.n2
+        check(load().bkma_adv_error_norms(self._h, _dev(data, "data", None, n), dd,
+                                          _dev(ref, "ref", None, n), rd, out,
                                           _stream(stream)))
         maxabs, maxref, se, sr = list(out)
         return {"max_abs": maxabs, "max_ref": maxref,
@@ -158,7 +185,8 @@ class AdvectionPlan:
 
     def validate(self, data, max_iter: int, stream=None) -> tuple[float, float]:
         hi, lo = C.c_double(), C.c_double()
-        check(load().bkma_adv_validate(self._h, _ptr(data), max_iter, C.byref(hi), C.byref(lo),
+        check(load().bkma_adv_validate(self._h, self._field(data, "data"), max_iter,
+                                       C.byref(hi), C.byref(lo),
                                        _stream(stream)))
         return hi.value, lo.value
 
@@ -175,7 +203,8 @@ class AdvectionPlan:
             w = np.ascontiguousarray(weights, dtype=np.float32)
             check(load().bkma_adv_plan_set_weights(self._h, w.ctypes.data, 0))
         else:
-            check(load().bkma_adv_plan_set_weights(self._h, _ptr(weights), 1))
+            n = self.lines * (self.desc.degree + 1)
+            check(load().bkma_adv_plan_set_weights(self._h, _dev(weights, "weights", "f32", n), 1))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -203,7 +232,9 @@ class AdvectionBatch:
             t = f["data"]
             n0, n1, n2 = t.shape
             a = arr[i]
-            a.data = t.data_ptr()
+            if len(t.shape) != 3:
+                raise BkmaError(_lib.BKMA_ERR_INVALID_ARG, f"field {i}: data must be n0 x n1 x n2")
+            a.data = _dev(t, f"field {i}", dtype)
             a.n0, a.n1, a.n2 = n0, n1, n2
             a.degree = f.get("degree", 5)
             a.weights = _W[f.get("weights", "reference" if a.degree == 5 else "lagrange")]
@@ -287,24 +318,31 @@ class LearnedStencil:
         assert q.shape == (self.NP,)
         check(load().bkma_mlp_params(self._h, q.ctypes.data, 1))
 
+    @staticmethod
+    def _samples(a, f4, t) -> tuple[int, int, int]:
+        n = a.numel()
+        return (_dev(a, "alpha", "f32"), _dev(f4, "taps4", "f32", 4 * n),
+                _dev(t, "target", "f32", n))
+
     def grad(self, a, f4, t) -> tuple[float, np.ndarray]:
         g = np.zeros(self.NP, dtype=np.float32)
         loss = C.c_double()
-        check(load().bkma_mlp_grad(self._h, a.data_ptr(), f4.data_ptr(), t.data_ptr(), a.numel(),
+        check(load().bkma_mlp_grad(self._h, *self._samples(a, f4, t), a.numel(),
                                    g.ctypes.data, C.byref(loss), _stream(None)))
         return loss.value, g
 
     def train(self, a, f4, t, steps: int, batch: int = 4096, lr: float = 3e-3,
               seed: int = 1) -> float:
         loss = C.c_double()
-        check(load().bkma_mlp_train(self._h, a.data_ptr(), f4.data_ptr(), t.data_ptr(), a.numel(),
+        check(load().bkma_mlp_train(self._h, *self._samples(a, f4, t), a.numel(),
                                     steps, batch, lr, seed, C.byref(loss), _stream(None)))
         return loss.value
 
     def infer(self, alpha):
         import torch
         out = torch.empty(alpha.numel(), 4, dtype=torch.float32, device=alpha.device)
-        check(load().bkma_mlp_infer(self._h, alpha.data_ptr(), alpha.numel(), out.data_ptr(),
+        check(load().bkma_mlp_infer(self._h, _dev(alpha, "alpha", "f32"), alpha.numel(),
+                                    out.data_ptr(),
                                     _stream(None)))
         return out
 
@@ -358,6 +396,7 @@ class Conv1dPlan:
                   "plain": _lib.BKMA_CONV_PLAIN}[impl]
         d.inplace = int(inplace)
         self.desc = d
+        self.dtype, self.semantics = dtype, semantics
         h = C.c_void_p()
         check(load().bkma_conv_plan_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -368,8 +407,17 @@ class Conv1dPlan:
         return b.value
 
     def run(self, data, weight, bias=None, out=None, stream=None):
-        check(load().bkma_conv_run(self._h, _ptr(data), _ptr(out), _ptr(weight), _ptr(bias),
-                                   _stream(stream)))
+        d = self.desc
+        dt = self.dtype
+        if self.semantics == "reference":
+            n_x = n_out = d.batch * d.cin * d.length * d.n2
+        else:
+            n_x = d.batch * d.cin * d.length
+            n_out = d.batch * d.cout * (d.length - d.ksize + 1)
+        check(load().bkma_conv_run(self._h, _dev(data, "data", dt, n_x),
+                                   _dev(out, "out", dt, n_out),
+                                   _dev(weight, "weight", dt, d.cout * d.cin * d.ksize),
+                                   _dev(bias, "bias", dt, d.cout), _stream(stream)))
         return data if out is None else out
 
     def status(self, stream=None):

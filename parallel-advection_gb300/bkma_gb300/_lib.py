@@ -13,6 +13,7 @@ from . import build as _build
 LIB_PATH = _build.LIB
 
 BKMA_OK = 0
+BKMA_ERR_INVALID_ARG = 1
 STATUS_NAMES = {0: "BKMA_OK", 1: "BKMA_ERR_INVALID_ARG", 2: "BKMA_ERR_UNSUPPORTED",
                 3: "BKMA_ERR_CUDA", 4: "BKMA_ERR_TIMEOUT", 5: "BKMA_ERR_NO_DEVICE",
                 6: "BKMA_ERR_HOST"}

@@ -680,3 +680,28 @@ def test_rows_path_misaligned_field_falls_back(bkma, cuda, oracle):
     want = oracle.adv_step(p, f0.copy(), 2)
     err = np.abs(aligned.cpu().numpy().astype(np.float64) - want).max() / np.abs(want).max()
     assert err <= 3e-7 * 2 + 2e-7, err
+
+
+def test_tensor_arguments_are_checked(bkma, cuda):
+    """Host, mistyped, short and strided tensors are refused in Python with
+    BKMA_ERR_INVALID_ARG before anything is launched; the field is untouched."""
+    import torch
+    plan = bkma.AdvectionPlan(8, 64, 4, dtype="f32")
+    good = torch.ones((8, 64, 4), device=cuda)
+    for bad, why in ((torch.ones((8, 64, 4)), "not a CUDA tensor"),
+                     (torch.ones((8, 64, 4), device=cuda, dtype=torch.float64), "dtype"),
+                     (torch.ones((7, 64, 4), device=cuda), "needed"),
+                     (torch.ones((8, 4, 64), device=cuda).transpose(1, 2), "not contiguous")):
+        with pytest.raises(bkma.BkmaError) as e:
+            plan.step(bad)
+        assert e.value.status == 1 and why in str(e.value)
+    with pytest.raises(bkma.BkmaError):
+        plan.step(good, out=torch.ones(10, device=cuda))
+    conv = bkma.Conv1dPlan(2, 16, 16, 64, 3, dtype="bf16", impl="tensor")
+    x = torch.ones((2, 16, 64), device=cuda, dtype=torch.bfloat16)
+    with pytest.raises(bkma.BkmaError) as e:
+        conv.run(x, torch.ones((16, 16, 2), device=cuda, dtype=torch.bfloat16))
+    assert "weight" in str(e.value)
+    torch.cuda.synchronize()
+    assert torch.equal(good, torch.ones_like(good))
+    assert torch.equal(x, torch.ones_like(x))

@@ -131,3 +131,18 @@ def test_host_allocation_failure_is_a_status(bkma):
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "STATUS 6 BKMA_ERR_HOST: bkma_adv_plan_create: " in r.stdout, r.stdout + r.stderr[-2000:]
+
+
+def test_tensor_arguments_are_checked_before_any_launch(bkma):
+    """The Python mirror refuses what a kernel would read out of bounds:
+    host tensors and arrays (the device checks are in the GPU tests). Raw
+    integer addresses and None pass through, as through the C ABI."""
+    import numpy as np
+    import torch
+    from bkma_gb300 import _dev
+    for bad in (torch.zeros(4), np.zeros(4, dtype=np.float32)):
+        with pytest.raises(bkma.BkmaError) as e:
+            _dev(bad, "data", "f32", 4)
+        assert e.value.status == 1 and "data: not a CUDA tensor" in str(e.value)
+    assert _dev(None, "out") is None
+    assert _dev(4096, "data", "f32", 1 << 20) == 4096
