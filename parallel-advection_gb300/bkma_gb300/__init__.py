@@ -135,7 +135,11 @@ class AdvectionPlan:
 
     def run_host(self, host: np.ndarray, nsteps: int = 1, stream=None) -> np.ndarray:
         want = np.float32 if self.dtype == "f32" else np.float64
-        assert host.dtype == want and host.flags["C_CONTIGUOUS"] and host.shape == self.shape
+        if not (isinstance(host, np.ndarray) and host.dtype == want and host.flags["C_CONTIGUOUS"]
+                and host.shape == self.shape):
+            raise BkmaError(_lib.BKMA_ERR_INVALID_ARG,
+                            f"host: a C-contiguous {np.dtype(want).name} array of shape "
+                            f"{self.shape} is needed")
         check(load().bkma_adv_run_host(self._h, host.ctypes.data, nsteps, _stream(stream)))
         return host
 
@@ -315,7 +319,8 @@ class LearnedStencil:
 
     def set_params(self, p):
         q = np.ascontiguousarray(p, dtype=np.float32)
-        assert q.shape == (self.NP,)
+        if q.shape != (self.NP,):
+            raise BkmaError(_lib.BKMA_ERR_INVALID_ARG, f"params: {self.NP} values needed")
         check(load().bkma_mlp_params(self._h, q.ctypes.data, 1))
 
     @staticmethod

@@ -146,3 +146,16 @@ def test_tensor_arguments_are_checked_before_any_launch(bkma):
         assert e.value.status == 1 and "data: not a CUDA tensor" in str(e.value)
     assert _dev(None, "out") is None
     assert _dev(4096, "data", "f32", 1 << 20) == 4096
+
+
+def test_host_array_checks_need_no_device(bkma):
+    """run_host refuses a mistyped or misshapen host array before the C ABI
+    is called (an object without a plan handle shows no call is made)."""
+    import numpy as np
+    plan = bkma.AdvectionPlan.__new__(bkma.AdvectionPlan)
+    plan.dtype, plan.lines, plan.n1, plan.n2, plan._h = "f32", 4, 16, 2, None
+    for bad in (np.zeros((4, 16, 2)), np.zeros((4, 16, 3), dtype=np.float32),
+                np.zeros((4, 2, 16), dtype=np.float32).transpose(0, 2, 1)):
+        with pytest.raises(bkma.BkmaError) as e:
+            plan.run_host(bad)
+        assert e.value.status == 1 and "(4, 16, 2)" in str(e.value)
