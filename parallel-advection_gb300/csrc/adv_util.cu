@@ -192,6 +192,7 @@ bkma_status bkma_adv_validate(const bkma_adv_plan *plan, const void *data, int64
     const AdvPlanImpl &p = plan_impl(plan);
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t n2 = p.desc.n2;
+    std::vector<double> h((size_t)n2);  // before the device buffers: a throw leaks nothing
     double *sums = nullptr;
     double *vx = nullptr;
     BKMA_CUDA_TRY(cudaMalloc(&sums, sizeof(double) * (size_t)n2));
@@ -209,7 +210,6 @@ bkma_status bkma_adv_validate(const bkma_adv_plan *plan, const void *data, int64
                                                      vx, p.phys.minX, p.phys.dx, t, sums);
         e = cudaGetLastError();
     }
-    std::vector<double> h((size_t)n2);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h.data(), sums, sizeof(double) * n2, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

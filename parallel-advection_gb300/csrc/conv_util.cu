@@ -67,6 +67,7 @@ __global__ void conv_check_kernel(const T *__restrict__ data, int64_t n0, int64_
 template <typename T>
 bkma_status check_t(const void *data, int64_t n0, int64_t n1, int64_t n2, int64_t nw,
                     double *mean, int32_t *equal, cudaStream_t st) {
+    std::vector<double> h(kCheckBlocks);  // before the device buffer: a throw leaks nothing
     double *d_partial = nullptr;
     int *d_differ = nullptr;
     BKMA_CUDA_TRY(cudaMalloc(&d_partial, sizeof(double) * kCheckBlocks + sizeof(int) * 4));
@@ -77,7 +78,6 @@ bkma_status check_t(const void *data, int64_t n0, int64_t n1, int64_t n2, int64_
             (const T *)data, n0, n1, n2, nw, d_partial, d_differ);
         e = cudaGetLastError();
     }
-    std::vector<double> h(kCheckBlocks);
     int differ = 0;
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h.data(), d_partial, sizeof(double) * kCheckBlocks,
