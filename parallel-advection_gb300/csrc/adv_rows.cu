@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kRowsThreads) adv_rows_f32(AdvStagedArgs<float
         const int c0 = i - l * n1;
         const int64_t line = line0 + l;
         const float *Sl = S + l * n1;
-        const int exc = a.exc_index[line];
+        const int exc = a.exc_index ? a.exc_index[line] : -1;
         float o[4];
         if (exc < 0) {
             float w[NT];
@@ -131,7 +131,9 @@ cudaError_t launch_rows(const AdvPlanImpl &p, const void *src, void *dst, int R,
     a.ncb = 1;
     a.base = p.d_base;
     a.w = (const float *)p.d_w;
-    a.exc_index = p.d_exc_index;
+    // no exception lines: the kernel skips the index (4 of the 32 table
+    // bytes a 16-cell line reads)
+    a.exc_index = p.n_exc > 0 ? p.d_exc_index : nullptr;
     a.exc = (const AdvExcCell<float> *)p.d_exc;
     a.line_list = nullptr;
     const size_t smem = adv_rows_smem(p, R);
