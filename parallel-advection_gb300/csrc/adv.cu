@@ -262,7 +262,7 @@ cudaError_t launch_staged_t(const AdvPlanImpl &p, const T *src, T *dst, int W, i
     a.ncb = p.ncb(W);
     a.base = p.d_base;
     a.w = (const T *)p.d_w;
-    a.exc_index = p.d_exc_index;
+    a.exc_index = p.n_exc > 0 ? p.d_exc_index : nullptr;  // null: no per-line index reads
     a.exc = (const AdvExcCell<T> *)p.d_exc;
     a.line_list = list;
     const size_t smem = p.smem_bytes(W, a.R);

@@ -271,7 +271,8 @@ template <typename T, int NT>
 __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const TileCoord &tc, T *sm) {
     // Parameters of the first line, loaded before the staging wait so their
     // latency hides behind the copies.
-    const int exc0 = a.exc_index[tc.line0];
+    // a null exception index: the plan has no exception lines
+    const int exc0 = a.exc_index ? a.exc_index[tc.line0] : -1;
     const int base0 = a.base[tc.line0];
     T w0[NT];
 #pragma unroll
@@ -317,7 +318,7 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
             const int64_t g0 = line * a.n1 * a.n2 + tc.c0;
             const int lead = packed ? 0 : chunk_lead(a.src + g0);
             const T *S = sm + (int64_t)s * sstride + lead;
-            const int exc = a.exc_index[line];
+            const int exc = a.exc_index ? a.exc_index[line] : -1;
             int rr;
             T w[NT];
             if (exc < 0) {
@@ -341,7 +342,7 @@ __device__ __forceinline__ void staged_tile(const AdvStagedArgs<T> &a, const Til
         const int lead = packed ? 0 : chunk_lead(a.src + g0);
         const T *S = sm + (int64_t)s * sstride + lead;
         T *G = a.dst + g0;
-        const int exc = s == 0 ? exc0 : a.exc_index[line];
+        const int exc = s == 0 ? exc0 : a.exc_index ? a.exc_index[line] : -1;
         if (exc < 0) {
             const int base = s == 0 ? base0 : a.base[line];
             T w[NT];

@@ -157,7 +157,7 @@ void staged_entry(std::vector<BatchFieldDev<T>> &f, BatchImpl &b, const AdvPlanI
     a.ncb = p.ncb(W);
     a.base = p.d_base;
     a.w = (const T *)p.d_w;
-    a.exc_index = p.d_exc_index;
+    a.exc_index = p.n_exc > 0 ? p.d_exc_index : nullptr;  // null: no per-line index reads
     a.exc = (const AdvExcCell<T> *)p.d_exc;
     a.line_list = list;
     e.npts = p.npts;
