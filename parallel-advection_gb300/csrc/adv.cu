@@ -272,7 +272,7 @@ cudaError_t launch_staged_t(const AdvPlanImpl &p, const T *src, T *dst, int W, i
     if (e != cudaSuccess) return e;
     const int64_t grid = list ? nlist * a.ncb : p.tiles(W, R);
     if (grid == 0) return cudaSuccess;
-    kern<<<(unsigned)grid, threads, smem, st>>>(a);
+    kern<<<grid_x(grid), threads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -307,7 +307,7 @@ cudaError_t launch_plain(const AdvPlanImpl &p, const double *src, double *dst, i
     cudaError_t e =
         cudaFuncSetAttribute(adv_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    adv_plain<<<(unsigned)p.tiles(W, R), threads, smem, st>>>(a);
+    adv_plain<<<grid_x(p.tiles(W, R)), threads, smem, st>>>(a);
     return cudaGetLastError();
 }
 

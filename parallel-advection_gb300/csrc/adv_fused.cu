@@ -384,7 +384,7 @@ cudaError_t launch_fused_f32(const AdvPlanImpl &p, const void *src, void *dst, i
     const int G = ((W + 3) & ~3) / 4;
     const int thr = (int)std::min<int64_t>(
         kFuseThreads, (G * ((p.desc.n1 + kRowsF32 - 1) / kRowsF32) + 31) / 32 * 32);
-    kern<<<(unsigned)p.tiles(W, 1), thr, smem, st>>>(a, ksteps);
+    kern<<<grid_x(p.tiles(W, 1)), thr, smem, st>>>(a, ksteps);
     return cudaGetLastError();
 }
 
@@ -414,7 +414,7 @@ cudaError_t launch_fused_x2(const AdvPlanImpl &p, const void *src, void *dst, in
     // SM at 74 registers instead of one 512-thread CTA with 170 idle
     // threads (766 -> 982 G cell-steps/s on 2048 x 1024 x 512, 50 steps)
     const int thr = (int)std::min<int64_t>(kFuseThreads, ((p.desc.n1 + R - 1) / R + 31) / 32 * 32);
-    kern<<<(unsigned)p.tiles(4, 1), thr, smem, st>>>(a, ksteps);
+    kern<<<grid_x(p.tiles(4, 1)), thr, smem, st>>>(a, ksteps);
     return cudaGetLastError();
 }
 
@@ -441,7 +441,7 @@ cudaError_t launch_fused_t(const AdvPlanImpl &p, const void *src, void *dst, int
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<(unsigned)p.tiles(W, 1), kFuseThreads, smem, st>>>(a, ksteps);
+    kern<<<grid_x(p.tiles(W, 1)), kFuseThreads, smem, st>>>(a, ksteps);
     return cudaGetLastError();
 }
 

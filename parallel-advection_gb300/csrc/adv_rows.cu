@@ -142,7 +142,7 @@ cudaError_t launch_rows(const AdvPlanImpl &p, const void *src, void *dst, int R,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (p.lines + R - 1) / R;
-    kern<<<(unsigned)grid, kRowsThreads, smem, st>>>(a);
+    kern<<<grid_x(grid), kRowsThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -218,7 +218,7 @@ template <int NT>
 cudaError_t launch_stream(StreamField one, const StreamField *many, int nfields, int64_t ctas,
                           cudaStream_t st) {
     if (ctas == 0) return cudaSuccess;
-    adv_stream_f32<NT><<<(unsigned)ctas, kWarps * 32, 0, st>>>(one, many, nfields);
+    adv_stream_f32<NT><<<grid_x(ctas), kWarps * 32, 0, st>>>(one, many, nfields);
     return cudaGetLastError();
 }
 

@@ -169,7 +169,7 @@ cudaError_t launch_tma_t(const CUtensorMap &tm, const AdvTmaArgs &a, int threads
     auto kern = adv_tma_f32<NT, WC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<(unsigned)grid, threads, smem, st>>>(tm, a);
+    kern<<<grid_x(grid), threads, smem, st>>>(tm, a);
     return cudaGetLastError();
 }
 

@@ -33,6 +33,13 @@ void *tensor_map_encoder();
         if (!(cond)) return ::bkma::fail(BKMA_ERR_INVALID_ARG, msg);         \
     } while (0)
 
+// x dimension of a 1-D launch: 0 (a launch error, "invalid configuration")
+// when the CTA count is above the 2^31 - 1 limit, never a silently truncated
+// grid that would leave tiles unprocessed.
+inline unsigned grid_x(int64_t ctas) {
+    return ctas > 0 && ctas <= 0x7fffffff ? (unsigned)ctas : 0u;
+}
+
 // Every entry point of the C ABI is a function-try-block closed by this
 // handler: no C++ exception crosses the ABI, the caller gets BKMA_ERR_HOST.
 #define BKMA_ABI_CATCH(fn) \

@@ -193,7 +193,7 @@ bkma_status run_torch_plain(ConvPlanImpl &p, void *data, void *out, const void *
     const size_t smem = sizeof(T) * (size_t)(d.cin * (p.TL + d.ksize - 1));
     BKMA_CUDA_TRY(cudaFuncSetAttribute(conv_torch_plain<T>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    conv_torch_plain<T><<<(unsigned)(d.batch * p.ntiles), 256, smem, st>>>(a);
+    conv_torch_plain<T><<<grid_x(d.batch * p.ntiles), 256, smem, st>>>(a);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
 }
@@ -224,7 +224,7 @@ bkma_status run_reference(ConvPlanImpl &p, void *data, void *out, const void *w,
     BKMA_CUDA_TRY(cudaFuncSetAttribute(conv_ref_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
     const int64_t ncb = (d.n2 + a.W - 1) / a.W;
-    conv_ref_kernel<<<(unsigned)(d.batch * ncb), 256, smem, st>>>(a);
+    conv_ref_kernel<<<grid_x(d.batch * ncb), 256, smem, st>>>(a);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
 }

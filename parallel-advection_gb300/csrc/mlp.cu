@@ -301,7 +301,7 @@ bkma_status launch_grad(MlpImpl &M, const float *alpha, const float *taps4, cons
     BKMA_CUDA_TRY(cudaFuncSetAttribute(mlp::fwd_bwd_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
     const int64_t blocks = (batch + mlp::TB - 1) / mlp::TB;
-    mlp::fwd_bwd_kernel<<<(unsigned)blocks, mlp::TB, kFwdSmem, st>>>(
+    mlp::fwd_bwd_kernel<<<grid_x(blocks), mlp::TB, kFwdSmem, st>>>(
         M.d_params, alpha, taps4, target, n, batch, pick_seed, pick, M.d_grad, M.d_loss);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
@@ -354,7 +354,7 @@ bkma_status bkma_mlp_samples(int64_t n, uint64_t seed, int64_t first, float *alp
                              float *target, void *stream) try {
     BKMA_CHECK_ARG(n > 0 && alpha && taps4 && target && first >= 0, "bad arguments");
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
-    mlp::samples_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(n, seed, first, alpha,
+    mlp::samples_kernel<<<grid_x(blocks), 256, 0, (cudaStream_t)stream>>>(n, seed, first, alpha,
                                                                            taps4, target);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
@@ -415,7 +415,7 @@ bkma_status bkma_mlp_infer(const bkma_mlp *mlp, const float *alpha, int64_t n, f
                            void *stream) try {
     BKMA_CHECK_ARG(mlp && alpha && weights && n > 0, "bad arguments");
     const int64_t blocks = std::min<int64_t>((n + 127) / 128, 152 * 8);
-    mlp::infer_kernel<<<(unsigned)blocks, 128, 0, (cudaStream_t)stream>>>(mlp->impl.d_params, alpha,
+    mlp::infer_kernel<<<grid_x(blocks), 128, 0, (cudaStream_t)stream>>>(mlp->impl.d_params, alpha,
                                                                          n, weights);
     BKMA_CUDA_TRY(cudaGetLastError());
     return BKMA_OK;
