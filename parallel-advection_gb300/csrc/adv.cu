@@ -564,6 +564,13 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
     }
     BKMA_CHECK_ARG(d.maxX > d.minX, "maxX must exceed minX");
     BKMA_CHECK_ARG(std::isfinite(d.dt), "dt must be finite");
+    BKMA_CHECK_ARG(std::isfinite(d.minX) && std::isfinite(d.maxX) && std::isfinite(d.minVx) &&
+                       std::isfinite(d.maxVx),
+                   "minX, maxX, minVx and maxVx must be finite");
+    // a NaN foot point would reach floor() and an int conversion
+    if (d.velocity)
+        for (int64_t l = 0; l < count; ++l)
+            BKMA_CHECK_ARG(std::isfinite(d.velocity[l]), "velocity values must be finite");
 
     // owned here until complete: an early return or an exception frees it
     std::unique_ptr<bkma_adv_plan> pl(new bkma_adv_plan);

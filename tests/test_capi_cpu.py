@@ -58,6 +58,8 @@ def test_impl_selector_unknown_name_message(bkma):
     (dict(maxX=-1.0), "maxX"),
     (dict(n0=2**31), "n0 must be < 2^31"),
     (dict(n0=2**28, n1=2**16, n2=2**8), "2^50"),
+    (dict(maxVx=float("inf")), "must be finite"),
+    (dict(velocity=[0.1] * 7 + [float("nan")]), "velocity values must be finite"),
 ])
 def test_adv_descriptor_validation(bkma, kw, msg):
     args = dict(n0=8, n1=64, n2=3)
