@@ -16,10 +16,13 @@ first length-kernel+1 values per line (`result`).
 Each benchmark runs `repetitions` times; like google-benchmark with
 --benchmark_repetitions it reports every repetition and the _mean, _median,
 _stddev and _cv aggregates, with items_per_second = cells per second and
-bytes_per_second = 2 x element size x cells per second.
+bytes_per_second = 2 x element size x cells per second. With
+--report-aggregates-only it writes the aggregates alone, as the reference's
+diag/launch_benchmarks.sh runs its benchmarks: the input diag/utils.py reads.
 
   python -m bkma_gb300.harness [--out sweep.json] [--dtype f64|f32]
                                [--repetitions 3] [--only adv|conv] [--sizes 0,5,9]
+                               [--report-aggregates-only]
 """
 from __future__ import annotations
 
@@ -79,6 +82,17 @@ def aggregate(runs: list[dict]) -> list[dict]:
             e["aggregate_unit"] = "percentage"
         out.append(e)
     return out
+
+
+def report(benches: list[dict], aggregates_only: bool) -> list[dict]:
+    """The records written out: all of them, or only the aggregates, as
+    google-benchmark's --benchmark_report_aggregates_only=true (which
+    diag/launch_benchmarks.sh:61 passes) writes them. diag/utils.py:88-155
+    (clean_raw_df) reads that form: it drops the _mean records and takes the
+    rest as (_median, _stddev, _cv) triples of one benchmark."""
+    if not aggregates_only:
+        return benches
+    return [b for b in benches if b.get("run_type") == "aggregate"]
 
 
 def entry(run_name: str, rep: int, reps: int, iterations: int, seconds: float, items: float,
@@ -207,6 +221,9 @@ def main(argv=None) -> int:
                     help="device time per advection repetition")
     ap.add_argument("--only", choices=["adv", "conv"], default=None)
     ap.add_argument("--sizes", default=None, help="comma list of EXP_SIZES indices")
+    ap.add_argument("--report-aggregates-only", action="store_true",
+                    help="write only the aggregate records (google-benchmark's "
+                         "--benchmark_report_aggregates_only; the input of diag/utils.py)")
     a = ap.parse_args(argv)
     import torch
 
@@ -219,7 +236,7 @@ def main(argv=None) -> int:
         benches += advection_sweep(bkma, dev, a.dtype, a.repetitions, a.min_seconds, sizes)
     if a.only in (None, "conv"):
         benches += conv_sweep(bkma, dev, a.repetitions)
-    doc = {"context": context(), "benchmarks": benches}
+    doc = {"context": context(), "benchmarks": report(benches, a.report_aggregates_only)}
     doc["context"]["wall_seconds"] = round(time.perf_counter() - t0, 3)
     with open(a.out, "w") as f:
         json.dump(doc, f, indent=1)

@@ -33,6 +33,41 @@ def test_records_and_aggregates():
     assert {"date", "host_name", "num_cpus", "library_build_type"} <= set(harness.context())
 
 
+def _clean_raw_df_groups(benches):
+    """The record filter and grouping of the reference's diag/utils.py
+    clean_raw_df (:88-155), restated without pandas: drop _mean and
+    BM_WgSize records, then read the rest three at a time as a benchmark's
+    _median, _stddev and _cv, with the fields it uses."""
+    rows = [b for b in benches
+            if not b["name"].endswith("_mean") and not b["name"].startswith("BM_WgSize")]
+    assert len(rows) % 3 == 0
+    groups = [rows[i:i + 3] for i in range(0, len(rows), 3)]
+    for g in groups:
+        assert [r["name"].rsplit("_", 1)[1] for r in g] == ["median", "stddev", "cv"]
+        assert len({r["name"].split("_")[0] for r in g}) == 1
+        for r in g:
+            for k in ("kernel_id", "n0", "n1", "n2", "items_per_second", "real_time", "gpu"):
+                assert k in r, (r["name"], k)
+    return groups
+
+
+def test_aggregates_only_report_reads_like_the_reference_diag():
+    benches = []
+    for impl in (0, 1):
+        for w in (128, 1024):
+            name = f"main-BKM-bench/1/{impl}/3/{w}/1/1/real_time"
+            runs = [harness.entry(name, r, 3, 10, 1.0 + r, 1e9, 4, {}) for r in range(3)]
+            for r in runs:
+                r.update({"gpu": 1, "n0": 8, "n1": 16, "n2": 1, "kernel_id": impl})
+            benches += runs + harness.aggregate(runs)
+    groups = _clean_raw_df_groups(harness.report(benches, aggregates_only=True))
+    assert len(groups) == 4
+    # with the per-repetition records the reference's grouping breaks: the
+    # reason for --report-aggregates-only
+    with pytest.raises(AssertionError):
+        _clean_raw_df_groups(harness.report(benches, aggregates_only=False))
+
+
 @pytest.mark.skipif(not os.path.isdir(REF), reason="reference checkout not available")
 def test_shapes_are_the_references():
     src = open(os.path.join(REF, "bench_config.hpp")).read()
