@@ -161,3 +161,48 @@ def test_host_array_checks_need_no_device(bkma):
         with pytest.raises(bkma.BkmaError) as e:
             plan.run_host(bad)
         assert e.value.status == 1 and "(4, 16, 2)" in str(e.value)
+
+
+_C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "bkma_gb300.h"
+
+int main(void) {
+    int32_t impl = -1, inplace = -1;
+    bkma_adv_plan *plan = NULL;
+    bkma_adv_desc d;
+    if (bkma_abi_version() != BKMA_ABI_VERSION) return 1;
+    if (bkma_impl_from_name("AdaptiveWg", &impl, &inplace) != BKMA_OK) return 2;
+    if (impl != BKMA_ADV_STAGED || inplace != 1) return 3;
+    if (bkma_impl_from_name("Hierarchical", &impl, &inplace) != BKMA_ERR_UNSUPPORTED) return 4;
+    if (strstr(bkma_last_error(), "not a valid implementation name") == NULL) return 5;
+    memset(&d, 0, sizeof d);
+    d.n0 = 0; /* invalid: refused before any device work */
+    if (bkma_adv_plan_create(&d, &plan) != BKMA_ERR_INVALID_ARG || plan != NULL) return 6;
+    printf("ok\n");
+    return 0;
+}
+"""
+
+
+def test_header_is_c_and_links_from_c(bkma, tmp_path):
+    """include/bkma_gb300.h compiles as C99 (-Wall -Werror -pedantic) and a C
+    program links against the library and calls the entry points that need
+    no GPU, with the documented statuses."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from bkma_gb300 import _lib
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    src = tmp_path / "caller.c"
+    src.write_text(_C_CALLER)
+    exe = tmp_path / "caller"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                    "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                    "-L", libdir, "-lbkma_gb300", f"-Wl,-rpath,{libdir}"],
+                   check=True, capture_output=True, text=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
