@@ -52,4 +52,4 @@ def test_reference_arm_under_torchrun_two_ranks():
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1, r.stdout[-2000:]
     d = json.loads(lines[0])
-    assert d["impl"] == "reference" and d["value"] > 0
+    assert d["impl"] == "reference" and d["value"] > 0 and d["n_gpus"] == 2
