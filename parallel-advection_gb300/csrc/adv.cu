@@ -603,23 +603,17 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
             e = cudaMemcpy(p.d_vx, p.vx.data(), sizeof(double) * p.lines, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) s = cuda_fail(e, "plan tables");
     }
-    if (s != BKMA_OK) {
-        return s;
-    }
+    if (s != BKMA_OK) return s;
     {
         cudaError_t e = cudaMalloc(&p.d_status, sizeof(int));
         if (e == cudaSuccess) e = cudaMemset(p.d_status, 0, sizeof(int));
-        if (e != cudaSuccess) {
-            return cuda_fail(e, "plan status word");
-        }
+        if (e != cudaSuccess) return cuda_fail(e, "plan status word");
     }
     default_tile(p);
     // the staged kernel runs every line, or (streamed form) the exception lines
     const bool too_long = p.path == 2 ? (p.n_exc > 0 && p.exc_tile_w(kMaxSmem) == 0)
                                       : p.smem_bytes(p.W, p.R) > kMaxSmem;
-    if (too_long) {
-        return fail(BKMA_ERR_UNSUPPORTED, "n1 too long for a shared-memory line tile");
-    }
+    if (too_long) return fail(BKMA_ERR_UNSUPPORTED, "n1 too long for a shared-memory line tile");
     *plan = pl.release();
     return BKMA_OK;
 } BKMA_ABI_CATCH("bkma_adv_plan_create")

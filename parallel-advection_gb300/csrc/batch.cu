@@ -340,13 +340,9 @@ bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields,
         b.cells += f.n0 * f.n1 * f.n2;
     }
     cudaError_t e = cudaMalloc(&b.d_counter, sizeof(unsigned long long));
-    if (e != cudaSuccess) {
-        return cuda_fail(e, "batch counter");
-    }
+    if (e != cudaSuccess) return cuda_fail(e, "batch counter");
     bkma_status s = rebuild(b, nullptr);
-    if (s != BKMA_OK) {
-        return s;
-    }
+    if (s != BKMA_OK) return s;
     *batch = bb.release();
     return BKMA_OK;
 } BKMA_ABI_CATCH("bkma_adv_batch_create")

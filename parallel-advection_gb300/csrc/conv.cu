@@ -282,9 +282,7 @@ bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **p
             if (e != cudaSuccess) s = cuda_fail(e, "conv halo scratch");
         }
     }
-    if (s != BKMA_OK) {
-        return s;
-    }
+    if (s != BKMA_OK) return s;
     *plan = pl.release();
     return BKMA_OK;
 } BKMA_ABI_CATCH("bkma_conv_plan_create")

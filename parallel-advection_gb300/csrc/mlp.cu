@@ -333,9 +333,7 @@ bkma_status bkma_mlp_create(uint64_t seed, bkma_mlp **out) try {
     if (e == cudaSuccess) e = cudaMemset(M.d_grad, 0, sizeof(float) * mlp::NP);
     if (e == cudaSuccess) e = cudaMemset(M.d_m, 0, sizeof(float) * mlp::NP);
     if (e == cudaSuccess) e = cudaMemset(M.d_v, 0, sizeof(float) * mlp::NP);
-    if (e != cudaSuccess) {
-        return cuda_fail(e, "bkma_mlp_create");
-    }
+    if (e != cudaSuccess) return cuda_fail(e, "bkma_mlp_create");
     *out = m.release();
     return BKMA_OK;
 } BKMA_ABI_CATCH("bkma_mlp_create")
