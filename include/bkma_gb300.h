@@ -157,6 +157,16 @@ bkma_status bkma_adv_plan_line_table(const bkma_adv_plan *plan, int32_t *offsets
 /* Synchronizes `stream`, returns the device status of the kernels' bounded
  * waits since the last query (BKMA_OK or BKMA_ERR_TIMEOUT) and clears it. */
 bkma_status bkma_adv_plan_status(bkma_adv_plan *plan, void *stream);
+/* Polls of each bounded device-side wait before it gives up (default
+ * 4194304: with the kernels' back-off, about half a second to a second).
+ * 0 makes every such wait give up at once: the launch then stops its tiles
+ * without writing them, waits (with the default bound) for its own copies in
+ * flight, and bkma_adv_plan_status reports BKMA_ERR_TIMEOUT - a way to test a
+ * caller's timeout handling without a stuck GPU. Applies to the TMA-staged
+ * kernel (the only advection kernel with a device-side wait). The reference
+ * has no device-side waits; its errors are C++ exceptions
+ * (src/core/bkma_tools.hpp:38-51). */
+bkma_status bkma_adv_plan_set_wait_limit(bkma_adv_plan *plan, uint32_t polls);
 bkma_status bkma_adv_plan_destroy(bkma_adv_plan *plan);
 
 /* bkma_run for the advection solver: nsteps time steps of the device field
@@ -252,6 +262,12 @@ bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const voi
  * kernel's bounded waits since the last query (BKMA_OK or BKMA_ERR_TIMEOUT),
  * then clears it. */
 bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream);
+/* Polls of each bounded wait of the tensor-core kernel's pipeline before it
+ * gives up (default 4194304, about a second); 0 makes the first wait of every
+ * role give up at once, so the call stops, drains the MMAs it issued, frees
+ * its tensor memory and bkma_conv_plan_status reports BKMA_ERR_TIMEOUT. For
+ * testing a caller's timeout handling; no counterpart in the reference. */
+bkma_status bkma_conv_plan_set_wait_limit(bkma_conv_plan *plan, uint32_t polls);
 bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan);
 
 /* fill_buffer_conv1d (src/tools/init.hpp:50-72): `count` elements of a
@@ -269,19 +285,27 @@ bkma_status bkma_conv_check(const void *data, int32_t dtype, int64_t n0, int64_t
  * data (batch, channels, length), weight (channels, channels, ksize), bias
  * (channels) or NULL) that allocates nothing. No counterpart in the
  * reference: it exists for callers that must not call cudaMalloc while they
- * run - code recorded into a replayable stream capture, runtimes that give all
- * device memory to their own pool at start-up, and loops that cannot afford
- * an allocation's implicit synchronization. Its scratch is one 16 MiB device
+ * run - runtimes that give all device memory to their own pool at start-up
+ * and forbid further driver allocations, and loops that cannot afford an
+ * allocation's implicit synchronization. Its scratch is one 16 MiB device
  * array inside the library (held by every GPU that loads it until exit):
  * 512 KiB for packed weights and 15.5 MiB for the halo snapshot, which keeps
  * one slot per chunk of consecutive tiles (at most 3840 slots of
  * channels * 2 * max(8, round_up(ksize-1, 8)) bytes: at most 15 MiB for every
- * shape the tensor path takes), so no batch or length is limited by it. The first call on a device looks the array's address up,
- * so make it before any stream capture. Calls share the array: calls that
- * overlap on the GPU race, and a device-side wait timeout is not reported. */
+ * shape the tensor path takes), so no batch or length is limited by it; a
+ * shape that would need more is refused with BKMA_ERR_INVALID_ARG. The
+ * arguments obey the same bounds as bkma_conv_plan_create. The first call on
+ * a device looks the array's address up, so make it before any stream
+ * capture. Calls share the array, which keeps the last call's contents:
+ * calls that overlap on the GPU race. */
 bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *weight, const void *bias,
                                              int64_t batch, int64_t channels, int64_t length,
                                              int64_t ksize, void *stream);
+/* Status of the last bkma_conv1d_bf16_inplace_noalloc call on the current
+ * device: synchronizes `stream`, returns BKMA_OK or BKMA_ERR_TIMEOUT (a
+ * bounded device-side wait gave up, so the output is incomplete) and clears
+ * it. Allocates nothing. No counterpart in the reference. */
+bkma_status bkma_conv1d_noalloc_status(void *stream);
 
 /* ------------------------------------------------------- learned stencil */
 /* A small MLP (1 -> 32 -> 32 -> 4, GELU, FP32) maps a line's fractional shift

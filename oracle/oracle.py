@@ -31,6 +31,20 @@ def build(force: bool = False) -> str:
     return ORACLE_SO
 
 
+def reference_dir() -> str | None:
+    """The reference checkout's root: BKMA_REFERENCE_DIR when set, else the
+    directory build_ref.sh compiled from (recorded in _ref/reference_dir.txt),
+    else None (no checkout on this machine)."""
+    env = os.environ.get("BKMA_REFERENCE_DIR")
+    if env:
+        return env if os.path.isdir(env) else None
+    rec = os.path.join(HERE, "_ref", "reference_dir.txt")
+    if os.path.exists(rec):
+        d = open(rec).read().strip()
+        return d if os.path.isdir(d) else None
+    return None
+
+
 def build_ref() -> str | None:
     """Compile the reference's solver/config sources (only where they exist)."""
     subprocess.run([os.path.join(HERE, "build_ref.sh")], check=True,

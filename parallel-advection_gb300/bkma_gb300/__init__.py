@@ -154,6 +154,10 @@ class AdvectionPlan:
         """Raise if a bounded device wait timed out since the last query."""
         check(load().bkma_adv_plan_status(self._h, _stream(stream)))
 
+    def set_wait_limit(self, polls: int):
+        """Polls of each bounded device wait before it gives up (0: at once)."""
+        check(load().bkma_adv_plan_set_wait_limit(self._h, polls))
+
     def set_fusion(self, steps_per_launch: int):
         """Time steps per kernel launch (shared-memory strips; 1 = off)."""
         check(load().bkma_adv_plan_set_fusion(self._h, steps_per_launch))
@@ -428,6 +432,10 @@ class Conv1dPlan:
     def status(self, stream=None):
         """Raise if a bounded device wait of the tensor kernel timed out."""
         check(load().bkma_conv_plan_status(self._h, _stream(stream)))
+
+    def set_wait_limit(self, polls: int):
+        """Polls of each bounded device wait before it gives up (0: at once)."""
+        check(load().bkma_conv_plan_set_wait_limit(self._h, polls))
 
     def close(self):
         if getattr(self, "_h", None):

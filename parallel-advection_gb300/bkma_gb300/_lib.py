@@ -77,6 +77,7 @@ SIGNATURES = {
     "bkma_adv_plan_set_weights": (_st, [_vp, _vp, C.c_int32]),
     "bkma_adv_plan_line_table": (_st, [_vp, _i32p, _dp]),
     "bkma_adv_plan_status": (_st, [_vp, _vp]),
+    "bkma_adv_plan_set_wait_limit": (_st, [_vp, C.c_uint32]),
     "bkma_adv_plan_destroy": (_st, [_vp]),
     "bkma_adv_step": (_st, [_vp, _vp, _vp, C.c_int32, _vp]),
     "bkma_adv_run_host": (_st, [_vp, _vp, C.c_int32, _vp]),
@@ -93,12 +94,14 @@ SIGNATURES = {
     "bkma_conv_plan_scratch_bytes": (_st, [_vp, _i64p]),
     "bkma_conv_run": (_st, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "bkma_conv_plan_status": (_st, [_vp, _vp]),
+    "bkma_conv_plan_set_wait_limit": (_st, [_vp, C.c_uint32]),
     "bkma_conv_plan_destroy": (_st, [_vp]),
     "bkma_fill": (_st, [_vp, C.c_int64, C.c_int32, C.c_double, _vp]),
     "bkma_conv_check": (_st, [_vp, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64, _dp,
                               _i32p, _vp]),
     "bkma_conv1d_bf16_inplace_noalloc": (_st, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64,
                                                C.c_int64, _vp]),
+    "bkma_conv1d_noalloc_status": (_st, [_vp]),
     "bkma_mlp_create": (_st, [C.c_uint64, C.POINTER(_vp)]),
     "bkma_mlp_params": (_st, [_vp, _vp, C.c_int32]),
     "bkma_mlp_samples": (_st, [C.c_int64, C.c_uint64, C.c_int64, _vp, _vp, _vp, _vp]),

@@ -22,7 +22,12 @@ diag/launch_benchmarks.sh runs its benchmarks: the input diag/utils.py reads.
 
   python -m bkma_gb300.harness [--out sweep.json] [--dtype f64|f32]
                                [--repetitions 3] [--only adv|conv] [--sizes 0,5,9]
+                               [--conv-configs 0,3] [--max-cells N]
                                [--report-aggregates-only]
+
+--max-cells caps an advection shape's n0 so that n0 x n1 x n2 <= N (the
+record keeps the reference's n0 as n0_full); --conv-configs picks conv
+configs by index.
 """
 from __future__ import annotations
 
@@ -133,14 +138,15 @@ def _timed(fn, min_seconds: float, max_iters: int) -> tuple[int, float]:
 
 
 def advection_sweep(bkma, dev, dtype: str, reps: int, min_seconds: float,
-                    sizes=None) -> list[dict]:
+                    sizes=None, max_cells: int | None = None) -> list[dict]:
     import torch
     tdt = torch.float64 if dtype == "f64" else torch.float32
     es = 8 if dtype == "f64" else 4
     out = []
-    for idx, (n0, n1, n2) in enumerate(EXP_SIZES):
+    for idx, (n0_full, n1, n2) in enumerate(EXP_SIZES):
         if sizes is not None and idx not in sizes:
             continue
+        n0 = n0_full if max_cells is None else max(1, min(n0_full, max_cells // (n1 * n2)))
         t0 = time.perf_counter()
         plan = bkma.AdvectionPlan(n0, n1, n2, dtype=dtype, dt=0.001, minX=0.0, maxX=1.0,
                                   minVx=-1.0, maxVx=1.0)
@@ -161,7 +167,8 @@ def advection_sweep(bkma, dev, dtype: str, reps: int, min_seconds: float,
                 plan.status()
                 err, _ = plan.validate(data, steps)
                 for r in runs:
-                    r.update({"gpu": 1, "n0": n0, "n1": n1, "n2": n2, "kernel_id": impl,
+                    r.update({"gpu": 1, "n0": n0, "n1": n1, "n2": n2, "n0_full": n0_full,
+                              "kernel_id": impl,
                               "pref_wg_size": w, "seq_size0": 1, "seq_size2": 1, "err": err,
                               "dtype": dtype, "path": info["path"],
                               "exception_lines": info["exception_lines"],
@@ -173,12 +180,14 @@ def advection_sweep(bkma, dev, dtype: str, reps: int, min_seconds: float,
     return out
 
 
-def conv_sweep(bkma, dev, reps: int) -> list[dict]:
+def conv_sweep(bkma, dev, reps: int, configs=None) -> list[dict]:
     """ConvSolver semantics, FP64 (the reference's real_t)."""
     import torch
     tdt = torch.float64
     out = []
     for idx, (batch, length, k, ch) in enumerate(CONV_CONFIGS):
+        if configs is not None and idx not in configs:
+            continue
         n0, n1, n2 = batch, length * ch, 1
         plan = bkma.Conv1dPlan(n0, ch, ch, length, k, dtype="f64", semantics="reference",
                                n2=n2)
@@ -221,6 +230,9 @@ def main(argv=None) -> int:
                     help="device time per advection repetition")
     ap.add_argument("--only", choices=["adv", "conv"], default=None)
     ap.add_argument("--sizes", default=None, help="comma list of EXP_SIZES indices")
+    ap.add_argument("--conv-configs", default=None, help="comma list of conv config indices")
+    ap.add_argument("--max-cells", type=int, default=None,
+                    help="cap n0 of an advection shape so that it has at most this many cells")
     ap.add_argument("--report-aggregates-only", action="store_true",
                     help="write only the aggregate records (google-benchmark's "
                          "--benchmark_report_aggregates_only; the input of diag/utils.py)")
@@ -230,12 +242,14 @@ def main(argv=None) -> int:
     import bkma_gb300 as bkma
     dev = torch.device("cuda", 0)
     sizes = None if a.sizes is None else {int(s) for s in a.sizes.split(",")}
+    confs = None if a.conv_configs is None else {int(s) for s in a.conv_configs.split(",")}
     benches = []
     t0 = time.perf_counter()
     if a.only in (None, "adv"):
-        benches += advection_sweep(bkma, dev, a.dtype, a.repetitions, a.min_seconds, sizes)
+        benches += advection_sweep(bkma, dev, a.dtype, a.repetitions, a.min_seconds, sizes,
+                                   a.max_cells)
     if a.only in (None, "conv"):
-        benches += conv_sweep(bkma, dev, a.repetitions)
+        benches += conv_sweep(bkma, dev, a.repetitions, confs)
     doc = {"context": context(), "benchmarks": report(benches, a.report_aggregates_only)}
     doc["context"]["wall_seconds"] = round(time.perf_counter() - t0, 3)
     with open(a.out, "w") as f:

@@ -648,6 +648,12 @@ bkma_status bkma_adv_plan_status(bkma_adv_plan *plan, void *stream) try {
     return BKMA_OK;
 } BKMA_ABI_CATCH("bkma_adv_plan_status")
 
+bkma_status bkma_adv_plan_set_wait_limit(bkma_adv_plan *plan, uint32_t polls) try {
+    BKMA_CHECK_ARG(plan, "null argument");
+    plan->impl.wait_polls = polls;
+    return BKMA_OK;
+} BKMA_ABI_CATCH("bkma_adv_plan_set_wait_limit")
+
 bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *field, void *stream) try {
     BKMA_CHECK_ARG(plan && field, "null argument");
     return adv_autotune(plan->impl, field, (cudaStream_t)stream);

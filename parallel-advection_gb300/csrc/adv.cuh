@@ -67,6 +67,7 @@ struct AdvTmaArgs {
     const int32_t *exc_index;  // [lines]
     const AdvExcCell<float> *exc;
     int *status;               // device status word (BKMA_ERR_TIMEOUT on a stuck copy)
+    uint32_t spin_limit;       // polls of the staging barrier before the CTA gives up
 };
 
 struct AdvPlainArgs {

@@ -47,6 +47,7 @@ struct AdvPlanImpl {
     };
     std::vector<TmapCache> tmaps;  // TMA descriptors of recently used fields
     int *d_status = nullptr;       // device status word of the bounded waits
+    uint32_t wait_polls = kWaitPolls;  // polls of a bounded device wait before it gives up
     // host-run buffer, and bkma_adv_run_host's pipeline: sub-plans over slab
     // chunks (lines are independent) on four streams, so the copies of one
     // chunk overlap the time steps of another

@@ -29,7 +29,23 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-constexpr uint32_t kTmaSpinLimit = 1u << 22;
+constexpr uint32_t kTmaSpinLimit = kWaitPolls;
+
+// Polls the staging barrier's phase 0 at most `polls` times.
+__device__ __forceinline__ bool tile_wait(uint64_t *bar, uint32_t polls) {
+    for (uint32_t i = 0; i < polls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+            " selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(smem_addr(bar))
+            : "memory");
+        if (done) return true;
+        if (i > 32) __nanosleep(128);
+    }
+    return false;
+}
 
 template <int NT, int WC>
 __global__ void __launch_bounds__(512) adv_tma_f32(const __grid_constant__ CUtensorMap tmap,
@@ -79,23 +95,16 @@ __global__ void __launch_bounds__(512) adv_tma_f32(const __grid_constant__ CUten
         const float wk = a.w[line * NT + k];
         w2[k] = make_float2(wk, wk);
     }
-    bool ok = false;
-    for (uint32_t i = 0; i < kTmaSpinLimit; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
-            " selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(smem_addr(&bar))
-            : "memory");
-        if (done) {
-            ok = true;
-            break;
-        }
-        if (i > 32) __nanosleep(128);
-    }
+    // Every thread polls the barrier at most a.spin_limit times; the CTA then
+    // agrees on one outcome. On a timeout the status word is raised and the
+    // issuing thread stays until its copies have landed (a second bounded
+    // wait), so that no copy writes into shared memory the CTA has left.
+    const bool ok = __syncthreads_and(tile_wait(&bar, a.spin_limit));
     if (!ok) {
-        if (threadIdx.x == 0) atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
+        if (threadIdx.x == 0) {
+            atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
+            tile_wait(&bar, kTmaSpinLimit);
+        }
         return;
     }
     // wrap halo: rows n1 .. n1+NT-2 repeat rows 0 .. NT-2
@@ -228,6 +237,7 @@ cudaError_t adv_tma_launch(AdvPlanImpl &p, const void *src, void *dst, int W, in
     a.exc_index = p.d_exc_index;
     a.exc = (const AdvExcCell<float> *)p.d_exc;
     a.status = p.d_status;
+    a.spin_limit = p.wait_polls;
     const size_t smem = adv_tma_smem(p, W);
     const int64_t grid = p.lines * a.ncb;
     if (p.npts == 6) {

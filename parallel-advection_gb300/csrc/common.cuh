@@ -33,6 +33,11 @@ void *tensor_map_encoder();
         if (!(cond)) return ::bkma::fail(BKMA_ERR_INVALID_ARG, msg);         \
     } while (0)
 
+// Polls of a bounded device-side wait before it gives up (with the kernels'
+// back-off, roughly half a second to a second): plans start with this limit,
+// bkma_adv_plan_set_wait_limit / bkma_conv_plan_set_wait_limit change it.
+constexpr uint32_t kWaitPolls = 1u << 22;
+
 // x dimension of a 1-D launch: 0 (a launch error, "invalid configuration")
 // when the CTA count is above the 2^31 - 1 limit, never a silently truncated
 // grid that would leave tiles unprocessed.

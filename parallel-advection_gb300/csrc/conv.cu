@@ -230,14 +230,8 @@ bkma_status run_reference(ConvPlanImpl &p, void *data, void *out, const void *w,
 }
 
 }  // namespace
-}  // namespace bkma
 
-extern "C" {
-
-bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **plan) try {
-    BKMA_CHECK_ARG(desc && plan, "bkma_conv_plan_create: null argument");
-    *plan = nullptr;
-    const bkma_conv_desc &d = *desc;
+bkma_status conv_check_desc(const bkma_conv_desc &d) {
     BKMA_CHECK_ARG(d.batch > 0 && d.cin > 0 && d.cout > 0 && d.length > 0 && d.ksize > 0,
                    "batch, cin, cout, length, ksize must be positive");
     BKMA_CHECK_ARG(d.ksize <= d.length, "ksize must not exceed length");
@@ -245,6 +239,8 @@ bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **p
                    "unknown semantics");
     BKMA_CHECK_ARG(d.impl >= BKMA_CONV_AUTO && d.impl <= BKMA_CONV_PLAIN, "unknown impl");
     BKMA_CHECK_ARG(d.cin < 65536 && d.cout < 65536 && d.ksize < 4096, "channel count or ksize too large");
+    // the kernels index rows and tiles with 32-bit fields
+    BKMA_CHECK_ARG(d.batch < (1ll << 31) && d.length < (1ll << 40), "batch or length too large");
     if (d.semantics == BKMA_CONV_REFERENCE) {
         BKMA_CHECK_ARG(d.cout == d.cin, "reference semantics force channel_out = channel_in");
         BKMA_CHECK_ARG(d.dtype == BKMA_F64, "reference semantics run in FP64");
@@ -256,6 +252,19 @@ bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **p
                        "dtype must be F64, F32 or BF16");
         if (d.inplace) BKMA_CHECK_ARG(d.cin == d.cout, "in place needs cin == cout");
     }
+    return BKMA_OK;
+}
+
+}  // namespace bkma
+
+extern "C" {
+
+bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **plan) try {
+    BKMA_CHECK_ARG(desc && plan, "bkma_conv_plan_create: null argument");
+    *plan = nullptr;
+    const bkma_conv_desc &d = *desc;
+    bkma_status cs = conv_check_desc(d);
+    if (cs != BKMA_OK) return cs;
     // owned here until complete: an early return or an exception frees it
     std::unique_ptr<bkma_conv_plan> pl(new bkma_conv_plan);
     ConvPlanImpl &p = pl->impl;
@@ -322,6 +331,12 @@ bkma_status bkma_conv_plan_status(bkma_conv_plan *plan, void *stream) try {
     if (st != 0) return fail((bkma_status)st, "tensor-core conv1d: a bounded device wait timed out");
     return BKMA_OK;
 } BKMA_ABI_CATCH("bkma_conv_plan_status")
+
+bkma_status bkma_conv_plan_set_wait_limit(bkma_conv_plan *plan, uint32_t polls) try {
+    BKMA_CHECK_ARG(plan, "null argument");
+    plan->impl.wait_polls = polls;
+    return BKMA_OK;
+} BKMA_ABI_CATCH("bkma_conv_plan_set_wait_limit")
 
 bkma_status bkma_conv_plan_destroy(bkma_conv_plan *plan) try {
     delete plan;

@@ -46,6 +46,7 @@ struct ConvPlanImpl {
     void *d_wpack = nullptr;  // weights packed for the tensor path
     size_t wpack_bytes = 0;
     void *d_status = nullptr; // device status word of the tensor kernel
+    uint32_t wait_polls = kWaitPolls;  // polls of a bounded device wait before it gives up
     int grid = 0;
     ~ConvPlanImpl() {
         cudaFree(d_halo);
@@ -54,6 +55,9 @@ struct ConvPlanImpl {
     }
 };
 
+// Argument checks shared by every conv1d entry point (bounds that keep the
+// kernels' int fields in range, semantics, dtype).
+bkma_status conv_check_desc(const bkma_conv_desc &d);
 bkma_status conv_halo_prepass(ConvPlanImpl &p, const void *x, cudaStream_t st);
 bkma_status conv_tc_scratch_need(const bkma_conv_desc &d, size_t *halo_bytes, size_t *wpack_bytes);
 bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w, const void *bias,

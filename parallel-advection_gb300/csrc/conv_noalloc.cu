@@ -1,14 +1,13 @@
 // Allocation-free entry point for the in-place BF16 tensor-core conv1d.
 //
-// Some callers cannot call cudaMalloc while they run: code inside a stream
-// capture that must stay replayable, runtimes that hand all device memory to
-// their own pool at start-up and forbid further driver allocations, and
-// latency-critical loops where an allocation (and the implicit device
-// synchronization cudaFree brings) is not allowed. The plan-based
-// bkma_conv_run needs plan-owned scratch (the halo snapshot and the packed
-// weights), which bkma_conv_plan_create allocates. This entry point instead
-// uses one file-scope device array, reserved when the library is loaded and
-// held by every GPU that loads it until the process exits.
+// Some callers cannot call cudaMalloc while they run: runtimes that hand all
+// device memory to their own pool at start-up and forbid further driver
+// allocations, and latency-critical loops where an allocation (and the
+// implicit device synchronization that cudaFree brings) is not allowed. The
+// plan-based bkma_conv_run needs plan-owned scratch (the halo snapshot and
+// the packed weights), which bkma_conv_plan_create allocates. This entry
+// point instead uses one file-scope device array, reserved when the library
+// is loaded and held by every GPU that loads it until the process exits.
 //
 // The array's name is only a host-side stand-in in host code; its device
 // address is looked up once per device (cudaGetSymbolAddress, with that device
@@ -16,6 +15,7 @@
 // capture. All calls share the array: it keeps the last call's contents, the
 // status word is cleared at every call, and calls that overlap on the GPU
 // (different streams, or different host threads on the same device) race on it.
+// bkma_conv1d_noalloc_status reads the status word of the last call.
 #include <array>
 #include <mutex>
 #include <string>
@@ -64,9 +64,6 @@ extern "C" bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *
                                                         int64_t channels, int64_t length,
                                                         int64_t ksize, void *stream) try {
     BKMA_CHECK_ARG(data && weight, "bkma_conv1d_bf16_inplace_noalloc: null data or weight");
-    BKMA_CHECK_ARG(batch > 0 && channels > 0 && length > 0 && ksize > 0 && ksize <= length,
-                   "bkma_conv1d_bf16_inplace_noalloc: need batch, channels, length > 0 and "
-                   "0 < ksize <= length");
     bkma_conv_desc d{};
     d.batch = batch;
     d.cin = channels;
@@ -78,8 +75,10 @@ extern "C" bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *
     d.semantics = BKMA_CONV_TORCH;
     d.impl = BKMA_CONV_TENSOR;
     d.inplace = 1;
+    bkma_status s = conv_check_desc(d);  // the same bounds as bkma_conv_plan_create
+    if (s != BKMA_OK) return s;
     size_t halo_bytes = 0, wpack_bytes = 0;
-    bkma_status s = conv_tc_scratch_need(d, &halo_bytes, &wpack_bytes);
+    s = conv_tc_scratch_need(d, &halo_bytes, &wpack_bytes);
     if (s != BKMA_OK) return s;
     if (halo_bytes > kHaloMax || wpack_bytes > kWpackMax)
         return fail(BKMA_ERR_INVALID_ARG,
@@ -98,3 +97,18 @@ extern "C" bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *
     BKMA_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
     return conv_tc_run_into(d, data, weight, bias, base + kHaloOff, base + kWpackOff, status, st);
 } BKMA_ABI_CATCH("bkma_conv1d_bf16_inplace_noalloc")
+
+extern "C" bkma_status bkma_conv1d_noalloc_status(void *stream) try {
+    unsigned char *base = nullptr;
+    bkma_status s = scratch_address(&base);
+    if (s != BKMA_OK) return s;
+    BKMA_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    int *status = reinterpret_cast<int *>(base + kStatusOff);
+    int v = 0;
+    BKMA_CUDA_TRY(cudaMemcpy(&v, status, sizeof(int), cudaMemcpyDeviceToHost));
+    BKMA_CUDA_TRY(cudaMemset(status, 0, sizeof(int)));
+    if (v != 0)
+        return fail((bkma_status)v,
+                    "bkma_conv1d_bf16_inplace_noalloc: a bounded device wait timed out");
+    return BKMA_OK;
+} BKMA_ABI_CATCH("bkma_conv1d_noalloc_status")

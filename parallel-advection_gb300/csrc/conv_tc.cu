@@ -68,7 +68,7 @@ constexpr int NUM_EPI_WARPS = 4;
 constexpr int NUM_PROD_WARPS = 8;  // two groups of 4 warps, alternate items
 constexpr int PROD_GROUP = 128;    // threads per producer group
 constexpr int THREADS = 32 * (NUM_EPI_WARPS + NUM_PROD_WARPS + 1);
-constexpr uint32_t kSpinLimit = 1u << 22;  // x ~ 0.25 us backoff: ~1 s
+constexpr uint32_t kSpinLimit = kWaitPolls;  // x ~ 0.25 us backoff: ~1 s
 constexpr int MAX_CTAS = 1024;             // grid cap
 constexpr int CHUNK_TILES = 64;            // preferred tiles per chunk
 constexpr int MAX_SLOTS = 3840;            // halo snapshot slots (chunks) per call: <= 15 MiB
@@ -102,6 +102,8 @@ struct Args {
     int epi_tma;     // 1 or 2: the epilogue stores through out_map from 1 or 2 tiles per warp
     int epi_off;     // offset of the epilogue tiles (after the stages)
     int *status;     // device status word (0 ok, 4 timeout)
+    uint32_t spin_limit;  // polls of a pipeline wait before the CTA gives up (the final
+                          // drain of the MMAs always uses kSpinLimit)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -126,11 +128,12 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait. Returns false (and raises the CTA abort flag) on timeout, or
-// when another thread already aborted.
+// Bounded wait (at most `polls` polls of the barrier). Returns false (and
+// raises the CTA abort flag) on timeout, or when another thread already
+// aborted.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
-                                          int *status) {
-    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+                                          int *status, uint32_t polls) {
+    for (uint32_t i = 0; i < polls; ++i) {
         if (mbar_try(bar, parity)) return true;
         if (*abort_flag) return false;
         if (i > 64) __nanosleep(256);
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             if ((it & 1) != grp) continue;
             const int s = it % stages;
             const uint32_t ph = (uint32_t)(it / stages) & 1u;
-            if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_flag, a.status)) break;
+            if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_flag, a.status, a.spin_limit)) break;
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
             unsigned char *stage = stages_sm + (size_t)s * a.stage_bytes;
@@ -508,10 +511,10 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             BKMA_TC_FOR_ITEMS {
                 const int s = it % stages;
                 const uint32_t ph = (uint32_t)(it / stages) & 1u;
-                if (!mbar_wait(&full_bar[s], ph, &abort_flag, a.status)) break;
+                if (!mbar_wait(&full_bar[s], ph, &abort_flag, a.status, a.spin_limit)) break;
                 const int acc = a.nacc == 2 ? (it & 1) : 0;
                 const uint32_t aph = (uint32_t)(a.nacc == 2 ? (it >> 1) : it) & 1u;
-                if (!mbar_wait(&acce_bar[acc], aph ^ 1u, &abort_flag, a.status)) break;
+                if (!mbar_wait(&acce_bar[acc], aph ^ 1u, &abort_flag, a.status, a.spin_limit)) break;
                 fence_after();
                 const uint32_t d_tmem = tmem + (uint32_t)(a.tm_cols + acc * TILE);
                 // descriptor low word: start address >> 4 (bits 0-13, < 256 KB so
@@ -554,7 +557,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             const int tile = (int)(item % a.ntiles);
             const int acc = a.nacc == 2 ? (it & 1) : 0;
             const uint32_t aph = (uint32_t)(a.nacc == 2 ? (it >> 1) : it) & 1u;
-            if (!mbar_wait(&accf_bar[acc], aph, &abort_flag, a.status)) break;
+            if (!mbar_wait(&accf_bar[acc], aph, &abort_flag, a.status, a.spin_limit)) break;
             fence_after();
             const int64_t l0 = (int64_t)tile * TILE;
             // The tensor map ends at lt = lout rounded down to 8 positions (a
@@ -777,7 +780,7 @@ size_t tc_halo_bytes(const bkma_conv_desc &d, int halo_rows) {
 // one slot per chunk), grid = min(sms, items, MAX_CTAS).
 bkma_status tc_launch(const bkma_conv_desc &d, const void *data, void *out, int64_t out_stride,
                       const void *w, const void *bias, void *halo, void *wpack, int *status,
-                      int64_t ntiles, int sms, cudaStream_t st) {
+                      int64_t ntiles, int sms, uint32_t wait_polls, cudaStream_t st) {
     TcLayout t = tc_layout(d, true);
     tc::Args a;
     memset(&a, 0, sizeof(a));
@@ -826,6 +829,7 @@ bkma_status tc_launch(const bkma_conv_desc &d, const void *data, void *out, int6
     a.wpack_tmem = tm_img;
     a.wpack_smem = reinterpret_cast<const uint4 *>(sm_img);
     a.status = status;
+    a.spin_limit = wait_polls;
     void (*kern)(const tc::Args) = nullptr;
     switch (a.cin / 16) {
     case 1: kern = tc::conv_tc_kernel<1>; break;
@@ -883,7 +887,7 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
         return fail(BKMA_ERR_INVALID_ARG, "tensor path: data, out and weight must be 16-byte aligned");
     return tc_launch(d, data, inplace ? data : out, inplace ? d.length : d.length - d.ksize + 1, w,
                      bias, (inplace && d.ksize > 1) ? p.d_halo : nullptr, p.d_wpack,
-                     (int *)p.d_status, p.ntiles, p.grid, st);
+                     (int *)p.d_status, p.ntiles, p.grid, p.wait_polls, st);
 }
 
 }  // namespace bkma
@@ -891,7 +895,8 @@ bkma_status conv_tc_run(ConvPlanImpl &p, void *data, void *out, const void *w, c
 namespace bkma {
 
 // Scratch needs of the tensor path for one in-place call: the halo snapshot
-// (one slot per CTA) and the packed weights (bytes, each rounded to 256).
+// (one slot per chunk of tiles, at most MAX_SLOTS) and the packed weights
+// (bytes, each rounded to 256).
 bkma_status conv_tc_scratch_need(const bkma_conv_desc &d, size_t *halo_bytes, size_t *wpack_bytes) {
     if (d.cout > 128 || d.cin > 128 || d.cin % 16 != 0 || d.length % 8 != 0)
         return fail(BKMA_ERR_UNSUPPORTED,
@@ -918,7 +923,7 @@ bkma_status conv_tc_run_into(const bkma_conv_desc &d, void *data, const void *w,
     BKMA_CUDA_TRY(cudaGetDevice(&dev));
     BKMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     return tc_launch(d, data, data, d.length, w, bias, d.ksize > 1 ? halo : nullptr, wpack, status,
-                     ntiles, sms, st);
+                     ntiles, sms, kWaitPolls, st);
 }
 
 }  // namespace bkma

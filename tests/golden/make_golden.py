@@ -1,7 +1,8 @@
 """Generate the golden fixtures in tests/golden/ from the reference's OWN code.
 
-Runs only where the reference checkout exists (default /root/reference, or
-BKMA_REFERENCE_DIR): it builds oracle/_ref/libbkma_ref.so (the reference's
+Runs only where the reference checkout exists (BKMA_REFERENCE_DIR, or the
+directory oracle/build_ref.sh found it in): it builds
+oracle/_ref/libbkma_ref.so (the reference's
 AdvectionSolver, ConvSolver, ConfigMap/ADVParams/Conv1dParams compiled on the
 CPU with oracle/ref_shim) and records what that code outputs. The committed
 .npz/.json files are what tests/test_oracle_golden.py checks the oracle
@@ -22,9 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from oracle import AdvParams, Reference, build_ref  # noqa: E402
-
-REF_DIR = os.environ.get("BKMA_REFERENCE_DIR", "/root/reference")
+from oracle import AdvParams, Reference, build_ref, reference_dir  # noqa: E402
 
 # INI texts exercising the reference parser: strtof rounding of reals,
 # base-0 strtol (hex), ';' inline comments vs '#' kept in values,
@@ -91,7 +90,8 @@ inplace = true
 
 def main():
     so = build_ref()
-    if not so:
+    REF_DIR = reference_dir()
+    if not so or not REF_DIR:
         raise SystemExit("reference sources not found; cannot regenerate fixtures")
     ref = Reference(so)
     out_json = {}

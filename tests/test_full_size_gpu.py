@@ -12,7 +12,13 @@ not need the oracle to run the whole field:
   FP32 conv1d (TF32 off) on the same BF16 inputs, and the last K - 1 samples
   of every row untouched;
 - the 64-field uneven batch of the batched workload (about 4e9 cells): after
-  the batch autotuner, every field has the bits of its own single plan."""
+  the batch autotuner, every field has the bits of its own single plan;
+- the advection workload's error target over its 50 steps, against the plain
+  FP64 kernel (the reference's per-cell math, bit-exact with the oracle) from
+  the same FP32-representable field: with the FP32 hi + lo state fused over
+  the 50 steps (one FP32 rounding of the field), max |err| / max |f| <= 1e-6;
+  one step per launch (FP32 rounding every step) within its documented
+  bound, 8e-8 per step (8e-7 at 10 steps, 4e-6 at 50)."""
 import numpy as np
 import pytest
 
@@ -129,4 +135,42 @@ def test_batched_full_size(bkma, cuda):
         bkma.AdvectionPlan(n0, n1, n2, dtype="f32", **kw).step(d0, nsteps=STEPS)
         assert torch.equal(f["data"], d0), (n0, n1, n2, f["degree"])
     del fields, init, batch
+    _release()
+
+
+def test_advection_50_step_error_targets(bkma, cuda):
+    import torch
+    vel = -1.0 + 2.0 * np.arange(N0, dtype=np.float64) / (N0 - 1)
+    kw = dict(dt=DT, minX=0.0, maxX=1.0, minVx=-1.0, maxVx=1.0, velocity=vel)
+    plain = bkma.AdvectionPlan(N0, N1, N2, dtype="f64", impl="plain", **kw)
+    ref = torch.empty((N0, N1, N2), dtype=torch.float64, device=cuda)
+    plain.fill(ref, mode=1, amp=0.01, seed=12345)
+    f0 = ref.float()
+    ref.copy_(f0)
+    ref10 = ref.clone()
+    plain.step(ref10, nsteps=10)
+    plain.step(ref, nsteps=50)
+    plain.status()
+
+    one = bkma.AdvectionPlan(N0, N1, N2, dtype="f32", **kw)
+    fused = bkma.AdvectionPlan(N0, N1, N2, dtype="f32", **kw)
+    fused.set_fused_state("f32x2")
+    fused.set_fusion(50)
+    x = f0.clone()
+    fused.step(x, nsteps=50)
+    fused.status()
+    nx = one.error_norms(x, ref)
+    assert nx["max_rel"] <= 1e-6, nx
+    assert nx["l2_rel"] <= 1e-7, nx
+
+    x.copy_(f0)
+    one.step(x, nsteps=10)
+    n10 = one.error_norms(x, ref10)
+    assert n10["max_rel"] <= 8e-8 * 10, n10
+    one.step(x, nsteps=40)
+    one.status()
+    n50 = one.error_norms(x, ref)
+    assert n50["max_rel"] <= 8e-8 * 50, n50
+    assert n50["l2_rel"] <= 1e-6, n50
+    del ref, ref10, f0, x
     _release()

@@ -8,7 +8,9 @@ import pytest
 
 from bkma_gb300 import harness
 
-REF = os.path.join(os.environ.get("BKMA_REFERENCE_DIR", "/root/reference"), "benchmark")
+from oracle import reference_dir
+
+REF = os.path.join(reference_dir() or "", "benchmark")
 
 
 def test_records_and_aggregates():
@@ -68,7 +70,7 @@ def test_aggregates_only_report_reads_like_the_reference_diag():
         _clean_raw_df_groups(harness.report(benches, aggregates_only=False))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference checkout not available")
+@pytest.mark.skipif(reference_dir() is None, reason="reference checkout not available")
 def test_shapes_are_the_references():
     src = open(os.path.join(REF, "bench_config.hpp")).read()
 

@@ -10,7 +10,6 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = json.load(open(os.path.join(ROOT, "tests", "golden", "params.json")))
-REF_DIR = os.environ.get("BKMA_REFERENCE_DIR", "/root/reference")
 
 
 @pytest.fixture(scope="module")
@@ -46,7 +45,9 @@ def test_ini_cases_match_reference(params_bin, tmp_path, case):
 
 @pytest.mark.parametrize("name,kind", [("advection.ini", "adv"), ("conv1d.ini", "conv")])
 def test_reference_ini_files(params_bin, name, kind):
-    path = os.path.join(REF_DIR, "src", name)
+    from oracle import reference_dir
+    ref = reference_dir()
+    path = os.path.join(ref, "src", name) if ref else ""
     if not os.path.exists(path):
         pytest.skip("reference checkout not available")
     _compare(_parse(params_bin, kind, path), GOLDEN[name])

@@ -1,10 +1,10 @@
 """The allocation-free conv1d entry point, called through the C ABI.
 
 bkma_conv1d_bf16_inplace_noalloc serves callers that must not allocate device
-memory while they run (replayable stream captures, runtimes that own the whole
-device heap, allocation-free loops); it keeps its scratch in a fixed device
-array inside the library. This file is collected last so that a run stopping
-at the first failure has already run every other test.
+memory while they run (runtimes that own the whole device heap, loops that
+cannot afford an allocation's implicit synchronization); it keeps its scratch
+in a fixed device array inside the library. This file is collected last so
+that a run stopping at the first failure has already run every other test.
 
 Its output must equal the plan-based entry point's (bkma_conv_run): the same
 kernels run in the same order, so the check is exact; the tensor-path
@@ -58,8 +58,52 @@ def test_noalloc_matches_plan_entry_point_twice(bkma, cuda, oracle):
         assert err <= 1e-2 * np.abs(ref).max()
 
 
+def test_noalloc_allocates_nothing(bkma, cuda):
+    """After the first call (which looks the array's address up and loads the
+    kernels), repeated calls change neither the device's free memory nor the
+    torch allocator's counters, and the status call reports each call OK."""
+    import torch
+    lib = bkma.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    B, Ch, L, K = 4, 128, 2048, 7
+    x, w, b = _inputs(cuda, 21, B, Ch, L, K)
+    assert _noalloc(lib, x.clone(), w, b, stream) == 0, lib.bkma_last_error().decode()
+    assert lib.bkma_conv1d_noalloc_status(C.c_void_p(stream)) == 0
+    bufs = [x.clone() for _ in range(3)]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats()
+    for buf in bufs:
+        assert _noalloc(lib, buf, w, b, stream) == 0, lib.bkma_last_error().decode()
+        assert lib.bkma_conv1d_noalloc_status(C.c_void_p(stream)) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = torch.cuda.memory_stats()
+    assert free1 == free0, (free0, free1)
+    for k in ("allocation.all.allocated", "segment.all.allocated", "allocated_bytes.all.current"):
+        assert stats1.get(k, 0) == stats0.get(k, 0), k
+    assert torch.equal(bufs[0], bufs[1]) and torch.equal(bufs[1], bufs[2])
+
+
+def test_noalloc_refuses_out_of_bounds_arguments(bkma, cuda):
+    """The same argument bounds as the plan entry point: a huge ksize is refused
+    before anything runs, not truncated to a small one."""
+    import torch
+    lib = bkma.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    x, w, b = _inputs(cuda, 5, 1, 16, 8192, 3)
+    got = lib.bkma_conv1d_bf16_inplace_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
+                                               C.c_void_p(b.data_ptr()), 1, 16, 8192,
+                                               (1 << 32) + 3, C.c_void_p(stream))
+    assert got == 1, got  # BKMA_ERR_INVALID_ARG
+    got = lib.bkma_conv1d_bf16_inplace_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
+                                               C.c_void_p(b.data_ptr()), 1, 16, 8192, 5000,
+                                               C.c_void_p(stream))
+    assert got == 1, got
+
+
 def test_noalloc_large_batch_matches_plan(bkma, cuda):
-    """The halo snapshot keeps one slot per CTA, so a batch whose per-tile
+    """The halo snapshot keeps one slot per chunk of tiles, so a batch whose per-tile
     snapshot would not have fit the fixed array (160 rows x 64 tiles x 128
     channels x 16 bytes = 21 MB > 15.5 MiB) runs and equals bkma_conv_run."""
     import torch
