@@ -51,8 +51,15 @@ typedef enum bkma_dtype { BKMA_F32 = 0, BKMA_F64 = 1, BKMA_BF16 = 2 } bkma_dtype
  * "ndrange", "adaptivewg" (the reference's two live strategies), "basicrange"
  * (out of place), "plain" (per-cell FP64 reference math), "staged" and
  * "gb300"/"cuda" (the per-line staged kernel). */
+/* AUTO and STAGED run the fastest kernel for the shape. For FP64 fields that
+ * is, wherever the shape allows it (degree 3 or 5, even n2 >= 4, n1 >= 16,
+ * lines that fit shared memory, a 16-byte aligned field), the kernel that
+ * keeps FP64 in HBM but sums the stencil in FP32-pair arithmetic (GB300's
+ * FP64 rate would otherwise bound the step near 100 GCells/s): it agrees with
+ * FP64 arithmetic to about 2e-13 max|f| per step. bkma_adv_plan_set_tile
+ * with path 0 selects the FP64-arithmetic staged kernel. */
 typedef enum bkma_adv_impl {
-    BKMA_ADV_AUTO = 0,   /* staged kernel, autotuned tile */
+    BKMA_ADV_AUTO = 0,   /* staged kernels, autotuned tile */
     BKMA_ADV_STAGED = 1, /* per-line FP64 departure + weights, lines staged in shared memory */
     BKMA_ADV_PLAIN = 2   /* per-cell FP64 reference math (AdvectionSolver.hpp:71-99); FP64 only */
 } bkma_adv_impl;
@@ -94,7 +101,8 @@ typedef struct bkma_adv_plan_info {
     int32_t autotuned;         /* 1 once bkma_adv_plan_autotune picked the tile */
     int64_t tiles;             /* CTAs per step */
     int32_t path;              /* 0: cp.async staging, 1: TMA (cp.async.bulk.tensor) staging,
-                                  2: streamed columns, 3: contiguous lines (n2 = 1) */
+                                  2: streamed columns, 3: contiguous lines (n2 = 1),
+                                  4: FP64 in FP32-pair arithmetic (TMA staging) */
     int32_t reserved;
 } bkma_adv_plan_info;
 
@@ -123,14 +131,18 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * field's size, k = up to k segments per 32-column group, k <= 8) and W the
  * tile width of the staged pass over exception lines, or path 3: contiguous
  * lines (FP32, n2 = 1, n1 % 4 == 0, n1 >= 16; W = 1, R whole lines per CTA,
- * `threads` ignored: 256). R <= 1024 on paths 0, 1 and 3. */
+ * `threads` ignored: 256), or path 4: FP64 in FP32-pair arithmetic (FP64,
+ * degree 3 or 5, even n2 >= W, n1 >= 16; W = 4 with 128 threads or W = 8 with
+ * 256, R = 1; a field off the 16-byte grid runs the FP64 staged kernel on the
+ * same tiles). R <= 1024 on paths 0, 1 and 3. */
 bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
                                    int32_t path);
 /* Multi-step fusion: bkma_adv_step runs `steps_per_launch` time steps per
  * kernel launch on column strips held in shared memory (the last launch of
  * a call runs the remainder), 1 = one step per launch (default). Results
- * are bit-identical to one step per launch; HBM traffic per cell-step falls
- * by the factor. Out of place, `data` is left unchanged. Not for the plain
+ * are bit-identical to one step per launch of the staged kernels (FP32; for
+ * FP64 the FP64-arithmetic staged kernel, path 0); HBM traffic per cell-step
+ * falls by the factor. Out of place, `data` is left unchanged. Not for the plain
  * FP64 form; BKMA_ERR_UNSUPPORTED when a strip of the plan's n1 rows does
  * not fit shared memory, and for FP32 lines longer than 4608 rows (the strips
  * would hold one column: slower than one step per launch). No counterpart in the reference, which runs one

@@ -197,6 +197,16 @@ void default_tile(AdvPlanImpl &p) {
         p.R = adv_rows_default_r(p);
         p.threads = 256;  // the contiguous-line kernel's fixed CTA
     }
+    if (adv_ds_shape_ok(p, 4) && adv_ds_smem(p, 4) <= kMaxSmem) {
+        // FP64 storage in FP32-pair arithmetic (GB300's FP64 rate bounds the
+        // FP64 staged kernel near 100 GCells/s): 4-column TMA tiles, six CTAs
+        // of 128 threads per SM (2048 x 1024 x 512: 301 GCells/s; 8-column
+        // tiles, three CTAs of 256 threads: 289)
+        p.path = 4;
+        p.W = 4;
+        p.R = 1;
+        p.threads = adv_ds_threads(4);  // the FP32-pair kernel's CTA for the width
+    }
 }
 
 template <typename T>
@@ -214,6 +224,19 @@ bkma_status upload_tables(AdvPlanImpl &p) {
     BKMA_CUDA_TRY(cudaMemcpy(p.d_exc_index, p.exc_index.data(), sizeof(int32_t) * L,
                              cudaMemcpyHostToDevice));
     BKMA_CUDA_TRY(cudaMemcpy(p.d_vx, p.vx.data(), sizeof(double) * L, cudaMemcpyHostToDevice));
+    if (sizeof(T) == 8 && p.desc.impl != BKMA_ADV_PLAIN) {
+        // FP32-pair weights of the FP64 kernel in FP32-pair arithmetic (adv_ds.cu):
+        // w = a + b + r, a = RN32(w), b = RN32(w - a), |r| <= 2^-48 |w|
+        std::vector<float2> w2((size_t)(L * NT));
+        for (int64_t i = 0; i < L * NT; ++i) {
+            const double wd = p.w64[(size_t)i];
+            const float a = (float)wd;
+            w2[(size_t)i] = make_float2(a, (float)(wd - (double)a));
+        }
+        BKMA_CUDA_TRY(cudaMalloc(&p.d_w2, sizeof(float2) * (size_t)(L * NT)));
+        BKMA_CUDA_TRY(cudaMemcpy(p.d_w2, w2.data(), sizeof(float2) * (size_t)(L * NT),
+                                 cudaMemcpyHostToDevice));
+    }
     if (p.n_exc > 0) {
         std::vector<int32_t> lst;
         for (int64_t l = 0; l < L; ++l)
@@ -313,6 +336,9 @@ cudaError_t launch_plain(const AdvPlanImpl &p, const double *src, double *dst, i
 
 cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R, int threads,
                         int path, cudaStream_t st) {
+    // FP32-pair FP64 kernel; a field off the 16-byte grid takes the FP64
+    // staged kernel on the same 8-column tiles
+    if (path == 4 && adv_ds_eligible(p, src, W)) return adv_ds_launch(p, src, dst, W, st);
     if (path == 1 && R == 1 && adv_tma_eligible(p, src, W))
         return adv_tma_launch(p, src, dst, W, threads, st);
     if (path == 2 && p.stream_ok) {
@@ -463,11 +489,17 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
         }
     }
     // The plan's own tile is the first candidate, so tuning never ends on a
-    // tile slower than the default.
+    // tile slower than the default. An FP64 plan on the FP32-pair kernel
+    // (path 4) keeps it: the other FP64 kernels round differently, and
+    // tuning must not change results.
     std::vector<TuneVal> cands{{p.W, p.R, p.threads, p.path}};
     const int64_t n2 = p.desc.n2;
     const int ths[3] = {128, 256, 512};
-    if (n2 >= 8) {
+    if (p.path == 4) {
+        // the other tile width of the same kernel (same arithmetic per cell)
+        for (int W : {4, 8})
+            if (W != p.W && adv_ds_shape_ok(p, W)) cands.push_back({W, 1, adv_ds_threads(W), 4});
+    } else if (n2 >= 8) {
         for (int W : {8, 16, 32, 64})
             if (W <= n2 || W == 8)
                 for (int t : ths) {
@@ -475,16 +507,17 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
                     if (adv_tma_eligible(p, field, W)) cands.push_back({W, 1, t, 1});
                 }
     }
-    if (p.stream_ok)
+    const bool other = p.path != 4;
+    if (p.stream_ok && other)
         for (int segs : {0, 1, 2, 4, 8}) cands.push_back({(int)std::min<int64_t>(16, n2), segs, 256, 2});
     for (int R : {1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024})
-        if (n2 < 32 && R <= p.lines && p.smem_bytes((int)n2, R) <= kMaxSmem)
+        if (other && n2 < 32 && R <= p.lines && p.smem_bytes((int)n2, R) <= kMaxSmem)
             for (int t : ths) cands.push_back({(int)n2, R, t, 0});
     // whole-row tiles of a few slabs for wider rows of short lines
     for (int R : {1, 2, 4, 8, 16})
-        if (n2 >= 32 && n2 <= 256 && R <= p.lines && p.smem_bytes((int)n2, R) <= 96 * 1024)
+        if (other && n2 >= 32 && n2 <= 256 && R <= p.lines && p.smem_bytes((int)n2, R) <= 96 * 1024)
             for (int t : ths) cands.push_back({(int)n2, R, t, 0});
-    if (adv_rows_shape_ok(p))
+    if (other && adv_rows_shape_ok(p))
         for (int R = 1; R <= 4096 && R <= p.lines; R *= 2)
             if (adv_rows_eligible(p, field, field, R)) cands.push_back({1, R, 256, 3});
     cudaEvent_t e0, e1;
@@ -494,6 +527,7 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     TuneVal bestv{p.W, p.R, p.threads, p.path};
     for (const TuneVal &c : cands) {
         const size_t need = c.path == 1 ? adv_tma_smem(p, c.W)
+                            : c.path == 4 ? adv_ds_smem(p, c.W)
                             : c.path == 2 ? 0
                             : c.path == 3 ? adv_rows_smem(p, c.R) : p.smem_bytes(c.W, c.R);
         if (need > kMaxSmem) continue;
@@ -627,6 +661,7 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
     info->tile_slabs = p.R;
     info->threads = p.threads;
     info->smem_bytes = (int32_t)(p.path == 1   ? adv_tma_smem(p, p.W)
+                                 : p.path == 4 ? adv_ds_smem(p, p.W)
                                  : p.path == 2 ? adv_stream_smem()
                                  : p.path == 3 ? adv_rows_smem(p, p.R)
                                                : p.smem_bytes(p.W, p.R));
@@ -666,7 +701,7 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
     BKMA_CHECK_ARG(W >= 1 && W <= 1024 && R >= (path == 2 ? 0 : 1) && R <= 1024,
                    "W must be in [1,1024], R in [1,1024] (path 2: row-segment mode 0..8)");
     BKMA_CHECK_ARG(threads == 128 || threads == 256 || threads == 512, "threads must be 128, 256 or 512");
-    BKMA_CHECK_ARG(path >= 0 && path <= 3, "path must be 0, 1, 2 or 3");
+    BKMA_CHECK_ARG(path >= 0 && path <= 4, "path must be 0, 1, 2, 3 or 4");
     BKMA_CHECK_ARG(path != 2 || p.stream_ok, "streamed form not available for this plan");
     BKMA_CHECK_ARG(path >= 2 || R == 1 || W >= p.desc.n2, "R > 1 needs whole-row tiles (W >= n2)");
     BKMA_CHECK_ARG(path != 2 || R <= 8, "path 2: R is the row-segment mode, 0 (auto) to 8");
@@ -680,6 +715,12 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
         BKMA_CHECK_ARG(adv_rows_shape_ok(p) && W == 1 && adv_rows_smem(p, R) <= kMaxSmem,
                        "path 3 needs an FP32 plan with n2 = 1, n1 % 4 == 0, n1 >= 16, "
                        "W = 1 and R lines that fit shared memory");
+    } else if (path == 4) {
+        BKMA_CHECK_ARG(adv_ds_shape_ok(p, W) && adv_ds_smem(p, W) <= kMaxSmem && R == 1 &&
+                           threads == adv_ds_threads(W),
+                       "path 4 needs an FP64 plan of degree 3 or 5 with an even n2 >= W, n1 >= 16, "
+                       "lines that fit shared memory, W = 4 (128 threads) or 8 (256 threads) "
+                       "and R = 1");
     }
     p.W = W;
     p.R = R;

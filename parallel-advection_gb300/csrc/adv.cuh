@@ -70,6 +70,22 @@ struct AdvTmaArgs {
     uint32_t spin_limit;       // polls of the staging barrier before the CTA gives up
 };
 
+// FP64-storage kernel with FP32-pair arithmetic (adv_ds.cu): 8-column TMA
+// tiles of one slab.
+struct AdvDsArgs {
+    double *dst;
+    int64_t n1, n2;
+    int64_t ncb;               // 8-column blocks per slab
+    int box_rows, nbox;        // TMA boxes of box_rows rows cover n1
+    const int32_t *base;       // [lines]
+    const double *w;           // [lines][NT] FP64 weights (FP64 tiles)
+    const float2 *w2;          // [lines][NT] (a, b): w = a + b, a = RN32(w), b = RN32(w - a)
+    const int32_t *exc_index;  // [lines], or null when the plan has no exception lines
+    const AdvExcCell<double> *exc;
+    int *status;
+    uint32_t spin_limit;
+};
+
 struct AdvPlainArgs {
     const double *src;
     double *dst;

@@ -1,0 +1,334 @@
+// FP64-storage advection computed in FP32-pair ("double-single") arithmetic.
+//
+// GB300 runs FP64 FMAs at a small fraction of its FP32 rate: the staged FP64
+// kernel (one DMUL + NT-1 DFMA per cell) tops out near 100 GCells/s, a quarter
+// of what HBM allows at 16 B per cell-step. This kernel keeps the field in
+// FP64 in HBM and forms each cell's sum_k w_k f_k from FP32 pieces:
+//
+//  * staging: one CTA = one slab i0 x 8 columns (64-byte rows) x all n1 rows,
+//    copied by TMA (cp.async.bulk.tensor, FP64 tensor map) into shared memory;
+//  * split: a thread walks a run of consecutive rows of one column pair and
+//    splits every tap it loads once, into a register ring of npts pairs:
+//    x = h + l, h = x's leading 24 bits (truncated; integer operations on the
+//    bit pattern), l = the remaining 29 bits rounded to 24 (one
+//    integer-to-float conversion and a power-of-two scale), so
+//    |x - (h + l)| <= 2^-48 |x|; zeros split exactly. A cell pair with a tap
+//    outside [2^-74, 2^126) in magnitude (or a subnormal, inf, NaN) is
+//    computed in FP64 from the staged doubles (the staged kernel's
+//    arithmetic, same bits), as are lines whose departure offset varies along
+//    n1 (per-cell stencils);
+//  * per tap, with the line's weight w = a + b split the same way on the
+//    host: p = a h (rounded) and e = a h - p (exact, one FMA), summed with
+//    TwoSum into (S, err) so that S + sum(err) is the exact sum of the p; the
+//    small terms e, err, a l and b h accumulate in three FP32 partial sums
+//    (b l is below 2^-48 of the term and dropped);
+//  * output: (y, y') = Fast2Sum(S, L), widened to FP64 with integer operations
+//    and added with one DADD (correct rounding of the pair), one 16-byte
+//    store per column pair.
+//
+// The sum is within a few 2^-48 of sum_k |w_k f_k| of the FP64 direct form:
+// against the staged FP64 kernel the result differs by at most ~2e-13 max|f|
+// per step. One step reads and writes each cell once (16 B per cell-step); the
+// tile is read completely before the first store, so in place is legal.
+#include <cuda.h>
+
+#include <algorithm>
+
+#include "adv.cuh"
+#include "adv_device.cuh"
+#include "adv_plan.cuh"
+#include "common.cuh"
+#include "tma.cuh"
+
+namespace bkma {
+
+namespace {
+
+// A tile is WC FP64 columns (8: 64-byte rows, 4: 32-byte rows) x all n1 rows;
+// a CTA has kDsRuns runs of rows per column pair: 32 * WC threads.
+constexpr int kDsRuns = 64;
+template <int WC> constexpr int ds_threads() { return kDsRuns * WC / 2; }
+
+// |x| in [2^-74, 2^126), or +-0: the split below is exact to 2^-48 |x| and
+// every intermediate FP32 value stays normal and finite.
+__device__ __forceinline__ bool ds_splittable(double x) {
+    const uint32_t xh = (uint32_t)__double2hiint(x), xl = (uint32_t)__double2loint(x);
+    const uint32_t e = (xh >> 20) & 0x7FFu;
+    return (e - 949u < 200u) || (e == 0u && ((xh & 0xFFFFFu) | xl) == 0u);
+}
+
+// x = h + l + r, |r| <= 2^-48 |x| (x splittable). h keeps x's sign, exponent
+// and leading 23 stored mantissa bits; l is the rest, the low 29 bits times
+// 2^(E-52), rounded to 24 bits.
+__device__ __forceinline__ void ds_split(double x, float &h, float &l) {
+    const uint32_t xh = (uint32_t)__double2hiint(x), xl = (uint32_t)__double2loint(x);
+    const uint32_t sign = xh & 0x80000000u;
+    const uint32_t e = (xh >> 20) & 0x7FFu;
+    // exponent rebased from 1023 to 127 in place, then the 8-bit exponent and
+    // 23 mantissa bits moved up by 3 (the sign bit is restored after)
+    const uint32_t hb = __funnelshift_l(xl, xh - (896u << 20), 3) | sign;
+    const float lo = __uint2float_rn(xl & 0x1FFFFFFFu) * __uint_as_float(((e - 948u) << 23) | sign);
+    h = e ? __uint_as_float(hb) : __uint_as_float(sign);
+    l = e ? lo : 0.0f;
+}
+
+// FP32 -> FP64 by moving the bits, with no FP64-pipe conversion. A subnormal
+// (below 2^-126, which only a pair part of an output far smaller than the
+// tile's values can be: every input is >= 2^-74 or zero) becomes +-0, an
+// error below 2^-52 of the smallest nonzero input.
+__device__ __forceinline__ double ds_widen(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t mag = u & 0x7FFFFFFFu;
+    const bool normal = mag >= 0x00800000u;
+    const uint32_t hi = (normal ? (mag >> 3) + (896u << 20) : 0u) | (u & 0x80000000u);
+    return __hiloint2double((int)hi, normal ? (int)(mag << 29) : 0);
+}
+
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+
+// Split both doubles of a column pair into v = (h0, h1, l0, l1); false when
+// either value is outside the split's range.
+__device__ __forceinline__ bool ds_split2(double2 x, float4 &v) {
+    ds_split(x.x, v.x, v.z);
+    ds_split(x.y, v.y, v.w);
+    return ds_splittable(x.x) && ds_splittable(x.y);
+}
+
+// sum_k w_k x_k of a column pair from its NT split taps T[(u + k) % NT]
+// (u: ring position of tap 0); two FP64 results. The high products a h are
+// summed exactly (TwoSum into s plus error terms); the low-order terms go to
+// three independent FP32 accumulators (a l, b h, and the product and sum
+// errors), so no dependence chain is longer than two operations per tap.
+template <int NT>
+__device__ __forceinline__ double2 ds_stencil(const float4 (&T)[NT], int u, const float2 (&A)[NT],
+                                              const float2 (&B)[NT]) {
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    float2 s, La, Lb, Le;
+    {
+        const float4 v = T[u % NT];
+        const float2 h = make_float2(v.x, v.y), l = make_float2(v.z, v.w);
+        s = __fmul2_rn(h, A[0]);
+        Le = __ffma2_rn(h, A[0], neg2(s));  // exact error of the product
+        La = __fmul2_rn(l, A[0]);
+        Lb = __fmul2_rn(h, B[0]);
+    }
+#pragma unroll
+    for (int k = 1; k < NT; ++k) {
+        const float4 v = T[(u + k) % NT];
+        const float2 h = make_float2(v.x, v.y), l = make_float2(v.z, v.w);
+        const float2 p = __fmul2_rn(h, A[k]);
+        const float2 e = __ffma2_rn(h, A[k], neg2(p));
+        La = __ffma2_rn(l, A[k], La);
+        Lb = __ffma2_rn(h, B[k], Lb);
+        // TwoSum(s, p): t + (ea + eb) = s + p exactly
+        const float2 t = __fadd2_rn(s, p);
+        const float2 bv = __ffma2_rn(s, m1, t);   // t - s
+        const float2 av = __ffma2_rn(bv, m1, t);  // t - bv
+        const float2 eb = __ffma2_rn(bv, m1, p);  // p - bv
+        const float2 ea = __ffma2_rn(av, m1, s);  // s - av
+        Le = __fadd2_rn(Le, __fadd2_rn(e, __fadd2_rn(ea, eb)));
+        s = t;
+    }
+    const float2 L = __fadd2_rn(__fadd2_rn(La, Lb), Le);
+    // Fast2Sum(s, L): |s| >= |L|
+    const float2 y = __fadd2_rn(s, L);
+    const float2 yl = __ffma2_rn(__ffma2_rn(s, m1, y), m1, L);  // L - (y - s)
+    return make_double2(__dadd_rn(ds_widen(y.x), ds_widen(yl.x)),
+                        __dadd_rn(ds_widen(y.y), ds_widen(yl.y)));
+}
+
+// Rows per thread run of a CTA with `runs` runs over n1 rows.
+__host__ __device__ __forceinline__ int ds_run_rows(int64_t n1, int runs) {
+    return (int)((n1 + runs - 1) / runs);
+}
+
+// One row of a thread's run: load and split the ring's newest tap (slot
+// (u + NT - 1) % NT, row P[NT - 1] of this output's window), then the
+// output pair from the window's taps. A tap outside the split's range sets
+// `bad` (the pair is then redone in FP64 after the run).
+template <int NT, int TPR>
+__device__ __forceinline__ void ds_row(const double2 *P, int u, float4 (&T)[NT], bool &bad,
+                                       const float2 (&A)[NT], const float2 (&B)[NT], double *G) {
+    const int sn = (u + NT - 1) % NT;
+    bad |= !ds_split2(P[(NT - 1) * TPR], T[sn]);
+    *reinterpret_cast<double2 *>(G) = ds_stencil<NT>(T, u, A, B);
+}
+
+// Thread map: column pair g of the 8-column tile, run j of consecutive rows
+// [j*RL, (j+1)*RL). A thread splits each staged tap once into a register
+// ring of NT pairs (one 16-byte shared load per output row) and computes
+// its rows in order. The wrap halo repeats rows 0 .. RL+NT-2 after row n1-1,
+// so a run's taps never wrap: the ring walks a plain pointer.
+template <int NT, int WC>
+__global__ void __launch_bounds__(ds_threads<WC>(), 24 / WC) adv_ds_f64(
+    const __grid_constant__ CUtensorMap tmap, AdvDsArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    constexpr int W = WC;
+    constexpr int TPR = W / 2;  // column pairs per row
+    const uint32_t raw = smem_u32addr(smem_raw);
+    const uint32_t pad = ((raw + 127u) & ~127u) - raw;
+    double *S = reinterpret_cast<double *>(smem_raw + pad);
+
+    const int64_t line = blockIdx.x / a.ncb;
+    const int c0 = (int)(blockIdx.x - line * a.ncb) * W;
+    const int n1 = (int)a.n1;
+    const int runs = blockDim.x / TPR;
+    const int RL = ds_run_rows(n1, runs);
+
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(&bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        staging_issue(&tmap, &bar, S, (uint32_t)(a.nbox * a.box_rows * W * 8), a.nbox, a.box_rows,
+                      (uint32_t)(a.box_rows * W * 8), c0, (int)line);
+    const int exc = a.exc_index ? a.exc_index[line] : -1;
+    const int base = a.base[line];
+    float2 A[NT], B[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        const float2 ab = a.w2[line * NT + k];
+        A[k] = make_float2(ab.x, ab.x);
+        B[k] = make_float2(ab.y, ab.y);
+    }
+    const bool ok_wait = __syncthreads_and(staging_wait(&bar, a.spin_limit));
+    if (!ok_wait) {
+        if (threadIdx.x == 0) {
+            atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
+            staging_wait(&bar, kWaitPolls);  // let the copies land before the CTA leaves
+        }
+        return;
+    }
+    // wrap halo: rows n1 .. n1+RL+NT-2 repeat rows 0 .. RL+NT-2
+    for (int i = threadIdx.x; i < (RL + NT - 1) * W; i += blockDim.x) S[n1 * W + i] = S[i];
+    __syncthreads();
+
+    if (exc >= 0) {
+        // per-cell stencils: FP64 direct form (the staged kernel's arithmetic)
+        const int total = n1 * W;
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            const int r = idx / W, c = idx - (idx / W) * W;
+            if (c0 + c >= a.n2) continue;
+            const AdvExcCell<double> &ec = a.exc[(int64_t)exc * n1 + r];
+            int rr = r + ec.base;
+            if (rr >= n1) rr -= n1;
+            double we[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k) we[k] = ec.w[k];
+            a.dst[(line * a.n1 + r) * a.n2 + c0 + c] = stencil_cell<double, NT>(S + rr * W + c, W, we);
+        }
+        return;
+    }
+
+    const int g = threadIdx.x % TPR;
+    const int rs = (int)(threadIdx.x / TPR) * RL;
+    const int cnt = min(n1 - rs, RL);
+    if (cnt <= 0 || c0 + 2 * g >= a.n2) return;  // n2 is even: a pair is whole or absent
+    int q0 = rs + base;  // row of the first output's tap 0
+    if (q0 >= n1) q0 -= n1;
+    const double2 *P0 = reinterpret_cast<const double2 *>(S) + (size_t)q0 * TPR + g;
+    double *G0 = a.dst + (line * a.n1 + rs) * a.n2 + c0 + 2 * g;
+    float4 T[NT];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < NT - 1; ++k) bad |= !ds_split2(P0[k * TPR], T[k]);
+    int i = 0;
+    const double2 *P = P0;
+    double *G = G0;
+    for (; i + NT <= cnt; i += NT) {
+#pragma unroll
+        for (int u = 0; u < NT; ++u) ds_row<NT, TPR>(P + u * TPR, u, T, bad, A, B, G + (int64_t)u * a.n2);
+        P += NT * TPR;
+        G += (int64_t)NT * a.n2;
+    }
+#pragma unroll
+    for (int u = 0; u < NT - 1; ++u)
+        if (i + u < cnt) ds_row<NT, TPR>(P + u * TPR, u, T, bad, A, B, G + (int64_t)u * a.n2);
+    if (bad) {
+        // a tap the split cannot carry: redo the pairs whose window holds one
+        // in FP64 (the staged kernel's arithmetic); the same thread wrote them
+        double w64[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) w64[k] = a.w[line * NT + k];
+        for (int r = 0; r < cnt; ++r) {
+            const double2 *Pr = P0 + r * TPR;
+            bool ok = true;
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                const double2 x = Pr[k * TPR];
+                ok = ok && ds_splittable(x.x) && ds_splittable(x.y);
+            }
+            if (ok) continue;
+            const double *p = S + (q0 + r) * W + 2 * g;
+            *reinterpret_cast<double2 *>(G0 + (int64_t)r * a.n2) =
+                make_double2(stencil_cell<double, NT>(p, W, w64),
+                             stencil_cell<double, NT>(p + 1, W, w64));
+        }
+    }
+}
+
+template <int NT, int WC>
+cudaError_t launch_ds_t(const CUtensorMap &tm, const AdvDsArgs &a, size_t smem, int64_t grid,
+                        cudaStream_t st) {
+    auto kern = adv_ds_f64<NT, WC>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid_x(grid), ds_threads<WC>(), smem, st>>>(tm, a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t adv_ds_smem(const AdvPlanImpl &p, int W) {
+    const int64_t n1 = p.desc.n1;
+    const int box_rows = (int)std::min<int64_t>(256, n1);
+    const int64_t nbox = (n1 + box_rows - 1) / box_rows;
+    const int RL = ds_run_rows(n1, kDsRuns);
+    const int64_t rows = std::max<int64_t>(nbox * box_rows, n1 + RL + p.npts - 1);
+    return (size_t)rows * W * 8 + 128;
+}
+
+bool adv_ds_shape_ok(const AdvPlanImpl &p, int W) {
+    return p.desc.dtype == BKMA_F64 && p.desc.impl != BKMA_ADV_PLAIN && p.d_w2 != nullptr &&
+           (W == 4 || W == 8) && (p.npts == 4 || p.npts == 6) && p.desc.n2 % 2 == 0 &&
+           p.desc.n2 >= W && p.desc.n1 >= 16 && p.lines < (1ll << 31) &&
+           tensor_map_encoder() != nullptr;
+}
+
+bool adv_ds_eligible(const AdvPlanImpl &p, const void *src, int W) {
+    return adv_ds_shape_ok(p, W) && ((uintptr_t)src % 16) == 0;
+}
+
+int adv_ds_threads(int W) { return W == 4 ? ds_threads<4>() : ds_threads<8>(); }
+
+cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cudaStream_t st) {
+    const CUtensorMap *tm = adv_field_tmap(p, src, W);
+    if (!tm) return cudaErrorInvalidValue;
+    AdvDsArgs a;
+    a.dst = (double *)dst;
+    a.n1 = p.desc.n1;
+    a.n2 = p.desc.n2;
+    a.ncb = p.ncb(W);
+    a.box_rows = (int)std::min<int64_t>(256, p.desc.n1);
+    a.nbox = (int)((p.desc.n1 + a.box_rows - 1) / a.box_rows);
+    a.base = p.d_base;
+    a.w = (const double *)p.d_w;
+    a.w2 = p.d_w2;
+    a.exc_index = p.n_exc > 0 ? p.d_exc_index : nullptr;
+    a.exc = (const AdvExcCell<double> *)p.d_exc;
+    a.status = p.d_status;
+    a.spin_limit = p.wait_polls;
+    const size_t smem = adv_ds_smem(p, W);
+    const int64_t grid = p.lines * a.ncb;
+    if (W == 4) {
+        if (p.npts == 6) return launch_ds_t<6, 4>(*tm, a, smem, grid, st);
+        return launch_ds_t<4, 4>(*tm, a, smem, grid, st);
+    }
+    if (p.npts == 6) return launch_ds_t<6, 8>(*tm, a, smem, grid, st);
+    return launch_ds_t<4, 8>(*tm, a, smem, grid, st);
+}
+
+}  // namespace bkma

@@ -27,6 +27,7 @@ struct AdvPlanImpl {
     // device tables
     int32_t *d_base = nullptr;
     void *d_w = nullptr;  // T weights
+    float2 *d_w2 = nullptr;  // FP64 plans: each weight split into two FP32 parts (a, b)
     int32_t *d_exc_index = nullptr;
     void *d_exc = nullptr;
     double *d_vx = nullptr;
@@ -35,7 +36,7 @@ struct AdvPlanImpl {
     bool stream_ok = false;
     // launch shape: path 0 = cp.async staging (any shape), 1 = TMA staging,
     // 2 = streamed columns (+ staged exception lines), 3 = contiguous lines
-    // (n2 = 1, R lines per CTA)
+    // (n2 = 1, R lines per CTA), 4 = FP64 in FP32-pair arithmetic (TMA tiles)
     int W = 16, R = 1, threads = 256, path = 0;
     bool autotuned = false;
     int fuse = 1;  // time steps per launch (adv_fused.cu when > 1)
@@ -74,6 +75,7 @@ struct AdvPlanImpl {
             if (e) cudaEventDestroy(e);
         cudaFree(d_base);
         cudaFree(d_w);
+        cudaFree(d_w2);
         cudaFree(d_exc_index);
         cudaFree(d_exc);
         cudaFree(d_vx);
@@ -151,6 +153,14 @@ bool adv_fused_f32_fast(const AdvPlanImpl &p, size_t max_smem);
 size_t adv_fused_x2_smem(const AdvPlanImpl &p);
 cudaError_t adv_fused_launch(const AdvPlanImpl &p, const void *src, void *dst, int W, int k,
                              cudaStream_t st);
+
+// FP64 storage, FP32-pair arithmetic (adv_ds.cu): TMA tiles of W = 4 or 8
+// columns, adv_ds_threads(W) threads per CTA.
+bool adv_ds_shape_ok(const AdvPlanImpl &p, int W);
+bool adv_ds_eligible(const AdvPlanImpl &p, const void *src, int W);
+size_t adv_ds_smem(const AdvPlanImpl &p, int W);
+int adv_ds_threads(int W);
+cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cudaStream_t st);
 
 bool adv_tma_eligible(const AdvPlanImpl &p, const void *src, int W);
 size_t adv_tma_smem(const AdvPlanImpl &p, int W);

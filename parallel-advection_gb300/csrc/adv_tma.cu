@@ -20,32 +20,15 @@
 #include "adv.cuh"
 #include "adv_plan.cuh"
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace bkma {
 
 namespace {
 
-__device__ __forceinline__ uint32_t smem_addr(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return smem_u32addr(p); }
 
 constexpr uint32_t kTmaSpinLimit = kWaitPolls;
-
-// Polls the staging barrier's phase 0 at most `polls` times.
-__device__ __forceinline__ bool tile_wait(uint64_t *bar, uint32_t polls) {
-    for (uint32_t i = 0; i < polls; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
-            " selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(smem_addr(bar))
-            : "memory");
-        if (done) return true;
-        if (i > 32) __nanosleep(128);
-    }
-    return false;
-}
 
 template <int NT, int WC>
 __global__ void __launch_bounds__(512) adv_tma_f32(const __grid_constant__ CUtensorMap tmap,
@@ -99,11 +82,11 @@ __global__ void __launch_bounds__(512) adv_tma_f32(const __grid_constant__ CUten
     // agrees on one outcome. On a timeout the status word is raised and the
     // issuing thread stays until its copies have landed (a second bounded
     // wait), so that no copy writes into shared memory the CTA has left.
-    const bool ok = __syncthreads_and(tile_wait(&bar, a.spin_limit));
+    const bool ok = __syncthreads_and(staging_wait(&bar, a.spin_limit));
     if (!ok) {
         if (threadIdx.x == 0) {
             atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
-            tile_wait(&bar, kTmaSpinLimit);
+            staging_wait(&bar, kTmaSpinLimit);
         }
         return;
     }
@@ -199,32 +182,35 @@ size_t adv_tma_smem(const AdvPlanImpl &p, int W) {
     return (size_t)rows * W * 4 + 128;
 }
 
+const CUtensorMap *adv_field_tmap(AdvPlanImpl &p, const void *src, int W) {
+    for (auto &c : p.tmaps)
+        if (c.ptr == src && c.W == W) return &c.map;
+    if (!encode_fn()) return nullptr;
+    AdvPlanImpl::TmapCache c;
+    c.ptr = src;
+    c.W = W;
+    const int box_rows = (int)std::min<int64_t>(256, p.desc.n1);
+    const cuuint64_t es = (cuuint64_t)p.esize;
+    const cuuint64_t dims[3] = {(cuuint64_t)p.desc.n2, (cuuint64_t)p.desc.n1, (cuuint64_t)p.lines};
+    const cuuint64_t strides[2] = {(cuuint64_t)p.desc.n2 * es, (cuuint64_t)(p.desc.n1 * p.desc.n2) * es};
+    const cuuint32_t box[3] = {(cuuint32_t)W, (cuuint32_t)box_rows, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUtensorMapDataType dt =
+        p.esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    CUresult r = encode_fn()(&c.map, dt, 3, const_cast<void *>(src), dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return nullptr;
+    if (p.tmaps.size() >= 4) p.tmaps.erase(p.tmaps.begin());
+    p.tmaps.push_back(c);
+    return &p.tmaps.back().map;
+}
+
 cudaError_t adv_tma_launch(AdvPlanImpl &p, const void *src, void *dst, int W, int threads,
                            cudaStream_t st) {
     // tensor map of the source field (cached per pointer)
-    CUtensorMap *tm = nullptr;
-    for (auto &c : p.tmaps)
-        if (c.ptr == src && c.W == W) tm = &c.map;
-    if (!tm) {
-        AdvPlanImpl::TmapCache c;
-        c.ptr = src;
-        c.W = W;
-        const int box_rows = (int)std::min<int64_t>(256, p.desc.n1);
-        const cuuint64_t dims[3] = {(cuuint64_t)p.desc.n2, (cuuint64_t)p.desc.n1,
-                                    (cuuint64_t)p.lines};
-        const cuuint64_t strides[2] = {(cuuint64_t)p.desc.n2 * 4,
-                                       (cuuint64_t)(p.desc.n1 * p.desc.n2 * 4)};
-        const cuuint32_t box[3] = {(cuuint32_t)W, (cuuint32_t)box_rows, 1};
-        const cuuint32_t es[3] = {1, 1, 1};
-        CUresult r = encode_fn()(&c.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(src),
-                                 dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-        if (p.tmaps.size() >= 4) p.tmaps.erase(p.tmaps.begin());
-        p.tmaps.push_back(c);
-        tm = &p.tmaps.back().map;
-    }
+    const CUtensorMap *tm = adv_field_tmap(p, src, W);
+    if (!tm) return cudaErrorInvalidValue;
     AdvTmaArgs a;
     a.dst = (float *)dst;
     a.n1 = p.desc.n1;

@@ -375,8 +375,13 @@ __global__ void conv_tc_prologue(const __nv_bfloat16 *w, int cin, int cout, int 
     }
 }
 
-template <int KC>  // K16 steps per tap: Cin / 16
+// KC: K16 steps per tap (Cin / 16). kPlanPolls: the pipeline waits poll
+// a.spin_limit times (a plan whose wait limit was changed) instead of the
+// compile-time kSpinLimit; a runtime bound in the MMA issue loop measured 11 %
+// slower on the bench workload, so the default instantiation keeps the constant.
+template <int KC, bool kPlanPolls>
 __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_constant__ Args a) {
+    const uint32_t polls = kPlanPolls ? a.spin_limit : kSpinLimit;
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t full_bar[STAGES_MAX], empty_bar[STAGES_MAX];
     __shared__ __align__(8) uint64_t accf_bar[2], acce_bar[2];
@@ -470,7 +475,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             if ((it & 1) != grp) continue;
             const int s = it % stages;
             const uint32_t ph = (uint32_t)(it / stages) & 1u;
-            if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_flag, a.status, a.spin_limit)) break;
+            if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_flag, a.status, polls)) break;
             const int b = (int)(item / a.ntiles);
             const int tile = (int)(item % a.ntiles);
             unsigned char *stage = stages_sm + (size_t)s * a.stage_bytes;
@@ -511,10 +516,10 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             BKMA_TC_FOR_ITEMS {
                 const int s = it % stages;
                 const uint32_t ph = (uint32_t)(it / stages) & 1u;
-                if (!mbar_wait(&full_bar[s], ph, &abort_flag, a.status, a.spin_limit)) break;
+                if (!mbar_wait(&full_bar[s], ph, &abort_flag, a.status, polls)) break;
                 const int acc = a.nacc == 2 ? (it & 1) : 0;
                 const uint32_t aph = (uint32_t)(a.nacc == 2 ? (it >> 1) : it) & 1u;
-                if (!mbar_wait(&acce_bar[acc], aph ^ 1u, &abort_flag, a.status, a.spin_limit)) break;
+                if (!mbar_wait(&acce_bar[acc], aph ^ 1u, &abort_flag, a.status, polls)) break;
                 fence_after();
                 const uint32_t d_tmem = tmem + (uint32_t)(a.tm_cols + acc * TILE);
                 // descriptor low word: start address >> 4 (bits 0-13, < 256 KB so
@@ -557,7 +562,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __grid_consta
             const int tile = (int)(item % a.ntiles);
             const int acc = a.nacc == 2 ? (it & 1) : 0;
             const uint32_t aph = (uint32_t)(a.nacc == 2 ? (it >> 1) : it) & 1u;
-            if (!mbar_wait(&accf_bar[acc], aph, &abort_flag, a.status, a.spin_limit)) break;
+            if (!mbar_wait(&accf_bar[acc], aph, &abort_flag, a.status, polls)) break;
             fence_after();
             const int64_t l0 = (int64_t)tile * TILE;
             // The tensor map ends at lt = lout rounded down to 8 positions (a
@@ -831,17 +836,20 @@ bkma_status tc_launch(const bkma_conv_desc &d, const void *data, void *out, int6
     a.status = status;
     a.spin_limit = wait_polls;
     void (*kern)(const tc::Args) = nullptr;
+    const bool plan_polls = wait_polls != kWaitPolls;
+#define BKMA_TC_KERN(kc) (plan_polls ? tc::conv_tc_kernel<kc, true> : tc::conv_tc_kernel<kc, false>)
     switch (a.cin / 16) {
-    case 1: kern = tc::conv_tc_kernel<1>; break;
-    case 2: kern = tc::conv_tc_kernel<2>; break;
-    case 3: kern = tc::conv_tc_kernel<3>; break;
-    case 4: kern = tc::conv_tc_kernel<4>; break;
-    case 5: kern = tc::conv_tc_kernel<5>; break;
-    case 6: kern = tc::conv_tc_kernel<6>; break;
-    case 7: kern = tc::conv_tc_kernel<7>; break;
-    case 8: kern = tc::conv_tc_kernel<8>; break;
+    case 1: kern = BKMA_TC_KERN(1); break;
+    case 2: kern = BKMA_TC_KERN(2); break;
+    case 3: kern = BKMA_TC_KERN(3); break;
+    case 4: kern = BKMA_TC_KERN(4); break;
+    case 5: kern = BKMA_TC_KERN(5); break;
+    case 6: kern = BKMA_TC_KERN(6); break;
+    case 7: kern = BKMA_TC_KERN(7); break;
+    case 8: kern = BKMA_TC_KERN(8); break;
     default: return fail(BKMA_ERR_UNSUPPORTED, "tensor path: cin must be 16..128");
     }
+#undef BKMA_TC_KERN
     BKMA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t.smem));
     kern<<<grid, tc::THREADS, t.smem, st>>>(a);
     BKMA_CUDA_TRY(cudaGetLastError());

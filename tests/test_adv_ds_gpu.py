@@ -1,0 +1,218 @@
+"""FP64 advection in FP32-pair arithmetic (the FP64 plans' default kernel
+where the shape allows it: degree 3 or 5, an even n2 >= 8), through the C ABI.
+
+Tolerances:
+  - against the staged FP64 kernel (FP64 direct form sum_k w_k f_k, the same
+    per-line weights): |diff| <= 2e-13 * max|f| per step (each product of the
+    pair arithmetic is exact, the sum carries ~48 bits);
+  - against the oracle (the reference's per-cell FP64 math): 1e-11 * max|f|,
+    the staged FP64 kernel's own bound (per-line weights);
+  - tiles that hold a value the split cannot carry (|x| >= 2^126 or
+    0 < |x| < 2^-74, subnormals, inf, NaN), exception lines and fields off
+    the 16-byte grid run the staged kernel's FP64 arithmetic: bit-identical.
+"""
+import numpy as np
+import pytest
+
+from oracle import AdvParams
+
+pytestmark = pytest.mark.gpu
+
+DS_CASES = [
+    # n0, n1, n2, dt, minX, maxX, minVx, maxVx
+    (3, 256, 64, 0.003, 0.0, 1.0, -1.0, 1.0),
+    (4, 1000, 10, 0.0011, 0.0, 1.0, -1.0, 1.0),   # 8 + 2 columns: ragged last tile
+    (2, 2048, 16, 0.0007, 0.0, 1.0, -2.0, 2.0),
+    (5, 300, 8, 0.02, 0.0, 1.0, -3.0, 3.0),       # shifts of several cells
+    (3, 64, 24, 0.01, -0.5, 1.5, -1.0, 1.0),
+]
+TOL = 2e-13
+
+
+def _init(p, seed):
+    rng = np.random.default_rng(seed)
+    x = p.minX + np.arange(p.n1) * ((p.maxX - p.minX) / p.n1)
+    f = np.sin(2 * np.pi * (x - p.minX) / (p.maxX - p.minX))[None, :, None]
+    return np.ascontiguousarray(f + 0.01 * rng.uniform(-1, 1, (p.n0, p.n1, p.n2)))
+
+
+def _plans(bkma, p, **kw):
+    args = dict(dt=p.dt, minX=p.minX, maxX=p.maxX, minVx=p.minVx, maxVx=p.maxVx, dtype="f64")
+    args.update(kw)
+    ds = bkma.AdvectionPlan(p.n0, p.n1, p.n2, **args)
+    st = bkma.AdvectionPlan(p.n0, p.n1, p.n2, **args)
+    st.set_tile(8, 1, 256, 0)
+    return ds, st
+
+
+def test_ds_tile_widths_bit_identical(bkma, cuda):
+    """4- and 8-column tiles run the same arithmetic per cell: same bits."""
+    import torch
+    p = AdvParams(*DS_CASES[1])
+    f0 = _init(p, 9)
+    ref = None
+    for w in (4, 8):
+        plan, _ = _plans(bkma, p)
+        plan.set_tile(w, 1, 32 * w, 4)
+        d = torch.tensor(f0, device=cuda)
+        plan.step(d, nsteps=3)
+        plan.status()
+        if ref is None:
+            ref = d
+        else:
+            assert torch.equal(d, ref)
+
+
+@pytest.mark.parametrize("case", DS_CASES)
+@pytest.mark.parametrize("degree", [5, 3])
+def test_ds_close_to_staged_and_oracle(bkma, cuda, oracle, case, degree):
+    import torch
+    p = AdvParams(*case)
+    weights = "reference" if degree == 5 else "lagrange"
+    ds, st = _plans(bkma, p, degree=degree, weights=weights)
+    assert ds.info()["path"] == 4, ds.info()
+    f0 = _init(p, 1)
+    steps = 4
+    a = torch.tensor(f0, device=cuda)
+    b = torch.tensor(f0, device=cuda)
+    ds.step(a, nsteps=steps)
+    st.step(b, nsteps=steps)
+    ds.status()
+    scale = b.abs().max().item()
+    assert (a - b).abs().max().item() <= TOL * steps * scale
+    want = oracle.adv_step(p, f0.copy(), steps, degree=degree, ref_weights=degree == 5)
+    assert np.abs(a.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_ds_inplace_equals_out_of_place(bkma, cuda):
+    import torch
+    p = AdvParams(*DS_CASES[0])
+    ds, _ = _plans(bkma, p)
+    f0 = _init(p, 2)
+    a = torch.tensor(f0, device=cuda)
+    ds.step(a, nsteps=3)
+    oop = bkma.AdvectionPlan(p.n0, p.n1, p.n2, dtype="f64", dt=p.dt, minVx=p.minVx,
+                             maxVx=p.maxVx, inplace=False)
+    src = torch.tensor(f0, device=cuda)
+    out = torch.empty_like(src)
+    oop.step(src, out=out, nsteps=3)
+    assert torch.equal(a, out)
+
+
+@pytest.mark.parametrize("value", [1e200, -3e38 * 1e3, 1e-30, 5e-324, float("inf")])
+def test_ds_unsplittable_value_runs_fp64(bkma, cuda, value):
+    """A value the FP32 pair cannot carry sends every cell pair whose stencil
+    reads it to the FP64 arithmetic: those cells equal the staged kernel bit
+    for bit; every other cell stays within the pair arithmetic's bound."""
+    import torch
+    p = AdvParams(3, 256, 24, 0.003, 0.0, 1.0, -1.0, 1.0)
+    ds, st = _plans(bkma, p)
+    f0 = _init(p, 3)
+    i0, r_bad, col = 1, 100, 11  # slab 1, column pair (10, 11)
+    f0[i0, r_bad, col] = value
+    a = torch.tensor(f0, device=cuda)
+    b = torch.tensor(f0, device=cuda)
+    ds.step(a)
+    st.step(b)
+    ds.status()
+    offs, _ = ds.line_table()
+    npts = 6
+    rows = [r for r in range(p.n1) if (r_bad - (r + int(offs[i0]))) % p.n1 < npts]
+    assert len(rows) == npts
+    pair = slice(col - col % 2, col - col % 2 + 2)
+    hit = torch.zeros_like(a, dtype=torch.bool)
+    hit[i0, rows, pair] = True
+    assert torch.allclose(a[hit], b[hit], rtol=0, atol=0, equal_nan=True)
+    diff = (a - b).abs()[~hit].max().item()
+    assert diff <= TOL * b[~hit].abs().max().item()
+
+
+def test_ds_zeros_and_sign_changes(bkma, cuda):
+    """Exact zeros split exactly (a zero field stays zero); a field crossing
+    zero with many tiny values stays within the bound."""
+    import torch
+    p = AdvParams(2, 512, 16, 0.001, 0.0, 1.0, -1.0, 1.0)
+    ds, st = _plans(bkma, p)
+    z = torch.zeros((p.n0, p.n1, p.n2), dtype=torch.float64, device=cuda)
+    ds.step(z, nsteps=3)
+    assert torch.count_nonzero(z).item() == 0
+    x = np.arange(p.n1) / p.n1
+    f0 = np.ascontiguousarray(np.broadcast_to((np.sin(2 * np.pi * x) ** 9)[None, :, None],
+                                              (p.n0, p.n1, p.n2)))
+    a = torch.tensor(f0, device=cuda)
+    b = torch.tensor(f0, device=cuda)
+    ds.step(a, nsteps=5)
+    st.step(b, nsteps=5)
+    assert (a - b).abs().max().item() <= TOL * 5 * b.abs().max().item()
+
+
+def test_ds_exception_lines_bit_identical_to_staged(bkma, cuda, oracle):
+    """Lines whose departure offset varies along n1 use per-cell FP64
+    stencils: the FP64 arithmetic, bit for bit."""
+    import torch
+    p = AdvParams(6, 1000, 8, 0.001, 0.0, 1.0, -2.0, 3.0)
+    vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
+    ds, st = _plans(bkma, p, velocity=vel)
+    assert ds.info()["exception_lines"] > 0 and ds.info()["path"] == 4
+    f0 = _init(p, 4)
+    a = torch.tensor(f0, device=cuda)
+    b = torch.tensor(f0, device=cuda)
+    ds.step(a, nsteps=2)
+    st.step(b, nsteps=2)
+    exc = [i0 for i0 in range(p.n0)
+           if len({(oracle.departure(p, i1, vel[i0])[0] - i1) % p.n1 for i1 in range(p.n1)}) > 1]
+    assert exc and len(exc) == ds.info()["exception_lines"]
+    for i0 in exc:
+        assert torch.equal(a[i0], b[i0]), i0
+    assert (a - b).abs().max().item() <= TOL * 2 * b.abs().max().item()
+
+
+def test_ds_misaligned_field_runs_fp64(bkma, cuda):
+    import torch
+    p = AdvParams(*DS_CASES[0])
+    ds, st = _plans(bkma, p)
+    f0 = _init(p, 5)
+    n = f0.size
+    buf = torch.empty(n + 1, dtype=torch.float64, device=cuda)
+    d = buf[1:].view(f0.shape)  # 8 bytes past a 16-byte boundary
+    d.copy_(torch.tensor(f0, device=cuda))
+    ds.step(d, nsteps=2)
+    b = torch.tensor(f0, device=cuda)
+    st.step(b, nsteps=2)
+    assert torch.equal(d, b)
+
+
+def test_ds_timeout_reported(bkma, cuda):
+    import torch
+    p = AdvParams(*DS_CASES[0])
+    ds, st = _plans(bkma, p)
+    f0 = torch.tensor(_init(p, 6), device=cuda)
+    a = f0.clone()
+    ds.set_wait_limit(0)
+    ds.step(a)
+    with pytest.raises(bkma.BkmaError) as e:
+        ds.status()
+    assert e.value.status == 4
+    assert torch.equal(a, f0)
+    ds.set_wait_limit(1 << 22)
+    ds.step(a)
+    ds.status()
+    b = f0.clone()
+    ds2, _ = _plans(bkma, p)
+    ds2.step(b)
+    assert torch.equal(a, b)
+
+
+def test_ds_autotune_keeps_the_pair_kernel(bkma, cuda):
+    import torch
+    p = AdvParams(*DS_CASES[2])
+    ds, _ = _plans(bkma, p)
+    f0 = torch.tensor(_init(p, 7), device=cuda)
+    scratch = f0.clone()
+    info = ds.autotune(scratch)
+    assert info["path"] == 4
+    a, b = f0.clone(), f0.clone()
+    ds.step(a, nsteps=2)
+    fresh, _ = _plans(bkma, p)
+    fresh.step(b, nsteps=2)
+    assert torch.equal(a, b)
