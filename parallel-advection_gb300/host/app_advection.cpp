@@ -5,9 +5,11 @@
 // kernelImpl selects the strategy like impl_selector: NDRange / AdaptiveWg /
 // GB300 run in place, BasicRange out of place into a second buffer (the
 // reference's global scratch), Plain runs the per-cell FP64 reference math.
-// The field is FP64 like the reference unless --fp32 is given. --fused K
-// runs K time steps per kernel launch on shared-memory strips (same bits, one
-// call for all maxIter steps instead of a wait after each); --hi-lo (FP32,
+// The field is FP64 like the reference unless --fp32 is given (FP64 steps run
+// in FP32-pair arithmetic, within 2e-13 max|f| per step of FP64 arithmetic).
+// --fused K runs K time steps per kernel launch on shared-memory strips (FP32:
+// the same bits; FP64: FP64 arithmetic; one call for all maxIter steps
+// instead of a wait after each); --hi-lo (FP32,
 // with --fused) keeps each cell as an FP32 hi + lo pair between the steps of
 // a launch, rounding to FP32 once per launch.
 #include <cuda_runtime.h>

@@ -62,9 +62,16 @@ def _l1(apps, tmp_path, impl, extra):
 @pytest.mark.parametrize("impl,extra", [("AdaptiveWg", ["--fp32"]), ("AdaptiveWg", []),
                                         ("BasicRange", ["--fp32"])])
 def test_advection_driver_fused_same_result(apps, tmp_path, impl, extra):
-    """--fused K gives the bits of one step per launch, so the printed
-    validation errors are the same; --hi-lo stays within the check."""
-    assert _l1(apps, tmp_path, impl, extra + ["--fused", "4"]) == _l1(apps, tmp_path, impl, extra)
+    """--fused K gives the bits of one step per launch in FP32, so the printed
+    validation errors are the same. FP64 fused steps run FP64 arithmetic while
+    one step per launch runs the FP32-pair kernel (2e-13 max|f| per step
+    apart), so the FP64 errors agree to 1e-13; --hi-lo stays within the check."""
+    fused = _l1(apps, tmp_path, impl, extra + ["--fused", "4"])
+    one = _l1(apps, tmp_path, impl, extra)
+    if "--fp32" in extra:
+        assert fused == one
+    else:
+        assert all(abs(float(a) - float(b)) <= 1e-13 for a, b in zip(fused, one)), (fused, one)
     if "--fp32" in extra:
         hi, _ = _l1(apps, tmp_path, impl, extra + ["--fused", "10", "--hi-lo"])
         assert float(hi) < 1e-6
