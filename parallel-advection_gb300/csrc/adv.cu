@@ -569,6 +569,7 @@ using namespace bkma;
 extern "C" {
 
 bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan) try {
+    bkma::NvtxRange nvtx_range("bkma_adv_plan_create");
     BKMA_CHECK_ARG(desc && plan, "bkma_adv_plan_create: null argument");
     *plan = nullptr;
     const bkma_adv_desc &d = *desc;
@@ -690,6 +691,7 @@ bkma_status bkma_adv_plan_set_wait_limit(bkma_adv_plan *plan, uint32_t polls) tr
 } BKMA_ABI_CATCH("bkma_adv_plan_set_wait_limit")
 
 bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *field, void *stream) try {
+    bkma::NvtxRange nvtx_range("bkma_adv_plan_autotune");
     BKMA_CHECK_ARG(plan && field, "null argument");
     return adv_autotune(plan->impl, field, (cudaStream_t)stream);
 } BKMA_ABI_CATCH("bkma_adv_plan_autotune")
@@ -790,6 +792,7 @@ bkma_status bkma_adv_plan_destroy(bkma_adv_plan *plan) try {
 } BKMA_ABI_CATCH("bkma_adv_plan_destroy")
 
 bkma_status bkma_adv_step(bkma_adv_plan *plan, void *data, void *out, int32_t nsteps, void *stream) try {
+    bkma::NvtxRange nvtx_range("bkma_adv_step");
     BKMA_CHECK_ARG(plan && data, "bkma_adv_step: null argument");
     BKMA_CHECK_ARG(nsteps >= 0, "nsteps must be >= 0");
     AdvPlanImpl &p = plan->impl;
@@ -797,6 +800,7 @@ bkma_status bkma_adv_step(bkma_adv_plan *plan, void *data, void *out, int32_t ns
 } BKMA_ABI_CATCH("bkma_adv_step")
 
 bkma_status bkma_adv_run_host(bkma_adv_plan *plan, void *host_data, int32_t nsteps, void *stream) try {
+    bkma::NvtxRange nvtx_range("bkma_adv_run_host");
     BKMA_CHECK_ARG(plan && host_data, "bkma_adv_run_host: null argument");
     AdvPlanImpl &p = plan->impl;
     const size_t slab = (size_t)(p.desc.n1 * p.desc.n2) * (size_t)p.esize;

@@ -293,6 +293,7 @@ extern "C" {
 
 bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields, int32_t dtype,
                                   bkma_adv_batch **batch) try {
+    bkma::NvtxRange nvtx_range("bkma_adv_batch_create");
     BKMA_CHECK_ARG(fields && batch && nfields > 0, "bkma_adv_batch_create: bad arguments");
     BKMA_CHECK_ARG(dtype == BKMA_F32 || dtype == BKMA_F64, "dtype must be BKMA_F32 or BKMA_F64");
     *batch = nullptr;
@@ -348,6 +349,7 @@ bkma_status bkma_adv_batch_create(const bkma_adv_field *fields, int32_t nfields,
 } BKMA_ABI_CATCH("bkma_adv_batch_create")
 
 bkma_status bkma_adv_batch_step(bkma_adv_batch *batch, int32_t nsteps, void *stream) try {
+    bkma::NvtxRange nvtx_range("bkma_adv_batch_step");
     BKMA_CHECK_ARG(batch && nsteps >= 0, "bkma_adv_batch_step: bad arguments");
     BatchImpl &b = batch->impl;
     for (int i = 0; i < nsteps; ++i) BKMA_CUDA_TRY(cudaGraphLaunch(b.exec, (cudaStream_t)stream));
@@ -355,6 +357,7 @@ bkma_status bkma_adv_batch_step(bkma_adv_batch *batch, int32_t nsteps, void *str
 } BKMA_ABI_CATCH("bkma_adv_batch_step")
 
 bkma_status bkma_adv_batch_autotune(bkma_adv_batch *batch, void *stream) try {
+    bkma::NvtxRange nvtx_range("bkma_adv_batch_autotune");
     BKMA_CHECK_ARG(batch, "null argument");
     BatchImpl &b = batch->impl;
     cudaStream_t st = (cudaStream_t)stream;

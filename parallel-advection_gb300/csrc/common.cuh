@@ -3,6 +3,7 @@
 // operation order on host and device).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <string>
@@ -32,6 +33,16 @@ void *tensor_map_encoder();
     do {                                                                     \
         if (!(cond)) return ::bkma::fail(BKMA_ERR_INVALID_ARG, msg);         \
     } while (0)
+
+// A named NVTX range for the duration of an entry point: the library's calls
+// show up by name on a profiler's timeline (Nsight Systems / Compute); without
+// a profiler attached a push/pop costs a few nanoseconds.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Polls of a bounded device-side wait before it gives up (with the kernels'
 // back-off, roughly half a second to a second): plans start with this limit,

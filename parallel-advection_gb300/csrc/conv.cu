@@ -260,6 +260,7 @@ bkma_status conv_check_desc(const bkma_conv_desc &d) {
 extern "C" {
 
 bkma_status bkma_conv_plan_create(const bkma_conv_desc *desc, bkma_conv_plan **plan) try {
+    bkma::NvtxRange nvtx_range("bkma_conv_plan_create");
     BKMA_CHECK_ARG(desc && plan, "bkma_conv_plan_create: null argument");
     *plan = nullptr;
     const bkma_conv_desc &d = *desc;
@@ -304,6 +305,7 @@ bkma_status bkma_conv_plan_scratch_bytes(const bkma_conv_plan *plan, int64_t *by
 
 bkma_status bkma_conv_run(bkma_conv_plan *plan, void *data, void *out, const void *weight,
                           const void *bias, void *stream) try {
+    bkma::NvtxRange nvtx_range("bkma_conv_run");
     BKMA_CHECK_ARG(plan && data && weight, "bkma_conv_run: null argument");
     ConvPlanImpl &p = plan->impl;
     const bkma_conv_desc &d = p.desc;
