@@ -320,17 +320,24 @@ bkma_status bkma_conv1d_bf16_inplace_noalloc(void *data, const void *weight, con
 bkma_status bkma_conv1d_noalloc_status(void *stream);
 
 /* ------------------------------------------------------- learned stencil */
-/* A small MLP (1 -> 32 -> 32 -> 4, GELU, FP32) maps a line's fractional shift
- * a in [0,1) to a corrected 4-point stencil w(a) = L3(a) + c(a) - mean(c(a))
- * (L3: degree-3 Lagrange; the weights keep summing to one). No counterpart in
- * the reference (which only has the fixed degree-5 stencil); the trained
- * weights feed an advection plan created with BKMA_W_TABLE and degree 3
- * through bkma_adv_plan_set_weights. Parameter layout (1252 floats):
- * W1[32] b1[32] W2[32][32] b2[32] W3[4][32] b3[4]; the output layer starts at
- * zero, so an untrained model is the degree-3 Lagrange stencil. */
+/* A small MLP (1 -> 32 -> 32 -> npts, GELU, FP32) maps a line's fractional
+ * shift a in [0,1) to a corrected stencil w(a) = L(a) + c(a) - mean(c(a)) of
+ * npts = 4 points (L: degree-3 Lagrange on nodes 0..3 at 1 + a) or 6 points
+ * (degree-5 Lagrange on nodes 0..5 at 2 + a); the weights keep summing to one.
+ * No counterpart in the reference (which only has the fixed degree-5
+ * stencil); the trained weights feed an advection plan created with
+ * BKMA_W_TABLE and degree npts - 1 through bkma_adv_plan_set_weights.
+ * Parameter layout (32 + 32 + 1024 + 32 + 33 npts floats: 1252 for 4 points,
+ * 1318 for 6): W1[32] b1[32] W2[32][32] b2[32] W3[npts][32] b3[npts]; the output
+ * layer starts at zero, so an untrained model is the Lagrange stencil. */
 typedef struct bkma_mlp bkma_mlp;
+/* A 4-point model. */
 bkma_status bkma_mlp_create(uint64_t seed, bkma_mlp **mlp);
-/* Copy the 1252 parameters to (set = 0) or from (set = 1) a host array. */
+/* A model of npts = 4 or 6 points. */
+bkma_status bkma_mlp_create_stencil(uint64_t seed, int32_t npts, bkma_mlp **mlp);
+/* The model's stencil points and parameter count. */
+bkma_status bkma_mlp_info(const bkma_mlp *mlp, int32_t *npts, int32_t *nparams);
+/* Copy the parameters to (set = 0) or from (set = 1) a host array. */
 bkma_status bkma_mlp_params(bkma_mlp *mlp, float *host_params, int32_t set);
 /* Training samples first .. first+n-1 into device arrays alpha[n],
  * taps4[n][4], target[n]: a random periodic line (32 Fourier modes with
@@ -338,17 +345,26 @@ bkma_status bkma_mlp_params(bkma_mlp *mlp, float *host_params, int32_t set);
  * at j + alpha. */
 bkma_status bkma_mlp_samples(int64_t n, uint64_t seed, int64_t first, float *alpha, float *taps4,
                              float *target, void *stream);
-/* Mean squared error over all n samples and its gradient (host float[1252]). */
-bkma_status bkma_mlp_grad(bkma_mlp *mlp, const float *alpha, const float *taps4,
+/* The same on lines sampled on n1 cells, with the npts nodes around node j
+ * (taps[n][npts]) and, when exact = 1, the target f(x_j + a/n1) of the line's
+ * own Fourier series instead of the degree-9 Lagrange value (for coarse
+ * grids, where degree 9 is not accurate either). bkma_mlp_samples is
+ * n1 = 1024, npts = 4, exact = 0. */
+bkma_status bkma_mlp_samples_grid(int64_t n, uint64_t seed, int64_t first, int64_t n1,
+                                  int32_t npts, int32_t exact, float *alpha, float *taps,
+                                  float *target, void *stream);
+/* Mean squared error over all n samples and its gradient (host float[nparams]);
+ * taps is [n][npts] of the model's npts. */
+bkma_status bkma_mlp_grad(bkma_mlp *mlp, const float *alpha, const float *taps,
                           const float *target, int64_t n, float *host_grad, double *host_loss,
                           void *stream);
 /* `steps` Adam steps on random batches of `batch` samples drawn from the n
  * samples, cosine learning rate from lr_max; host_loss gets the last batch's
  * mean squared error. */
-bkma_status bkma_mlp_train(bkma_mlp *mlp, const float *alpha, const float *taps4,
+bkma_status bkma_mlp_train(bkma_mlp *mlp, const float *alpha, const float *taps,
                            const float *target, int64_t n, int32_t steps, int32_t batch,
                            float lr_max, uint64_t seed, double *host_loss, void *stream);
-/* Stencils of n shifts: device alpha[n] -> device weights[n][4]. */
+/* Stencils of n shifts: device alpha[n] -> device weights[n][npts]. */
 bkma_status bkma_mlp_infer(const bkma_mlp *mlp, const float *alpha, int64_t n, float *weights,
                            void *stream);
 bkma_status bkma_mlp_destroy(bkma_mlp *mlp);

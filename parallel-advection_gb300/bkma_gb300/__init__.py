@@ -295,26 +295,33 @@ class AdvectionBatch:
 
 
 class LearnedStencil:
-    """Learned 4-point stencil (bkma_mlp_*): training data, training, gradient
-    and inference all run in the library's CUDA kernels."""
+    """Learned stencil of 4 or 6 points (bkma_mlp_*): training data, training,
+    gradient and inference all run in the library's CUDA kernels."""
 
-    NP = 1252
+    NP = 1252  # parameters of a 4-point model
 
-    def __init__(self, seed: int = 0):
+    def __init__(self, seed: int = 0, npts: int = 4):
         h = C.c_void_p()
-        check(load().bkma_mlp_create(seed, C.byref(h)))
+        check(load().bkma_mlp_create_stencil(seed, npts, C.byref(h)))
         self._h = h
+        k, n = C.c_int32(), C.c_int32()
+        check(load().bkma_mlp_info(h, C.byref(k), C.byref(n)))
+        self.npts, self.NP = k.value, n.value
 
     @staticmethod
-    def samples(n: int, seed: int, first: int = 0, device=None):
+    def samples(n: int, seed: int, first: int = 0, device=None, n1: int = 1024, npts: int = 4,
+                exact: bool = False):
+        """Training samples (alpha[n], taps[n][npts], target[n]) of random
+        periodic lines sampled on n1 cells; the target is the degree-9
+        Lagrange value, or with exact=True the line's own value."""
         import torch
         dev = device or torch.device("cuda", torch.cuda.current_device())
         a = torch.empty(n, dtype=torch.float32, device=dev)
-        f4 = torch.empty(n, 4, dtype=torch.float32, device=dev)
+        f = torch.empty(n, npts, dtype=torch.float32, device=dev)
         t = torch.empty(n, dtype=torch.float32, device=dev)
-        check(load().bkma_mlp_samples(n, seed, first, a.data_ptr(), f4.data_ptr(), t.data_ptr(),
-                                      _stream(None)))
-        return a, f4, t
+        check(load().bkma_mlp_samples_grid(n, seed, first, n1, npts, int(exact), a.data_ptr(),
+                                           f.data_ptr(), t.data_ptr(), _stream(None)))
+        return a, f, t
 
     def params(self) -> np.ndarray:
         p = np.zeros(self.NP, dtype=np.float32)
@@ -327,39 +334,39 @@ class LearnedStencil:
             raise BkmaError(_lib.BKMA_ERR_INVALID_ARG, f"params: {self.NP} values needed")
         check(load().bkma_mlp_params(self._h, q.ctypes.data, 1))
 
-    @staticmethod
-    def _samples(a, f4, t) -> tuple[int, int, int]:
+    def _samples(self, a, f, t) -> tuple[int, int, int]:
         n = a.numel()
-        return (_dev(a, "alpha", "f32"), _dev(f4, "taps4", "f32", 4 * n),
+        return (_dev(a, "alpha", "f32"), _dev(f, "taps", "f32", self.npts * n),
                 _dev(t, "target", "f32", n))
 
-    def grad(self, a, f4, t) -> tuple[float, np.ndarray]:
+    def grad(self, a, f, t) -> tuple[float, np.ndarray]:
         g = np.zeros(self.NP, dtype=np.float32)
         loss = C.c_double()
-        check(load().bkma_mlp_grad(self._h, *self._samples(a, f4, t), a.numel(),
+        check(load().bkma_mlp_grad(self._h, *self._samples(a, f, t), a.numel(),
                                    g.ctypes.data, C.byref(loss), _stream(None)))
         return loss.value, g
 
-    def train(self, a, f4, t, steps: int, batch: int = 4096, lr: float = 3e-3,
+    def train(self, a, f, t, steps: int, batch: int = 4096, lr: float = 3e-3,
               seed: int = 1) -> float:
         loss = C.c_double()
-        check(load().bkma_mlp_train(self._h, *self._samples(a, f4, t), a.numel(),
+        check(load().bkma_mlp_train(self._h, *self._samples(a, f, t), a.numel(),
                                     steps, batch, lr, seed, C.byref(loss), _stream(None)))
         return loss.value
 
     def infer(self, alpha):
         import torch
-        out = torch.empty(alpha.numel(), 4, dtype=torch.float32, device=alpha.device)
+        out = torch.empty(alpha.numel(), self.npts, dtype=torch.float32, device=alpha.device)
         check(load().bkma_mlp_infer(self._h, _dev(alpha, "alpha", "f32"), alpha.numel(),
                                     out.data_ptr(),
                                     _stream(None)))
         return out
 
     def plan_for(self, n0: int, n1: int, n2: int, **kw) -> "AdvectionPlan":
-        """An FP32 advection plan whose per-line 4-point weights come from the
-        network (degree-3 tap layout, the plan's own departure offsets)."""
+        """An FP32 advection plan whose per-line weights come from the network
+        (the Lagrange tap layout of degree npts - 1, the plan's own departure
+        offsets)."""
         import torch
-        plan = AdvectionPlan(n0, n1, n2, dtype="f32", degree=3, weights="table", **kw)
+        plan = AdvectionPlan(n0, n1, n2, dtype="f32", degree=self.npts - 1, weights="table", **kw)
         _, shifts = plan.line_table()
         a = torch.tensor(shifts, dtype=torch.float32, device="cuda")
         w = self.infer(a)

@@ -103,6 +103,10 @@ SIGNATURES = {
                                                C.c_int64, _vp]),
     "bkma_conv1d_noalloc_status": (_st, [_vp]),
     "bkma_mlp_create": (_st, [C.c_uint64, C.POINTER(_vp)]),
+    "bkma_mlp_create_stencil": (_st, [C.c_uint64, C.c_int32, C.POINTER(_vp)]),
+    "bkma_mlp_info": (_st, [_vp, _i32p, _i32p]),
+    "bkma_mlp_samples_grid": (_st, [C.c_int64, C.c_uint64, C.c_int64, C.c_int64, C.c_int32,
+                                    C.c_int32, _vp, _vp, _vp, _vp]),
     "bkma_mlp_params": (_st, [_vp, _vp, C.c_int32]),
     "bkma_mlp_samples": (_st, [C.c_int64, C.c_uint64, C.c_int64, _vp, _vp, _vp, _vp]),
     "bkma_mlp_grad": (_st, [_vp, _vp, _vp, _vp, C.c_int64, _vp, _dp, _vp]),
