@@ -178,7 +178,18 @@ void default_tile(AdvPlanImpl &p) {
     const void *aligned_probe = reinterpret_cast<const void *>(uintptr_t(256));
     p.path = (p.R == 1 && adv_tma_eligible(p, aligned_probe, p.W) &&
               adv_tma_smem(p, p.W) <= kMaxSmem) ? 1 : 0;
-    if (p.path == 1) p.threads = 512;
+    if (p.path == 1) {
+        // 32-column tiles while a tile stays within ~64 KB (n1 <= 512), and
+        // about eight row passes per thread. Measured (GCells/s, 16 columns x
+        // 512 threads before): 1024 x 128 x 2048 382 -> 876 (32 x 128),
+        // 4096 x 64 x 1024 244 -> 848, 512 x 256 x 2048 578 -> 874 (32 x 256),
+        // 2048 x 512 x 512 772 -> 881 (32 x 512); n1 = 1024 keeps 16 x 512.
+        if (p.desc.n1 * 32 * p.esize <= 65536 && adv_tma_eligible(p, aligned_probe, 32) &&
+            adv_tma_smem(p, 32) <= kMaxSmem)
+            p.W = 32;
+        const int64_t want = std::max<int64_t>(128, p.desc.n1 * p.W / 32);
+        p.threads = want >= 512 ? 512 : want >= 256 ? 256 : 128;
+    }
     // Streaming beats TMA tiles when a tile leaves one CTA per SM (n1 >= 2048:
     // 534 vs 760 GCells/s at 1024 x 2048 x 1024) or when rows are 1 MB or
     // more apart (1 x 1024 x 2^21: 400 vs 699, every box row a new page).
