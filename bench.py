@@ -341,6 +341,13 @@ def config1_block(bkma_gb300, dev, cores: int):
                                  torch.float64),
                  "fp32": (bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f32", **kw),
                           torch.float32)}
+        # the 10 steps in one launch, each line held in shared memory: the
+        # same bits as one step per launch (FP64 staged arithmetic; FP32)
+        for name, tdt, dt_name in (("staged_fp64_fused", torch.float64, "f64"),
+                                   ("fp32_fused", torch.float32, "f32")):
+            pl = bkma_gb300.AdvectionPlan(n0, n1, n2, dtype=dt_name, **kw)
+            pl.set_fusion(steps)
+            plans[name] = (pl, tdt)
         st = torch.cuda.current_stream()
         res = {}
         for name, (pl, tdt) in plans.items():
@@ -359,11 +366,17 @@ def config1_block(bkma_gb300, dev, cores: int):
             res[name] = d
             out[name] = {"gcells_s": n0 * n1 * n2 * steps / (statistics.median(times) / 1e3) / 1e9}
         ref = res["plain_fp64"]
-        for name in ("staged_fp64", "fp32"):
+        for name in ("staged_fp64", "fp32", "staged_fp64_fused", "fp32_fused"):
             e = plans["plain_fp64"][0].error_norms(res[name], ref)
             out[name]["max_rel_vs_plain"] = e["max_rel"]
+        out["staged_fp64_fused"]["bit_equal_to_one_step_per_launch"] = bool(
+            torch.equal(res["staged_fp64_fused"], res["staged_fp64"]))
+        out["fp32_fused"]["bit_equal_to_one_step_per_launch"] = bool(
+            torch.equal(res["fp32_fused"], res["fp32"]))
         out["speedup_staged_vs_plain"] = (out["staged_fp64"]["gcells_s"]
                                           / out["plain_fp64"]["gcells_s"])
+        out["speedup_fused_fp64_vs_plain"] = (out["staged_fp64_fused"]["gcells_s"]
+                                              / out["plain_fp64"]["gcells_s"])
         v, c, el = cpu_adv_fields_sample(
             [dict(n0=n0, n1=n1, n2=n2, degree=5, ref=True, velocity=vel, dt=DT)],
             cores, n0, steps)
@@ -1052,7 +1065,8 @@ def main():
     ap.add_argument("--n2", type=int, default=None, help="other column count (profiling captures)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="advection",
-                    choices=["advection", "conv", "batched", "learned", "fused", "fp64"],
+                    choices=["advection", "conv", "batched", "learned", "fused", "fp64",
+                             "config1"],
                     help="conv: only the conv1d block, as its own JSON line")
     ap.add_argument("--conv-batch", type=int, default=256, help="smaller batch for captures")
     ap.add_argument("--fields", type=int, default=64, help="batched workload: field count")
@@ -1071,10 +1085,14 @@ def main():
         WORKLOAD = f"single advection FP32 {N0}x{N1}x{N2}, degree 5 (profiling shape)"
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload in ("batched", "learned", "fused", "fp64") and args.impl != "reference":
+    if args.workload in ("batched", "learned", "fused", "fp64", "config1") and args.impl != "reference":
         import torch
         import bkma_gb300
         dev = torch.device("cuda", 0)
+        if args.workload == "config1":
+            r = config1_block(bkma_gb300, dev, os.cpu_count() or 1)
+            print(json.dumps(r))
+            return 0 if "error" not in r else 1
         if args.workload == "fp64":
             r = fp64_block(bkma_gb300, dev, args.steps, args.warmup, args.tile_w)
             print(json.dumps(r))
