@@ -22,9 +22,9 @@
 //    TwoSum into (S, err) so that S + sum(err) is the exact sum of the p; the
 //    small terms e, err, a l and b h accumulate in three FP32 partial sums
 //    (b l is below 2^-48 of the term and dropped);
-//  * output: (y, y') = Fast2Sum(S, L), widened to FP64 with integer operations
-//    and added with one DADD (correct rounding of the pair), one 16-byte
-//    store per column pair.
+//  * output: S and L widened to FP64 with integer operations and added with
+//    one DADD (correct rounding of the pair sum), one 16-byte store per
+//    column pair.
 //
 // The sum is within a few 2^-48 of sum_k |w_k f_k| of the FP64 direct form:
 // against the staged FP64 kernel the result differs by at most ~2e-13 max|f|
@@ -54,7 +54,7 @@ template <int WC> constexpr int ds_threads() { return kDsRuns * WC / 2; }
 __device__ __forceinline__ bool ds_splittable(double x) {
     const uint32_t xh = (uint32_t)__double2hiint(x), xl = (uint32_t)__double2loint(x);
     const uint32_t e = (xh >> 20) & 0x7FFu;
-    return (e - 949u < 200u) || (e == 0u && ((xh & 0xFFFFFu) | xl) == 0u);
+    return (e - 949u < 200u) || ((xh << 1) | xl) == 0u;  // in range, or +-0
 }
 
 // x = h + l + r, |r| <= 2^-48 |x| (x splittable). h keeps x's sign, exponent
@@ -130,11 +130,10 @@ __device__ __forceinline__ double2 ds_stencil(const float4 (&T)[NT], int u, cons
         s = t;
     }
     const float2 L = __fadd2_rn(__fadd2_rn(La, Lb), Le);
-    // Fast2Sum(s, L): |s| >= |L|
-    const float2 y = __fadd2_rn(s, L);
-    const float2 yl = __ffma2_rn(__ffma2_rn(s, m1, y), m1, L);  // L - (y - s)
-    return make_double2(__dadd_rn(ds_widen(y.x), ds_widen(yl.x)),
-                        __dadd_rn(ds_widen(y.y), ds_widen(yl.y)));
+    // s + L rounded once to FP64: both parts are exact in FP64, so one DADD
+    // of the widened parts is the correctly rounded pair sum
+    return make_double2(__dadd_rn(ds_widen(s.x), ds_widen(L.x)),
+                        __dadd_rn(ds_widen(s.y), ds_widen(L.y)));
 }
 
 // Rows per thread run of a CTA with `runs` runs over n1 rows.
