@@ -211,7 +211,7 @@ void default_tile(AdvPlanImpl &p) {
     if (adv_ds_shape_ok(p, 4) && adv_ds_smem(p, 4) <= kMaxSmem) {
         // FP64 storage in FP32-pair arithmetic (GB300's FP64 rate bounds the
         // FP64 staged kernel near 100 GCells/s): 4-column TMA tiles, six CTAs
-        // of 128 threads per SM (2048 x 1024 x 512: 301 GCells/s; 8-column
+        // of 128 threads per SM (2048 x 1024 x 512: 320 GCells/s; 8-column
         // tiles, three CTAs of 256 threads: 289)
         p.path = 4;
         p.W = 4;
