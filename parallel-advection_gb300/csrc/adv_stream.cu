@@ -121,6 +121,11 @@ __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group
     // would have covered.
     for (int j = max(a, a + d + (kRing - 1) * kU); j < min(b, a + d + (kRing - 1 + kPrefetch) * kU); ++j)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(src + (int64_t)j * n2));
+    // outputs are not read again this step: stores are marked first for L2
+    // eviction, so the prefetched rows ahead stay resident (batched workload
+    // 746 -> 754 GCells/s; the same hint on the loads: 514)
+    uint64_t evict_first;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(evict_first));
     float B[kRing * kU];
 #pragma unroll
     for (int i = 0; i < (kRing - 1) * kU; ++i) B[i] = ld(a + d + i);
@@ -159,7 +164,9 @@ __device__ __forceinline__ void stream_group(const StreamField &F, int64_t group
 #pragma unroll
                 for (int k = 0; k < NT; ++k)
                     if (k != C) acc = fmaf(w[k], B[(ph * kU + i + k) % (kRing * kU)] - fc, acc);
-                *po = fc + acc;
+                asm volatile("st.global.L1::no_allocate.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(po),
+                             "f"(fc + acc), "l"(evict_first)
+                             : "memory");
             }
             po += n2;
         }
