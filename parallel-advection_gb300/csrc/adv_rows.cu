@@ -2,8 +2,11 @@
 // floats, so a run of whole lines is one contiguous block of the field.
 //
 // A CTA stages R consecutive lines (R * n1 floats) into shared memory with
-// 16-byte cp.async (the block starts on a 16-byte boundary: n1 % 4 == 0 and
-// a 16-byte-aligned field), then each thread computes 4 consecutive cells of
+// one bulk copy (cp.async.bulk, completed on an mbarrier; the block starts on
+// a 16-byte boundary and is a multiple of 16 bytes long: n1 % 4 == 0 and a
+// 16-byte-aligned field; against 16-byte cp.async from every thread:
+// 2^21 lines of 1024 784 -> 836 GCells/s, 2^17 lines of 16384 784 -> 803,
+// 2^27 lines of 16 665 -> 669), then each thread computes 4 consecutive cells of
 // one line from a register window of npts + 3 staged values (the taps of 4
 // neighbouring cells overlap), read as aligned float4s (contiguous across the
 // lanes of a line: no bank conflicts; the periodic wrap falls on float4
@@ -22,6 +25,7 @@
 #include "adv_device.cuh"
 #include "adv_plan.cuh"
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace bkma {
 
@@ -29,18 +33,46 @@ namespace {
 
 constexpr int kRowsThreads = 256;
 
+// `polls` bounds the wait for the staged block; on a timeout the CTA raises
+// `status`, lets its copy land (a second bounded wait) and leaves without
+// writing.
 template <int NT>
-__global__ void __launch_bounds__(kRowsThreads) adv_rows_f32(AdvStagedArgs<float> a) {
+__global__ void __launch_bounds__(kRowsThreads) adv_rows_f32(AdvStagedArgs<float> a, int *status,
+                                                             uint32_t polls) {
     extern __shared__ __align__(16) float S[];
+    __shared__ __align__(8) uint64_t bar;
     constexpr int C = NT / 2 - 1;
     const int n1 = (int)a.n1;
     const int64_t line0 = (int64_t)blockIdx.x * a.R;
     const int nl = (int)min((int64_t)a.R, a.lines - line0);
     const int total = nl * n1;  // a multiple of 4
     const float *g = a.src + line0 * a.n1;
-    for (int i = (int)threadIdx.x * 4; i < total; i += kRowsThreads * 4) cp_async(S + i, g + i, 16);
-    cp_async_wait_all();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(&bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
     __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)total * 4u;
+        asm volatile(
+            "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
+                smem_u32addr(&bar)),
+            "r"(bytes)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                "r"(smem_u32addr(S)),
+            "l"(g), "r"(bytes), "r"(smem_u32addr(&bar))
+            : "memory");
+    }
+    if (!__syncthreads_and(staging_wait(&bar, polls))) {
+        if (threadIdx.x == 0) {
+            atomicExch(status, (int)BKMA_ERR_TIMEOUT);
+            staging_wait(&bar, kWaitPolls);
+        }
+        return;
+    }
     float *G = a.dst + line0 * a.n1;
     for (int i = (int)threadIdx.x * 4; i < total; i += kRowsThreads * 4) {
         const int l = i / n1;
@@ -142,7 +174,7 @@ cudaError_t launch_rows(const AdvPlanImpl &p, const void *src, void *dst, int R,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = (p.lines + R - 1) / R;
-    kern<<<grid_x(grid), kRowsThreads, smem, st>>>(a);
+    kern<<<grid_x(grid), kRowsThreads, smem, st>>>(a, p.d_status, p.wait_polls);
     return cudaGetLastError();
 }
 
@@ -161,7 +193,7 @@ bool adv_rows_shape_ok(const AdvPlanImpl &p) {
 bool adv_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R) {
     return adv_rows_shape_ok(p) && R >= 1 && ((uintptr_t)src % 16) == 0 &&
            ((uintptr_t)dst % 16) == 0 && (int64_t)R * p.desc.n1 <= (1 << 20) &&
-           adv_rows_smem(p, R) <= (size_t)227 * 1024;
+           adv_rows_smem(p, R) <= (size_t)227 * 1024 - 16;  // + the static barrier
 }
 
 int adv_rows_default_r(const AdvPlanImpl &p) {

@@ -1,7 +1,7 @@
 """Device-side timeout reporting, exercised without a stuck GPU.
 
-The kernels with device-side waits (the TMA-staged advection kernel and the
-tensor-core conv1d pipeline) bound every wait and report a timeout through a
+The kernels with device-side waits (the TMA-staged and contiguous-line
+advection kernels and the tensor-core conv1d pipeline) bound every wait and report a timeout through a
 status word that the plan's status call returns as BKMA_ERR_TIMEOUT (the
 reference raises C++ exceptions instead, src/core/bkma_tools.hpp:38-51). A
 plan's wait limit set to 0 makes every wait give up at once: the launch stops
@@ -44,6 +44,33 @@ def test_adv_tma_timeout_reported_then_cleared(bkma, cuda):
     # no tile was written: every CTA gave up before its stores
     assert torch.equal(d, f0)
     # the context is usable and the default limit gives the normal bits
+    plan.set_wait_limit(DEFAULT_POLLS)
+    plan.step(d)
+    plan.status()
+    fresh = bkma.AdvectionPlan(*shape, **kw)
+    want = f0.clone()
+    fresh.step(want)
+    fresh.status()
+    assert torch.equal(d, want)
+
+
+def test_adv_rows_timeout_reported_then_cleared(bkma, cuda):
+    """The contiguous-line kernel (n2 = 1) stages its lines with one bulk copy
+    completed on an mbarrier: its bounded wait reports the same way."""
+    import torch
+    shape = (64, 256, 1)
+    kw = dict(dtype="f32", dt=1e-3, minX=0.0, maxX=1.0, minVx=-1.0, maxVx=1.0)
+    plan = bkma.AdvectionPlan(*shape, **kw)
+    assert plan.info()["path"] == 3, plan.info()  # runs of contiguous lines
+    f0 = _field(cuda, shape, 5)
+    d = f0.clone()
+    plan.set_wait_limit(0)
+    plan.step(d)
+    with pytest.raises(bkma.BkmaError) as e:
+        plan.status()
+    assert e.value.status == 4  # BKMA_ERR_TIMEOUT
+    plan.status()  # cleared
+    assert torch.equal(d, f0)  # no CTA wrote its lines
     plan.set_wait_limit(DEFAULT_POLLS)
     plan.step(d)
     plan.status()
