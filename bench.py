@@ -319,7 +319,9 @@ def config1_block(bkma_gb300, dev, cores: int):
     sin(2 pi x) + U[-0.01, 0.01] from numpy's default_rng(12345), 10 steps.
     It is L2-resident (4 MiB): a parity workload, not a roofline one. Reports
     the plain FP64 kernel (the reference's per-cell math), the staged FP64
-    and FP32 kernels (GCells/s over 10-step runs, median of 5), their error
+    kernel (FP64 arithmetic), the FP64 default (contiguous lines in FP32-pair
+    arithmetic) and the FP32 kernels (GCells/s over 10-step runs, median of
+    5), their error
     against the plain form after the 10 steps, and the oracle on the host
     cores on the whole workload."""
     import numpy as np
@@ -335,10 +337,13 @@ def config1_block(bkma_gb300, dev, cores: int):
         f0 = np.ascontiguousarray(np.sin(2 * np.pi * x)[None, :, None]
                                   + NOISE * rng.uniform(-1, 1, (n0, n1, n2)))
         kw = dict(dt=DT, minX=MINX, maxX=MAXX, minVx=-1.0, maxVx=1.0, velocity=vel)
+        staged = bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f64", **kw)
+        staged.set_tile(1, 8, 256, 0)  # FP64 arithmetic, whole rows of 8 lines
         plans = {"plain_fp64": (bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f64", impl="plain",
                                                          **kw), torch.float64),
-                 "staged_fp64": (bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f64", **kw),
-                                 torch.float64),
+                 "staged_fp64": (staged, torch.float64),
+                 "pair_fp64": (bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f64", **kw),
+                               torch.float64),
                  "fp32": (bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f32", **kw),
                           torch.float32)}
         # the 10 steps in one launch, each line held in shared memory: the
@@ -366,7 +371,7 @@ def config1_block(bkma_gb300, dev, cores: int):
             res[name] = d
             out[name] = {"gcells_s": n0 * n1 * n2 * steps / (statistics.median(times) / 1e3) / 1e9}
         ref = res["plain_fp64"]
-        for name in ("staged_fp64", "fp32", "staged_fp64_fused", "fp32_fused"):
+        for name in ("staged_fp64", "pair_fp64", "fp32", "staged_fp64_fused", "fp32_fused"):
             e = plans["plain_fp64"][0].error_norms(res[name], ref)
             out[name]["max_rel_vs_plain"] = e["max_rel"]
         out["staged_fp64_fused"]["bit_equal_to_one_step_per_launch"] = bool(
@@ -377,6 +382,10 @@ def config1_block(bkma_gb300, dev, cores: int):
                                           / out["plain_fp64"]["gcells_s"])
         out["speedup_fused_fp64_vs_plain"] = (out["staged_fp64_fused"]["gcells_s"]
                                               / out["plain_fp64"]["gcells_s"])
+        out["speedup_pair_vs_plain"] = (out["pair_fp64"]["gcells_s"]
+                                        / out["plain_fp64"]["gcells_s"])
+        out["pair_fp64"]["kernel"] = ("adv_ds_rows (FP64 contiguous lines, FP32-pair "
+                                      "arithmetic; the FP64 plans' default for n2 = 1)")
         v, c, el = cpu_adv_fields_sample(
             [dict(n0=n0, n1=n1, n2=n2, degree=5, ref=True, velocity=vel, dt=DT)],
             cores, n0, steps)

@@ -52,8 +52,9 @@ typedef enum bkma_dtype { BKMA_F32 = 0, BKMA_F64 = 1, BKMA_BF16 = 2 } bkma_dtype
  * (out of place), "plain" (per-cell FP64 reference math), "staged" and
  * "gb300"/"cuda" (the per-line staged kernel). */
 /* AUTO and STAGED run the fastest kernel for the shape. For FP64 fields that
- * is, wherever the shape allows it (degree 3 or 5, even n2 >= 4, n1 >= 16,
- * lines that fit shared memory, a 16-byte aligned field), the kernel that
+ * is, wherever the shape allows it (degree 3 or 5, n1 >= 16, even n2 >= 4 or
+ * n2 = 1 with n1 % 4 == 0, lines that fit shared memory, a 16-byte aligned
+ * field), a kernel that
  * keeps FP64 in HBM but sums the stencil in FP32-pair arithmetic (GB300's
  * FP64 rate would otherwise bound the step near 100 GCells/s): it agrees with
  * FP64 arithmetic to about 2e-13 max|f| per step. bkma_adv_plan_set_tile
@@ -102,7 +103,8 @@ typedef struct bkma_adv_plan_info {
     int64_t tiles;             /* CTAs per step */
     int32_t path;              /* 0: cp.async staging, 1: TMA (cp.async.bulk.tensor) staging,
                                   2: streamed columns, 3: contiguous lines (n2 = 1),
-                                  4: FP64 in FP32-pair arithmetic (TMA staging) */
+                                  4: FP64 in FP32-pair arithmetic (TMA staging),
+                                  5: FP64 contiguous lines (n2 = 1) in FP32-pair arithmetic */
     int32_t reserved;
 } bkma_adv_plan_info;
 
@@ -134,7 +136,10 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * `threads` ignored: 256), or path 4: FP64 in FP32-pair arithmetic (FP64,
  * degree 3 or 5, even n2 >= W, n1 >= 16; W = 4 with 128 threads or W = 8 with
  * 256, R = 1; a field off the 16-byte grid runs the FP64 staged kernel on the
- * same tiles). R <= 1024 on paths 0, 1 and 3. */
+ * same tiles), or path 5: FP64 contiguous lines in FP32-pair arithmetic (FP64,
+ * degree 3 or 5, n2 = 1, n1 % 4 == 0, n1 >= 16; W = 1, R whole lines per CTA,
+ * `threads` ignored: 256; a field off the 16-byte grid runs the FP64 staged
+ * kernel on whole rows). R <= 1024 on paths 0, 1, 3 and 5. */
 bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
                                    int32_t path);
 /* Multi-step fusion: bkma_adv_step runs `steps_per_launch` time steps per

@@ -218,6 +218,13 @@ void default_tile(AdvPlanImpl &p) {
         p.R = 1;
         p.threads = adv_ds_threads(4);  // the FP32-pair kernel's CTA for the width
     }
+    if (adv_ds_rows_shape_ok(p) && adv_ds_rows_smem(p, adv_ds_rows_default_r(p)) <= kMaxSmem) {
+        // FP64 contiguous lines (n2 = 1) in the same FP32-pair arithmetic
+        p.path = 5;
+        p.W = 1;
+        p.R = adv_ds_rows_default_r(p);
+        p.threads = 256;  // the kernel's fixed CTA
+    }
 }
 
 template <typename T>
@@ -360,8 +367,10 @@ cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R
         return launch_staged_npts<float>(p, src, dst, p.exc_tile_w(kMaxSmem), 1, 256, st,
                                          p.d_exc_lines, p.n_exc);
     }
-    if (path == 3) {
-        if (adv_rows_eligible(p, src, dst, R)) return adv_rows_launch(p, src, dst, R, st);
+    if (path == 3 || path == 5) {
+        if (path == 3 && adv_rows_eligible(p, src, dst, R)) return adv_rows_launch(p, src, dst, R, st);
+        if (path == 5 && adv_ds_rows_eligible(p, src, dst, R))
+            return adv_ds_rows_launch(p, src, dst, R, st);
         // unaligned field: the generic staged kernel on whole rows
         W = 1;
         while (R > 1 && p.smem_bytes(W, R) > kMaxSmem) R /= 2;
@@ -500,8 +509,8 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
         }
     }
     // The plan's own tile is the first candidate, so tuning never ends on a
-    // tile slower than the default. An FP64 plan on the FP32-pair kernel
-    // (path 4) keeps it: the other FP64 kernels round differently, and
+    // tile slower than the default. An FP64 plan on an FP32-pair kernel
+    // (paths 4 and 5) keeps it: the other FP64 kernels round differently, and
     // tuning must not change results.
     std::vector<TuneVal> cands{{p.W, p.R, p.threads, p.path}};
     const int64_t n2 = p.desc.n2;
@@ -510,6 +519,10 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
         // the other tile width of the same kernel (same arithmetic per cell)
         for (int W : {4, 8})
             if (W != p.W && adv_ds_shape_ok(p, W)) cands.push_back({W, 1, adv_ds_threads(W), 4});
+    } else if (p.path == 5) {
+        // other line counts per CTA of the same kernel
+        for (int R = 1; R <= 1024 && R <= p.lines; R *= 2)
+            if (R != p.R && adv_ds_rows_eligible(p, field, field, R)) cands.push_back({1, R, 256, 5});
     } else if (n2 >= 8) {
         for (int W : {8, 16, 32, 64})
             if (W <= n2 || W == 8)
@@ -518,7 +531,7 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
                     if (adv_tma_eligible(p, field, W)) cands.push_back({W, 1, t, 1});
                 }
     }
-    const bool other = p.path != 4;
+    const bool other = p.path != 4 && p.path != 5;
     if (p.stream_ok && other)
         for (int segs : {0, 1, 2, 4, 8}) cands.push_back({(int)std::min<int64_t>(16, n2), segs, 256, 2});
     for (int R : {1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024})
@@ -540,7 +553,8 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
         const size_t need = c.path == 1 ? adv_tma_smem(p, c.W)
                             : c.path == 4 ? adv_ds_smem(p, c.W)
                             : c.path == 2 ? 0
-                            : c.path == 3 ? adv_rows_smem(p, c.R) : p.smem_bytes(c.W, c.R);
+                            : c.path == 3 ? adv_rows_smem(p, c.R)
+                            : c.path == 5 ? adv_ds_rows_smem(p, c.R) : p.smem_bytes(c.W, c.R);
         if (need > kMaxSmem) continue;
         cudaError_t err = launch_once(p, field, field, c.W, c.R, c.threads, c.path, st);  // warm-up
         if (err != cudaSuccess) {
@@ -676,10 +690,11 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
                                  : p.path == 4 ? adv_ds_smem(p, p.W)
                                  : p.path == 2 ? adv_stream_smem()
                                  : p.path == 3 ? adv_rows_smem(p, p.R)
+                                 : p.path == 5 ? adv_ds_rows_smem(p, p.R)
                                                : p.smem_bytes(p.W, p.R));
     info->npts = p.npts;
     info->autotuned = p.autotuned ? 1 : 0;
-    info->tiles = p.path == 3 ? (p.lines + p.R - 1) / p.R : p.tiles(p.W, p.R);
+    info->tiles = (p.path == 3 || p.path == 5) ? (p.lines + p.R - 1) / p.R : p.tiles(p.W, p.R);
     info->path = p.path;
     return BKMA_OK;
 } BKMA_ABI_CATCH("bkma_adv_plan_info_get")
@@ -714,7 +729,7 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
     BKMA_CHECK_ARG(W >= 1 && W <= 1024 && R >= (path == 2 ? 0 : 1) && R <= 1024,
                    "W must be in [1,1024], R in [1,1024] (path 2: row-segment mode 0..8)");
     BKMA_CHECK_ARG(threads == 128 || threads == 256 || threads == 512, "threads must be 128, 256 or 512");
-    BKMA_CHECK_ARG(path >= 0 && path <= 4, "path must be 0, 1, 2, 3 or 4");
+    BKMA_CHECK_ARG(path >= 0 && path <= 5, "path must be 0, 1, 2, 3, 4 or 5");
     BKMA_CHECK_ARG(path != 2 || p.stream_ok, "streamed form not available for this plan");
     BKMA_CHECK_ARG(path >= 2 || R == 1 || W >= p.desc.n2, "R > 1 needs whole-row tiles (W >= n2)");
     BKMA_CHECK_ARG(path != 2 || R <= 8, "path 2: R is the row-segment mode, 0 (auto) to 8");
@@ -734,6 +749,10 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                        "path 4 needs an FP64 plan of degree 3 or 5 with an even n2 >= W, n1 >= 16, "
                        "lines that fit shared memory, W = 4 (128 threads) or 8 (256 threads) "
                        "and R = 1");
+    } else if (path == 5) {
+        BKMA_CHECK_ARG(adv_ds_rows_shape_ok(p) && W == 1 && adv_ds_rows_smem(p, R) <= kMaxSmem,
+                       "path 5 needs an FP64 plan of degree 3 or 5 with n2 = 1, n1 % 4 == 0, "
+                       "n1 >= 16, W = 1 and R lines that fit shared memory");
     }
     p.W = W;
     p.R = R;

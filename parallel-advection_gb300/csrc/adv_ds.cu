@@ -296,6 +296,152 @@ cudaError_t launch_ds_t(const CUtensorMap &tm, const AdvDsArgs &a, size_t smem, 
     return cudaGetLastError();
 }
 
+// ---- contiguous lines (n2 = 1) in FP32-pair arithmetic
+//
+// A line is n1 consecutive doubles and a run of lines is one contiguous
+// block: a CTA stages R whole lines with one bulk copy (completed on an
+// mbarrier, bounded wait), then each thread computes 4 consecutive cells of
+// one line. Their NT + 3 taps (the windows of 4 neighbouring cells overlap)
+// are read as aligned double2s (the periodic wrap falls on double2
+// boundaries: n1 % 4 == 0), shifted in registers by the line's offset mod 2
+// and split once each; cells (c, c+1) and (c+2, c+3) are two lanes of the
+// packed FP32x2 stencil of the column-pair kernel (the same operations per
+// cell). A window holding a tap the split cannot carry, and exception lines,
+// run the staged kernel's FP64 arithmetic. The CTA has read its lines before
+// any store and no other CTA touches them, so in place is legal.
+constexpr int kDsRowsThreads = 256;
+
+struct AdvDsRowsArgs {
+    const double *src;
+    double *dst;
+    int64_t n1, lines;
+    int R;                     // lines per CTA
+    const int32_t *base;       // [lines]
+    const double *w;           // [lines][NT]
+    const float2 *w2;          // [lines][NT] FP32-pair weights
+    const int32_t *exc_index;  // [lines], or null when the plan has no exception lines
+    const AdvExcCell<double> *exc;
+    int *status;
+    uint32_t spin_limit;
+};
+
+template <int NT>
+__global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows(AdvDsRowsArgs a) {
+    extern __shared__ __align__(16) double Sd[];
+    __shared__ __align__(8) uint64_t bar;
+    const int n1 = (int)a.n1;
+    const int64_t line0 = (int64_t)blockIdx.x * a.R;
+    const int nl = (int)min((int64_t)a.R, a.lines - line0);
+    const int total = nl * n1;  // a multiple of 4
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(&bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)total * 8u;
+        asm volatile(
+            "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
+                smem_u32addr(&bar)),
+            "r"(bytes)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                "r"(smem_u32addr(Sd)),
+            "l"(a.src + line0 * a.n1), "r"(bytes), "r"(smem_u32addr(&bar))
+            : "memory");
+    }
+    if (!__syncthreads_and(staging_wait(&bar, a.spin_limit))) {
+        if (threadIdx.x == 0) {
+            atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
+            staging_wait(&bar, kWaitPolls);  // let the copy land before the CTA leaves
+        }
+        return;
+    }
+    constexpr int NW = NT + 3;            // taps of 4 consecutive cells
+    constexpr int NV = (NW + 2) / 2;      // double2s covering them from an even start
+    double *G = a.dst + line0 * a.n1;
+    for (int i = (int)threadIdx.x * 4; i < total; i += kDsRowsThreads * 4) {
+        const int l = i / n1;
+        const int c0 = i - l * n1;
+        const int64_t line = line0 + l;
+        const double *Sl = Sd + (size_t)l * n1;
+        const int exc = a.exc_index ? a.exc_index[line] : -1;
+        double o[4];
+        if (exc < 0) {
+            int q = c0 + a.base[line];
+            if (q >= n1) q -= n1;
+            double v[2 * NV];
+            int q2 = q & ~1;
+#pragma unroll
+            for (int j = 0; j < NV; ++j) {
+                const double2 t = *reinterpret_cast<const double2 *>(Sl + q2);
+                v[2 * j] = t.x;
+                v[2 * j + 1] = t.y;
+                q2 = q2 + 2 == n1 ? 0 : q2 + 2;
+            }
+            double f[NW];
+            const bool odd = (q & 1) != 0;  // the same for every thread of a line
+#pragma unroll
+            for (int j = 0; j < NW; ++j) f[j] = odd ? v[j + 1] : v[j];
+            float h[NW], lo[NW];
+            bool ok = true;
+#pragma unroll
+            for (int j = 0; j < NW; ++j) {
+                ds_split(f[j], h[j], lo[j]);
+                ok = ok && ds_splittable(f[j]);
+            }
+            if (ok) {
+                float2 A[NT], B[NT];
+#pragma unroll
+                for (int k = 0; k < NT; ++k) {
+                    const float2 ab = a.w2[line * NT + k];
+                    A[k] = make_float2(ab.x, ab.x);
+                    B[k] = make_float2(ab.y, ab.y);
+                }
+#pragma unroll
+                for (int pr = 0; pr < 2; ++pr) {
+                    float4 T[NT];
+#pragma unroll
+                    for (int k = 0; k < NT; ++k)
+                        T[k] = make_float4(h[2 * pr + k], h[2 * pr + k + 1], lo[2 * pr + k],
+                                           lo[2 * pr + k + 1]);
+                    const double2 r = ds_stencil<NT>(T, 0, A, B);
+                    o[2 * pr] = r.x;
+                    o[2 * pr + 1] = r.y;
+                }
+            } else {
+                // FP64 direct form, the staged kernel's arithmetic
+                double w64[NT];
+#pragma unroll
+                for (int k = 0; k < NT; ++k) w64[k] = a.w[line * NT + k];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) o[m] = stencil_cell<double, NT>(f + m, 1, w64);
+            }
+        } else {
+            // per-cell stencils of an exception line, FP64 arithmetic
+            const AdvExcCell<double> *cells = a.exc + (int64_t)exc * n1;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const AdvExcCell<double> &e = cells[c0 + m];
+                int q = c0 + m + e.base;
+                if (q >= n1) q -= n1;
+                double f[NT], we[NT];
+#pragma unroll
+                for (int k = 0; k < NT; ++k) {
+                    f[k] = Sl[q];
+                    we[k] = e.w[k];
+                    q = q + 1 == n1 ? 0 : q + 1;
+                }
+                o[m] = stencil_cell<double, NT>(f, 1, we);
+            }
+        }
+        *reinterpret_cast<double2 *>(G + i) = make_double2(o[0], o[1]);
+        *reinterpret_cast<double2 *>(G + i + 2) = make_double2(o[2], o[3]);
+    }
+}
+
 }  // namespace
 
 size_t adv_ds_smem(const AdvPlanImpl &p, int W) {
@@ -345,6 +491,50 @@ cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cud
     }
     if (p.npts == 6) return launch_ds_t<6, 8>(*tm, a, smem, grid, st);
     return launch_ds_t<4, 8>(*tm, a, smem, grid, st);
+}
+
+size_t adv_ds_rows_smem(const AdvPlanImpl &p, int R) {
+    return (size_t)R * (size_t)p.desc.n1 * sizeof(double);
+}
+
+bool adv_ds_rows_shape_ok(const AdvPlanImpl &p) {
+    return p.desc.dtype == BKMA_F64 && p.desc.impl != BKMA_ADV_PLAIN && p.d_w2 != nullptr &&
+           p.desc.n2 == 1 && p.desc.n1 % 4 == 0 && p.desc.n1 >= 16 &&
+           (p.npts == 4 || p.npts == 6) && p.lines * p.desc.n1 < (1ll << 40);
+}
+
+bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R) {
+    return adv_ds_rows_shape_ok(p) && R >= 1 && ((uintptr_t)src % 16) == 0 &&
+           ((uintptr_t)dst % 16) == 0 && (int64_t)R * p.desc.n1 <= (1 << 20) &&
+           adv_ds_rows_smem(p, R) <= (size_t)227 * 1024 - 16;  // + the static barrier
+}
+
+int adv_ds_rows_default_r(const AdvPlanImpl &p) {
+    // about 4096 cells (32 KB of shared memory) per CTA, whole lines
+    const int64_t r = std::max<int64_t>(1, 4096 / p.desc.n1);
+    return (int)std::min<int64_t>(r, p.lines);
+}
+
+cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int R, cudaStream_t st) {
+    AdvDsRowsArgs a;
+    a.src = (const double *)src;
+    a.dst = (double *)dst;
+    a.n1 = p.desc.n1;
+    a.lines = p.lines;
+    a.R = R;
+    a.base = p.d_base;
+    a.w = (const double *)p.d_w;
+    a.w2 = p.d_w2;
+    a.exc_index = p.n_exc > 0 ? p.d_exc_index : nullptr;
+    a.exc = (const AdvExcCell<double> *)p.d_exc;
+    a.status = p.d_status;
+    a.spin_limit = p.wait_polls;
+    const size_t smem = adv_ds_rows_smem(p, R);
+    auto kern = p.npts == 6 ? adv_ds_rows<6> : adv_ds_rows<4>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid_x((p.lines + R - 1) / R), kDsRowsThreads, smem, st>>>(a);
+    return cudaGetLastError();
 }
 
 }  // namespace bkma

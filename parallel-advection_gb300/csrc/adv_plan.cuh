@@ -161,6 +161,13 @@ bool adv_ds_eligible(const AdvPlanImpl &p, const void *src, int W);
 size_t adv_ds_smem(const AdvPlanImpl &p, int W);
 int adv_ds_threads(int W);
 cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cudaStream_t st);
+// The same arithmetic on contiguous lines (FP64, n2 = 1, n1 % 4 == 0, n1 >=
+// 16, degree 3 or 5): R whole lines per CTA, 4 cells per thread (path 5).
+bool adv_ds_rows_shape_ok(const AdvPlanImpl &p);
+bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R);
+size_t adv_ds_rows_smem(const AdvPlanImpl &p, int R);
+int adv_ds_rows_default_r(const AdvPlanImpl &p);
+cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int R, cudaStream_t st);
 
 bool adv_tma_eligible(const AdvPlanImpl &p, const void *src, int W);
 size_t adv_tma_smem(const AdvPlanImpl &p, int W);

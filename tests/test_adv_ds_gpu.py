@@ -1,5 +1,6 @@
-"""FP64 advection in FP32-pair arithmetic (the FP64 plans' default kernel
-where the shape allows it: degree 3 or 5, an even n2 >= 8), through the C ABI.
+"""FP64 advection in FP32-pair arithmetic (the FP64 plans' default kernels
+where the shape allows it: degree 3 or 5 with column pairs of an even n2 >= 4,
+or contiguous lines of n2 = 1 with n1 % 4 == 0), through the C ABI.
 
 Tolerances:
   - against the staged FP64 kernel (FP64 direct form sum_k w_k f_k, the same
@@ -214,5 +215,184 @@ def test_ds_autotune_keeps_the_pair_kernel(bkma, cuda):
     a, b = f0.clone(), f0.clone()
     ds.step(a, nsteps=2)
     fresh, _ = _plans(bkma, p)
+    fresh.step(b, nsteps=2)
+    assert torch.equal(a, b)
+
+
+# ---- contiguous lines (n2 = 1): the same arithmetic, 4 cells per thread (path 5)
+
+ROWS_CASES = [
+    # n0, n1, n2, dt, minX, maxX, minVx, maxVx
+    (64, 1024, 1, 0.001, 0.0, 1.0, -1.0, 1.0),
+    (16, 1000, 1, 0.0011, 0.0, 1.0, -1.0, 1.0),   # odd shifts of many lines, n1 % 8 != 0
+    (300, 64, 1, 0.003, 0.0, 1.0, -2.0, 2.0),     # many short lines per CTA, ragged last CTA
+    (9, 256, 1, 0.02, 0.0, 1.0, -3.0, 3.0),       # shifts of several cells
+    (5, 16, 1, 0.01, -0.5, 1.5, -1.0, 1.0),       # the shortest lines the kernel takes
+]
+
+
+def _rows_plans(bkma, p, **kw):
+    args = dict(dt=p.dt, minX=p.minX, maxX=p.maxX, minVx=p.minVx, maxVx=p.maxVx, dtype="f64")
+    args.update(kw)
+    ds = bkma.AdvectionPlan(p.n0, p.n1, p.n2, **args)
+    st = bkma.AdvectionPlan(p.n0, p.n1, p.n2, **args)
+    st.set_tile(1, 8, 256, 0)  # the FP64-arithmetic staged kernel on whole rows
+    return ds, st
+
+
+@pytest.mark.parametrize("case", ROWS_CASES)
+@pytest.mark.parametrize("degree", [5, 3])
+def test_ds_rows_close_to_staged_and_oracle(bkma, cuda, oracle, case, degree):
+    import torch
+    p = AdvParams(*case)
+    weights = "reference" if degree == 5 else "lagrange"
+    ds, st = _rows_plans(bkma, p, degree=degree, weights=weights)
+    assert ds.info()["path"] == 5, ds.info()
+    f0 = _init(p, 11)
+    steps = 4
+    a = torch.tensor(f0, device=cuda)
+    b = torch.tensor(f0, device=cuda)
+    ds.step(a, nsteps=steps)
+    st.step(b, nsteps=steps)
+    ds.status()
+    scale = b.abs().max().item()
+    assert (a - b).abs().max().item() <= TOL * steps * scale
+    want = oracle.adv_step(p, f0.copy(), steps, degree=degree, ref_weights=degree == 5)
+    assert np.abs(a.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_ds_rows_line_counts_bit_identical(bkma, cuda):
+    """Any number of lines per CTA runs the same arithmetic per cell."""
+    import torch
+    p = AdvParams(*ROWS_CASES[2])
+    f0 = _init(p, 12)
+    ref = None
+    for R in (1, 7, 64):
+        plan, _ = _rows_plans(bkma, p)
+        plan.set_tile(1, R, 256, 5)
+        d = torch.tensor(f0, device=cuda)
+        plan.step(d, nsteps=3)
+        plan.status()
+        if ref is None:
+            ref = d
+        else:
+            assert torch.equal(d, ref)
+
+
+def test_ds_rows_inplace_equals_out_of_place(bkma, cuda):
+    import torch
+    p = AdvParams(*ROWS_CASES[0])
+    ds, _ = _rows_plans(bkma, p)
+    f0 = _init(p, 13)
+    a = torch.tensor(f0, device=cuda)
+    ds.step(a, nsteps=3)
+    oop = bkma.AdvectionPlan(p.n0, p.n1, p.n2, dtype="f64", dt=p.dt, minVx=p.minVx,
+                             maxVx=p.maxVx, inplace=False)
+    assert oop.info()["path"] == 5
+    src = torch.tensor(f0, device=cuda)
+    out = torch.empty_like(src)
+    oop.step(src, out=out, nsteps=3)
+    assert torch.equal(a, out)
+
+
+@pytest.mark.parametrize("value", [1e200, 1e-30, float("inf")])
+def test_ds_rows_unsplittable_value_runs_fp64(bkma, cuda, value):
+    """Every cell whose stencil reads a value the pair cannot carry is computed
+    in FP64 (the staged kernel's bits); the rest stay within the bound."""
+    import torch
+    p = AdvParams(4, 256, 1, 0.003, 0.0, 1.0, -1.0, 1.0)
+    ds, st = _rows_plans(bkma, p)
+    f0 = _init(p, 14)
+    i0, r_bad = 2, 100
+    f0[i0, r_bad, 0] = value
+    a = torch.tensor(f0, device=cuda)
+    b = torch.tensor(f0, device=cuda)
+    ds.step(a)
+    st.step(b)
+    ds.status()
+    offs, _ = ds.line_table()
+    rows = [r for r in range(p.n1) if (r_bad - (r + int(offs[i0]))) % p.n1 < 6]
+    assert len(rows) == 6
+    hit = torch.zeros_like(a, dtype=torch.bool)
+    hit[i0, rows, 0] = True
+    assert torch.allclose(a[hit], b[hit], rtol=0, atol=0, equal_nan=True)
+    other = ~hit & torch.isfinite(b)
+    diff = (a - b)[other].abs().max().item()
+    assert diff <= TOL * b[other].abs().max().item()
+
+
+def test_ds_rows_zero_field_stays_zero(bkma, cuda):
+    import torch
+    p = AdvParams(8, 512, 1, 0.001, 0.0, 1.0, -1.0, 1.0)
+    ds, _ = _rows_plans(bkma, p)
+    z = torch.zeros((p.n0, p.n1, p.n2), dtype=torch.float64, device=cuda)
+    ds.step(z, nsteps=3)
+    assert torch.count_nonzero(z).item() == 0
+
+
+def test_ds_rows_exception_lines_bit_identical_to_staged(bkma, cuda, oracle):
+    import torch
+    p = AdvParams(6, 1000, 1, 0.001, 0.0, 1.0, -2.0, 3.0)
+    vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
+    ds, st = _rows_plans(bkma, p, velocity=vel)
+    assert ds.info()["exception_lines"] > 0 and ds.info()["path"] == 5
+    f0 = _init(p, 15)
+    a = torch.tensor(f0, device=cuda)
+    b = torch.tensor(f0, device=cuda)
+    ds.step(a, nsteps=2)
+    st.step(b, nsteps=2)
+    exc = [i0 for i0 in range(p.n0)
+           if len({(oracle.departure(p, i1, vel[i0])[0] - i1) % p.n1 for i1 in range(p.n1)}) > 1]
+    assert exc and len(exc) == ds.info()["exception_lines"]
+    for i0 in exc:
+        assert torch.equal(a[i0], b[i0]), i0
+    assert (a - b).abs().max().item() <= TOL * 2 * b.abs().max().item()
+
+
+def test_ds_rows_misaligned_field_runs_fp64(bkma, cuda):
+    import torch
+    p = AdvParams(*ROWS_CASES[0])
+    ds, st = _rows_plans(bkma, p)
+    f0 = _init(p, 16)
+    buf = torch.empty(f0.size + 1, dtype=torch.float64, device=cuda)
+    d = buf[1:].view(f0.shape)  # 8 bytes past a 16-byte boundary
+    d.copy_(torch.tensor(f0, device=cuda))
+    ds.step(d, nsteps=2)
+    b = torch.tensor(f0, device=cuda)
+    st.step(b, nsteps=2)
+    assert torch.equal(d, b)
+
+
+def test_ds_rows_timeout_reported(bkma, cuda):
+    import torch
+    p = AdvParams(*ROWS_CASES[0])
+    ds, _ = _rows_plans(bkma, p)
+    f0 = torch.tensor(_init(p, 17), device=cuda)
+    a = f0.clone()
+    ds.set_wait_limit(0)
+    ds.step(a)
+    with pytest.raises(bkma.BkmaError) as e:
+        ds.status()
+    assert e.value.status == 4
+    assert torch.equal(a, f0)
+    ds.set_wait_limit(1 << 22)
+    ds.step(a)
+    ds.status()
+    b = f0.clone()
+    ds2, _ = _rows_plans(bkma, p)
+    ds2.step(b)
+    assert torch.equal(a, b)
+
+
+def test_ds_rows_autotune_keeps_the_kernel(bkma, cuda):
+    import torch
+    p = AdvParams(*ROWS_CASES[1])
+    ds, _ = _rows_plans(bkma, p)
+    f0 = torch.tensor(_init(p, 18), device=cuda)
+    info = ds.autotune(f0.clone())
+    assert info["path"] == 5
+    a, b = f0.clone(), f0.clone()
+    ds.step(a, nsteps=2)
+    fresh, _ = _rows_plans(bkma, p)
     fresh.step(b, nsteps=2)
     assert torch.equal(a, b)

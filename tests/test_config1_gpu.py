@@ -6,7 +6,8 @@ sin(2 pi x) + U[-0.01, 0.01] from numpy's default_rng(12345), 10 steps.
 
 - the plain FP64 kernel (the reference's per-cell math) is bit-exact with the
   oracle after every step;
-- the staged FP64 kernel is within 1e-11 max|f| of it (per-line weights);
+- the FP64 default (contiguous lines in FP32-pair arithmetic) and the staged
+  FP64 kernel are within 1e-11 max|f| of it (per-line weights);
 - the FP32 kernels are within the FP32 storage bound.
 
 A second case runs the reference's own law (v_i = minVx + i (maxVx - minVx) /
@@ -56,12 +57,17 @@ def test_config1_plain_fp64_bitexact_every_step(bkma, cuda, oracle):
         assert np.array_equal(d.cpu().numpy(), want), f"step {step}"
 
 
-def test_config1_staged_fp64(bkma, cuda, oracle):
+@pytest.mark.parametrize("path", [None, 0])  # the default (FP32-pair contiguous lines), FP64 staged
+def test_config1_staged_fp64(bkma, cuda, oracle, path):
     import torch
     p, vel = _params(), _velocity()
     f0 = _init()
     want = oracle.adv_step(p, f0.copy(), STEPS, velocity=vel)
     plan = _plan(bkma, dtype="f64")
+    if path is None:
+        assert plan.info()["path"] == 5, plan.info()
+    else:
+        plan.set_tile(1, 8, 256, path)
     d = torch.tensor(f0, dtype=torch.float64, device=cuda)
     plan.step(d, nsteps=STEPS)
     plan.status()
