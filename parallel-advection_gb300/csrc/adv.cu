@@ -208,11 +208,14 @@ void default_tile(AdvPlanImpl &p) {
         p.R = adv_rows_default_r(p);
         p.threads = 256;  // the contiguous-line kernel's fixed CTA
     }
-    if (adv_ds_shape_ok(p, 4) && adv_ds_smem(p, 4) <= kMaxSmem) {
+    if (adv_ds_shape_ok(p, 4) && p.desc.n1 >= 128 && adv_ds_smem(p, 4) <= kMaxSmem) {
         // FP64 storage in FP32-pair arithmetic (GB300's FP64 rate bounds the
         // FP64 staged kernel near 100 GCells/s): 4-column TMA tiles, six CTAs
-        // of 128 threads per SM (2048 x 1024 x 512: 320 GCells/s; 8-column
-        // tiles, three CTAs of 256 threads: 289)
+        // of 128 threads per SM (2048 x 1024 x 512: 333 GCells/s; 8-column
+        // tiles, three CTAs of 256 threads: 289). Lines shorter than 128 rows
+        // leave runs of one or two rows that re-split most taps and stay on
+        // the staged kernel (x 128 columns, 2^27 cells, GCells/s pair / staged:
+        // n1 = 16 33 / 100, 64 97 / 100, 128 151 / 98, 256 216 / 99)
         p.path = 4;
         p.W = 4;
         p.R = 1;

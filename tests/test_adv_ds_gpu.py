@@ -1,6 +1,7 @@
 """FP64 advection in FP32-pair arithmetic (the FP64 plans' default kernels
-where the shape allows it: degree 3 or 5 with column pairs of an even n2 >= 4,
-or contiguous lines of n2 = 1 with n1 % 4 == 0), through the C ABI.
+where the shape allows it: degree 3 or 5 with column pairs of an even n2 >= 4
+and n1 >= 128, or contiguous lines of n2 = 1 with n1 % 4 == 0), through the
+C ABI.
 
 Tolerances:
   - against the staged FP64 kernel (FP64 direct form sum_k w_k f_k, the same
@@ -25,7 +26,7 @@ DS_CASES = [
     (4, 1000, 10, 0.0011, 0.0, 1.0, -1.0, 1.0),   # 8 + 2 columns: ragged last tile
     (2, 2048, 16, 0.0007, 0.0, 1.0, -2.0, 2.0),
     (5, 300, 8, 0.02, 0.0, 1.0, -3.0, 3.0),       # shifts of several cells
-    (3, 64, 24, 0.01, -0.5, 1.5, -1.0, 1.0),
+    (3, 128, 24, 0.01, -0.5, 1.5, -1.0, 1.0),     # the shortest lines it is the default for
 ]
 TOL = 2e-13
 
@@ -396,3 +397,13 @@ def test_ds_rows_autotune_keeps_the_kernel(bkma, cuda):
     fresh, _ = _rows_plans(bkma, p)
     fresh.step(b, nsteps=2)
     assert torch.equal(a, b)
+
+
+def test_ds_short_lines_stay_on_the_staged_kernel(bkma, cuda):
+    """Below 128 rows the column-pair kernel's runs are too short: the default
+    is the FP64-arithmetic staged kernel; path 4 can still be chosen."""
+    p = AdvParams(64, 64, 128, 0.001, 0.0, 1.0, -1.0, 1.0)
+    plan = bkma.AdvectionPlan(p.n0, p.n1, p.n2, dtype="f64", dt=p.dt, minVx=p.minVx,
+                              maxVx=p.maxVx)
+    assert plan.info()["path"] == 0, plan.info()
+    assert plan.set_tile(4, 1, 128, 4)["path"] == 4
