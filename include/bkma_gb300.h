@@ -52,9 +52,10 @@ typedef enum bkma_dtype { BKMA_F32 = 0, BKMA_F64 = 1, BKMA_BF16 = 2 } bkma_dtype
  * (out of place), "plain" (per-cell FP64 reference math), "staged" and
  * "gb300"/"cuda" (the per-line staged kernel). */
 /* AUTO and STAGED run the fastest kernel for the shape. For FP64 fields that
- * is, wherever the shape allows it (degree 3 or 5, n1 >= 16, even n2 >= 4 or
- * n2 = 1 with n1 % 4 == 0, lines that fit shared memory, a 16-byte aligned
- * field), a kernel that
+ * is, wherever the shape allows it (degree 3 or 5; column pairs of an even
+ * n2 with n1 >= 128, staged in shared memory or, for strips too tall or rows
+ * 1 MB or more apart, streamed; or n2 = 1 with n1 % 4 == 0; a 16-byte
+ * aligned field), a kernel that
  * keeps FP64 in HBM but sums the stencil in FP32-pair arithmetic (GB300's
  * FP64 rate would otherwise bound the step near 100 GCells/s): it agrees with
  * FP64 arithmetic to about 2e-13 max|f| per step. bkma_adv_plan_set_tile
@@ -104,7 +105,8 @@ typedef struct bkma_adv_plan_info {
     int32_t path;              /* 0: cp.async staging, 1: TMA (cp.async.bulk.tensor) staging,
                                   2: streamed columns, 3: contiguous lines (n2 = 1),
                                   4: FP64 in FP32-pair arithmetic (TMA staging),
-                                  5: FP64 contiguous lines (n2 = 1) in FP32-pair arithmetic */
+                                  5: FP64 contiguous lines (n2 = 1) in FP32-pair arithmetic,
+                                  6: FP64 column pairs streamed in FP32-pair arithmetic */
     int32_t reserved;
 } bkma_adv_plan_info;
 
@@ -139,7 +141,12 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * same tiles), or path 5: FP64 contiguous lines in FP32-pair arithmetic (FP64,
  * degree 3 or 5, n2 = 1, n1 % 4 == 0, n1 >= 16; W = 1, R whole lines per CTA,
  * `threads` ignored: 256; a field off the 16-byte grid runs the FP64 staged
- * kernel on whole rows). R <= 1024 on paths 0, 1, 3 and 5. */
+ * kernel on whole rows), or path 6: FP64 column pairs streamed in FP32-pair
+ * arithmetic (FP64, degree 3 or 5, even n2, n1 >= 64, every line's per-step
+ * shift d within -2 npts < d <= 24 - npts + 1; R the row-segment mode as on
+ * path 2, `threads` ignored: 256; the same bits as path 4; exception lines
+ * and a field off the 16-byte grid run the FP64 staged kernel). R <= 1024 on
+ * paths 0, 1, 3 and 5. */
 bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, int32_t threads,
                                    int32_t path);
 /* Multi-step fusion: bkma_adv_step runs `steps_per_launch` time steps per

@@ -221,6 +221,16 @@ void default_tile(AdvPlanImpl &p) {
         p.R = 1;
         p.threads = adv_ds_threads(4);  // the FP32-pair kernel's CTA for the width
     }
+    if (adv_stream_ds_shape_ok(p) && adv_stream_ds_smem(p) <= kMaxSmem && p.desc.n1 >= 128 &&
+        (p.path != 4 || n2 * 8 >= (1 << 20))) {
+        // FP64 column pairs that the staged form cannot take (strips too tall
+        // for shared memory) or takes badly (rows 1 MB or more apart: every
+        // TMA box row its own DRAM page): the streamed FP32-pair form
+        p.path = 6;
+        p.W = (int)std::min<int64_t>(8, n2);  // the staged passes' tile width
+        p.R = 0;                              // row-segment mode: from the size
+        p.threads = 256;
+    }
     if (adv_ds_rows_shape_ok(p) && adv_ds_rows_smem(p, adv_ds_rows_default_r(p)) <= kMaxSmem) {
         // FP64 contiguous lines (n2 = 1) in the same FP32-pair arithmetic
         p.path = 5;
@@ -370,6 +380,19 @@ cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R
         return launch_staged_npts<float>(p, src, dst, p.exc_tile_w(kMaxSmem), 1, 256, st,
                                          p.d_exc_lines, p.n_exc);
     }
+    if (path == 6 && adv_stream_ds_eligible(p, src, dst)) {
+        // streamed FP32-pair lines, then the exception lines through the staged kernel
+        cudaError_t e = adv_stream_ds_launch(p, src, dst, R, st);
+        if (e != cudaSuccess || p.n_exc == 0) return e;
+        return launch_staged_npts<double>(p, src, dst, p.exc_tile_w(kMaxSmem), 1, 256, st,
+                                          p.d_exc_lines, p.n_exc);
+    }
+    if (path == 6) {
+        // a field off the 16-byte grid: the FP64 staged kernel on strips that fit
+        W = std::max(1, p.exc_tile_w(kMaxSmem));
+        R = 1;
+        threads = 256;
+    }
     if (path == 3 || path == 5) {
         if (path == 3 && adv_rows_eligible(p, src, dst, R)) return adv_rows_launch(p, src, dst, R, st);
         if (path == 5 && adv_ds_rows_eligible(p, src, dst, R))
@@ -493,6 +516,18 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
     for (int64_t l = 0; l < p.lines && p.stream_ok; ++l)
         if (p.exc_index[(size_t)l] < 0 && !stream_line_ok(p.base[(size_t)l], n1, NT))
             p.stream_ok = false;
+    if (d.dtype == BKMA_F64) {
+        // the streamed FP32-pair form loads 2 NT rows ahead of its stores
+        p.ds_stream_ok = n1 >= kStreamMinN1;
+        p.ds_sa = p.ds_sb = 0;
+        for (int64_t l = 0; l < p.lines && p.ds_stream_ok; ++l) {
+            if (p.exc_index[(size_t)l] >= 0) continue;
+            const int dd = stream_offset(p.base[(size_t)l], n1);
+            if (!stream_line_ok(p.base[(size_t)l], n1, NT) || dd <= -2 * NT) p.ds_stream_ok = false;
+            p.ds_sa = std::max(p.ds_sa, dd + NT - 1);
+            p.ds_sb = std::max(p.ds_sb, -dd);
+        }
+    }
     if (d.dtype == BKMA_F32) return upload_tables<float>(p);
     return upload_tables<double>(p);
 }
@@ -518,10 +553,16 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     std::vector<TuneVal> cands{{p.W, p.R, p.threads, p.path}};
     const int64_t n2 = p.desc.n2;
     const int ths[3] = {128, 256, 512};
-    if (p.path == 4) {
-        // the other tile width of the same kernel (same arithmetic per cell)
+    if (p.path == 4 || p.path == 6) {
+        // the other forms of the same arithmetic per cell (same bits): tile
+        // widths of the staged column-pair kernel, row segments of the streamed one
         for (int W : {4, 8})
-            if (W != p.W && adv_ds_shape_ok(p, W)) cands.push_back({W, 1, adv_ds_threads(W), 4});
+            if ((p.path != 4 || W != p.W) && adv_ds_shape_ok(p, W) && p.desc.n1 >= 16)
+                cands.push_back({W, 1, adv_ds_threads(W), 4});
+        if (adv_stream_ds_eligible(p, field, field))
+            for (int segs : {0, 1, 2, 4, 8})
+                if (p.path != 6 || segs != p.R)
+                    cands.push_back({(int)std::min<int64_t>(8, n2), segs, 256, 6});
     } else if (p.path == 5) {
         // other line counts per CTA of the same kernel
         for (int R = 1; R <= 1024 && R <= p.lines; R *= 2)
@@ -534,7 +575,7 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
                     if (adv_tma_eligible(p, field, W)) cands.push_back({W, 1, t, 1});
                 }
     }
-    const bool other = p.path != 4 && p.path != 5;
+    const bool other = p.path != 4 && p.path != 5 && p.path != 6;
     if (p.stream_ok && other)
         for (int segs : {0, 1, 2, 4, 8}) cands.push_back({(int)std::min<int64_t>(16, n2), segs, 256, 2});
     for (int R : {1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024})
@@ -555,7 +596,7 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     for (const TuneVal &c : cands) {
         const size_t need = c.path == 1 ? adv_tma_smem(p, c.W)
                             : c.path == 4 ? adv_ds_smem(p, c.W)
-                            : c.path == 2 ? 0
+                            : c.path == 2 || c.path == 6 ? (c.path == 6 ? adv_stream_ds_smem(p) : 0)
                             : c.path == 3 ? adv_rows_smem(p, c.R)
                             : c.path == 5 ? adv_ds_rows_smem(p, c.R) : p.smem_bytes(c.W, c.R);
         if (need > kMaxSmem) continue;
@@ -674,7 +715,7 @@ bkma_status bkma_adv_plan_create(const bkma_adv_desc *desc, bkma_adv_plan **plan
     }
     default_tile(p);
     // the staged kernel runs every line, or (streamed form) the exception lines
-    const bool too_long = p.path == 2 ? (p.n_exc > 0 && p.exc_tile_w(kMaxSmem) == 0)
+    const bool too_long = (p.path == 2 || p.path == 6) ? (p.n_exc > 0 && p.exc_tile_w(kMaxSmem) == 0)
                                       : p.smem_bytes(p.W, p.R) > kMaxSmem;
     if (too_long) return fail(BKMA_ERR_UNSUPPORTED, "n1 too long for a shared-memory line tile");
     *plan = pl.release();
@@ -694,6 +735,7 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
                                  : p.path == 2 ? adv_stream_smem()
                                  : p.path == 3 ? adv_rows_smem(p, p.R)
                                  : p.path == 5 ? adv_ds_rows_smem(p, p.R)
+                                 : p.path == 6 ? adv_stream_ds_smem(p)
                                                : p.smem_bytes(p.W, p.R));
     info->npts = p.npts;
     info->autotuned = p.autotuned ? 1 : 0;
@@ -729,13 +771,14 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                                    int32_t path) try {
     BKMA_CHECK_ARG(plan, "null argument");
     AdvPlanImpl &p = plan->impl;
-    BKMA_CHECK_ARG(W >= 1 && W <= 1024 && R >= (path == 2 ? 0 : 1) && R <= 1024,
+    BKMA_CHECK_ARG(W >= 1 && W <= 1024 && R >= (path == 2 || path == 6 ? 0 : 1) && R <= 1024,
                    "W must be in [1,1024], R in [1,1024] (path 2: row-segment mode 0..8)");
     BKMA_CHECK_ARG(threads == 128 || threads == 256 || threads == 512, "threads must be 128, 256 or 512");
-    BKMA_CHECK_ARG(path >= 0 && path <= 5, "path must be 0, 1, 2, 3, 4 or 5");
+    BKMA_CHECK_ARG(path >= 0 && path <= 6, "path must be 0 to 6");
     BKMA_CHECK_ARG(path != 2 || p.stream_ok, "streamed form not available for this plan");
     BKMA_CHECK_ARG(path >= 2 || R == 1 || W >= p.desc.n2, "R > 1 needs whole-row tiles (W >= n2)");
-    BKMA_CHECK_ARG(path != 2 || R <= 8, "path 2: R is the row-segment mode, 0 (auto) to 8");
+    BKMA_CHECK_ARG((path != 2 && path != 6) || R <= 8,
+                   "paths 2 and 6: R is the row-segment mode, 0 (auto) to 8");
     if (path == 1) {
         const void *probe = reinterpret_cast<const void *>(uintptr_t(256));
         BKMA_CHECK_ARG(R == 1 && adv_tma_eligible(p, probe, W), "TMA staging not available for this tile");
@@ -752,6 +795,10 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                        "path 4 needs an FP64 plan of degree 3 or 5 with an even n2 >= W, n1 >= 16, "
                        "lines that fit shared memory, W = 4 (128 threads) or 8 (256 threads) "
                        "and R = 1");
+    } else if (path == 6) {
+        BKMA_CHECK_ARG(adv_stream_ds_shape_ok(p) && adv_stream_ds_smem(p) <= kMaxSmem,
+                       "path 6 needs an FP64 plan of degree 3 or 5 with an even n2, n1 >= 64 and "
+                       "every line's per-step shift within the streamed window");
     } else if (path == 5) {
         BKMA_CHECK_ARG(adv_ds_rows_shape_ok(p) && W == 1 && adv_ds_rows_smem(p, R) <= kMaxSmem,
                        "path 5 needs an FP64 plan of degree 3 or 5 with n2 = 1, n1 % 4 == 0, "

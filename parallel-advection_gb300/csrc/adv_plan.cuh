@@ -34,9 +34,16 @@ struct AdvPlanImpl {
     int32_t *d_exc_lines = nullptr;  // [n_exc] the exception lines, ascending
     // every non-exception line can stream (FP32 tables, see stream_line_ok)
     bool stream_ok = false;
+    // FP64 plans: every non-exception line can stream in FP32-pair arithmetic
+    // (adv_stream_ds.cu: d > -2 npts), with seams of ds_sa rows above and
+    // ds_sb rows below a segment
+    bool ds_stream_ok = false;
+    int ds_sa = 0, ds_sb = 0;
     // launch shape: path 0 = cp.async staging (any shape), 1 = TMA staging,
     // 2 = streamed columns (+ staged exception lines), 3 = contiguous lines
-    // (n2 = 1, R lines per CTA), 4 = FP64 in FP32-pair arithmetic (TMA tiles)
+    // (n2 = 1, R lines per CTA), 4 = FP64 in FP32-pair arithmetic (TMA tiles),
+    // 5 = the same on contiguous lines, 6 = the same streamed (+ staged
+    // exception lines)
     int W = 16, R = 1, threads = 256, path = 0;
     bool autotuned = false;
     int fuse = 1;  // time steps per launch (adv_fused.cu when > 1)
@@ -168,6 +175,15 @@ bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst
 size_t adv_ds_rows_smem(const AdvPlanImpl &p, int R);
 int adv_ds_rows_default_r(const AdvPlanImpl &p);
 cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int R, cudaStream_t st);
+// The same arithmetic streamed down column pairs (adv_stream_ds.cu, path 6;
+// FP64, degree 3 or 5, even n2, ds_stream_ok); segs_mode as the FP32
+// streamed form's row-segment mode; exception lines are left to the staged pass.
+bool adv_stream_ds_shape_ok(const AdvPlanImpl &p);
+bool adv_stream_ds_eligible(const AdvPlanImpl &p, const void *src, const void *dst);
+size_t adv_stream_ds_smem(const AdvPlanImpl &p);
+int adv_stream_ds_segs(const AdvPlanImpl &p, int mode);
+cudaError_t adv_stream_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int segs_mode,
+                                 cudaStream_t st);
 
 bool adv_tma_eligible(const AdvPlanImpl &p, const void *src, int W);
 size_t adv_tma_smem(const AdvPlanImpl &p, int W);

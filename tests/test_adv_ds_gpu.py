@@ -212,7 +212,7 @@ def test_ds_autotune_keeps_the_pair_kernel(bkma, cuda):
     f0 = torch.tensor(_init(p, 7), device=cuda)
     scratch = f0.clone()
     info = ds.autotune(scratch)
-    assert info["path"] == 4
+    assert info["path"] in (4, 6)  # the staged or streamed column pairs: the same bits
     a, b = f0.clone(), f0.clone()
     ds.step(a, nsteps=2)
     fresh, _ = _plans(bkma, p)
