@@ -139,9 +139,11 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * degree 3 or 5, even n2 >= W, n1 >= 16; W = 4 with 128 threads or W = 8 with
  * 256, R = 1; a field off the 16-byte grid runs the FP64 staged kernel on the
  * same tiles), or path 5: FP64 contiguous lines in FP32-pair arithmetic (FP64,
- * degree 3 or 5, n2 = 1, n1 % 4 == 0, n1 >= 16; W = 1, R whole lines per CTA,
- * `threads` ignored: 256; a field off the 16-byte grid runs the FP64 staged
- * kernel on whole rows), or path 6: FP64 column pairs streamed in FP32-pair
+ * degree 3 or 5, n2 = 1, n1 % 4 == 0, n1 >= 16; R whole lines per CTA; W = 1:
+ * 4 cells per thread, W = 2: runs along two line sections per thread, for
+ * n1 >= 512 and R = 1 or an even R <= 16, the same bits; `threads` ignored:
+ * 256; a field off the 16-byte grid runs the FP64 staged kernel on whole
+ * rows), or path 6: FP64 column pairs streamed in FP32-pair
  * arithmetic (FP64, degree 3 or 5, even n2, n1 >= 64, every line's per-step
  * shift d within -2 npts < d <= 24 - npts + 1; R the row-segment mode as on
  * path 2, `threads` ignored: 256; the same bits as path 4; exception lines

@@ -231,12 +231,16 @@ void default_tile(AdvPlanImpl &p) {
         p.R = 0;                              // row-segment mode: from the size
         p.threads = 256;
     }
-    if (adv_ds_rows_shape_ok(p) && adv_ds_rows_smem(p, adv_ds_rows_default_r(p)) <= kMaxSmem) {
+    if (adv_ds_rows_shape_ok(p)) {
         // FP64 contiguous lines (n2 = 1) in the same FP32-pair arithmetic
-        p.path = 5;
-        p.W = 1;
-        p.R = adv_ds_rows_default_r(p);
-        p.threads = 256;  // the kernel's fixed CTA
+        int W = 1, R = 1;
+        adv_ds_rows_default(p, &W, &R);
+        if (adv_ds_rows_smem(p, R) <= kMaxSmem) {
+            p.path = 5;
+            p.W = W;  // 1: 4 cells per thread, 2: runs along two sections
+            p.R = R;
+            p.threads = 256;  // the kernels' fixed CTA
+        }
     }
 }
 
@@ -396,7 +400,7 @@ cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R
     if (path == 3 || path == 5) {
         if (path == 3 && adv_rows_eligible(p, src, dst, R)) return adv_rows_launch(p, src, dst, R, st);
         if (path == 5 && adv_ds_rows_eligible(p, src, dst, R))
-            return adv_ds_rows_launch(p, src, dst, R, st);
+            return adv_ds_rows_launch(p, src, dst, W, R, st);
         // unaligned field: the generic staged kernel on whole rows
         W = 1;
         while (R > 1 && p.smem_bytes(W, R) > kMaxSmem) R /= 2;
@@ -566,7 +570,10 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     } else if (p.path == 5) {
         // other line counts per CTA of the same kernel
         for (int R = 1; R <= 1024 && R <= p.lines; R *= 2)
-            if (R != p.R && adv_ds_rows_eligible(p, field, field, R)) cands.push_back({1, R, 256, 5});
+            for (int W : {1, 2})
+                if ((R != p.R || W != p.W) && adv_ds_rows_eligible(p, field, field, R) &&
+                    (W == 1 || adv_ds_runs_ok(p, R)))
+                    cands.push_back({W, R, 256, 5});
     } else if (n2 >= 8) {
         for (int W : {8, 16, 32, 64})
             if (W <= n2 || W == 8)
@@ -727,7 +734,8 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
     const AdvPlanImpl &p = plan->impl;
     info->lines = p.lines;
     info->exception_lines = p.n_exc;
-    info->tile_cols = (int32_t)std::min<int64_t>(p.W, p.desc.n2);
+    // path 5: the contiguous-line kernel form (1: 4 cells per thread, 2: runs)
+    info->tile_cols = (int32_t)(p.path == 5 ? p.W : std::min<int64_t>(p.W, p.desc.n2));
     info->tile_slabs = p.R;
     info->threads = p.threads;
     info->smem_bytes = (int32_t)(p.path == 1   ? adv_tma_smem(p, p.W)
@@ -800,9 +808,11 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                        "path 6 needs an FP64 plan of degree 3 or 5 with an even n2, n1 >= 64 and "
                        "every line's per-step shift within the streamed window");
     } else if (path == 5) {
-        BKMA_CHECK_ARG(adv_ds_rows_shape_ok(p) && W == 1 && adv_ds_rows_smem(p, R) <= kMaxSmem,
+        BKMA_CHECK_ARG(adv_ds_rows_shape_ok(p) && (W == 1 || (W == 2 && adv_ds_runs_ok(p, R))) &&
+                           adv_ds_rows_smem(p, R) <= kMaxSmem,
                        "path 5 needs an FP64 plan of degree 3 or 5 with n2 = 1, n1 % 4 == 0, "
-                       "n1 >= 16, W = 1 and R lines that fit shared memory");
+                       "n1 >= 16, R lines that fit shared memory and W = 1 (4 cells per thread) "
+                       "or W = 2 (runs along two sections: n1 >= 512, R = 1 or an even R <= 16)");
     }
     p.W = W;
     p.R = R;

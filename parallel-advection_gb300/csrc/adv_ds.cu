@@ -35,6 +35,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "adv.cuh"
 #include "adv_device.cuh"
@@ -292,32 +293,37 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows(AdvDsRowsArgs a) {
                 ds_split(f[j], h[j], lo[j]);
                 ok = ok && ds_splittable(f[j]);
             }
-            if (ok) {
-                float2 A[NT], B[NT];
+            float2 A[NT], B[NT];
 #pragma unroll
-                for (int k = 0; k < NT; ++k) {
-                    const float2 ab = a.w2[line * NT + k];
-                    A[k] = make_float2(ab.x, ab.x);
-                    B[k] = make_float2(ab.y, ab.y);
-                }
+            for (int k = 0; k < NT; ++k) {
+                const float2 ab = a.w2[line * NT + k];
+                A[k] = make_float2(ab.x, ab.x);
+                B[k] = make_float2(ab.y, ab.y);
+            }
 #pragma unroll
-                for (int pr = 0; pr < 2; ++pr) {
-                    float4 T[NT];
+            for (int pr = 0; pr < 2; ++pr) {
+                float4 T[NT];
 #pragma unroll
-                    for (int k = 0; k < NT; ++k)
-                        T[k] = make_float4(h[2 * pr + k], h[2 * pr + k + 1], lo[2 * pr + k],
-                                           lo[2 * pr + k + 1]);
-                    const double2 r = ds_stencil<NT>(T, 0, A, B);
-                    o[2 * pr] = r.x;
-                    o[2 * pr + 1] = r.y;
-                }
-            } else {
+                for (int k = 0; k < NT; ++k)
+                    T[k] = make_float4(h[2 * pr + k], h[2 * pr + k + 1], lo[2 * pr + k],
+                                       lo[2 * pr + k + 1]);
+                const double2 r = ds_stencil<NT>(T, 0, A, B);
+                o[2 * pr] = r.x;
+                o[2 * pr + 1] = r.y;
+            }
+            if (!ok) {
+                // a cell whose own window holds a tap the pair cannot carry:
                 // FP64 direct form, the staged kernel's arithmetic
                 double w64[NT];
 #pragma unroll
                 for (int k = 0; k < NT; ++k) w64[k] = a.w[line * NT + k];
 #pragma unroll
-                for (int m = 0; m < 4; ++m) o[m] = stencil_cell<double, NT>(f + m, 1, w64);
+                for (int m = 0; m < 4; ++m) {
+                    bool own = true;
+#pragma unroll
+                    for (int k = 0; k < NT; ++k) own = own && ds_splittable(f[m + k]);
+                    if (!own) o[m] = stencil_cell<double, NT>(f + m, 1, w64);
+                }
             }
         } else {
             // per-cell stencils of an exception line, FP64 arithmetic
@@ -339,6 +345,191 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows(AdvDsRowsArgs a) {
         }
         *reinterpret_cast<double2 *>(G + i) = make_double2(o[0], o[1]);
         *reinterpret_cast<double2 *>(G + i + 2) = make_double2(o[2], o[3]);
+    }
+}
+
+// Long contiguous lines (n1 >= 512): each thread walks a run of RL
+// consecutive cells (RL odd, so that the 8-byte shared-memory loads of the 32
+// runs of a warp fall in distinct banks) of two line sections at once - two
+// lines, or the two halves of one line when a CTA holds a single line - as
+// the two lanes of the packed pair stencil, each lane with its own line
+// weights, splitting every tap once into a register ring (the column-pair
+// kernel's scheme). Windows the pair cannot carry and exception lines run the
+// staged kernel's FP64 arithmetic from the staged lines.
+constexpr int kDsRunsThreads = 256;
+
+template <int NT>
+__global__ void __launch_bounds__(kDsRunsThreads, 3) adv_ds_runs(AdvDsRowsArgs a, int rl) {
+    extern __shared__ __align__(16) double Sd[];
+    __shared__ __align__(8) uint64_t bar;
+    const int n1 = (int)a.n1;
+    const int64_t line0 = (int64_t)blockIdx.x * a.R;
+    const int nl = (int)min((int64_t)a.R, a.lines - line0);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(&bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)nl * (uint32_t)n1 * 8u;
+        asm volatile(
+            "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
+                smem_u32addr(&bar)),
+            "r"(bytes)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                "r"(smem_u32addr(Sd)),
+            "l"(a.src + line0 * a.n1), "r"(bytes), "r"(smem_u32addr(&bar))
+            : "memory");
+    }
+    if (!__syncthreads_and(staging_wait(&bar, a.spin_limit))) {
+        if (threadIdx.x == 0) {
+            atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
+            staging_wait(&bar, kWaitPolls);  // let the copy land before the CTA leaves
+        }
+        return;
+    }
+    // sections: pairs of lines (an odd last line pairs with itself and stores
+    // once), or the two halves of the CTA's single line
+    const bool halves = a.R == 1;
+    const int runs_pp = halves ? kDsRunsThreads : kDsRunsThreads / (a.R / 2);
+    const int p = (int)threadIdx.x / runs_pp, j = (int)threadIdx.x % runs_pp;
+    const int npairs = halves ? 1 : (nl + 1) / 2;
+    const int seclen = halves ? n1 / 2 : n1;
+    const int c0 = j * rl;
+    const int cnt = min(rl, seclen - c0);
+    if (p >= npairs || cnt <= 0) return;
+    int lx = halves ? 0 : 2 * p;
+    int ly = halves ? 0 : min(2 * p + 1, nl - 1);
+    bool store_y = halves || ly != lx;
+    int ox = 0, oy = halves ? n1 / 2 : 0;
+    int64_t gx = line0 + lx, gy = line0 + ly;
+    const double *Sx = Sd + (size_t)lx * n1, *Sy = Sd + (size_t)ly * n1;
+    double *Gx = a.dst + gx * a.n1 + ox + c0, *Gy = a.dst + gy * a.n1 + oy + c0;
+    const int ex = a.exc_index ? a.exc_index[gx] : -1;
+    const int ey = a.exc_index ? a.exc_index[gy] : -1;
+    // an exception line's section: per-cell stencils in FP64 arithmetic (the
+    // staged kernel's); its partner, if it is not one, keeps the pair
+    // arithmetic (with both lanes on it), so that no cell's bits depend on
+    // which lines share a CTA
+    for (int s2 = 0; s2 < (store_y ? 2 : 1); ++s2) {
+        const int e = s2 ? ey : ex;
+        if (e < 0) continue;
+        const double *Sl = s2 ? Sy : Sx;
+        double *G = s2 ? Gy : Gx;
+        const int o = (s2 ? oy : ox) + c0;
+        for (int i = 0; i < cnt; ++i) {
+            const AdvExcCell<double> &ec = a.exc[(int64_t)e * n1 + o + i];
+            int q = o + i + ec.base;
+            if (q >= n1) q -= n1;
+            double f[NT], we[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                f[k] = Sl[q];
+                we[k] = ec.w[k];
+                q = q + 1 == n1 ? 0 : q + 1;
+            }
+            G[i] = stencil_cell<double, NT>(f, 1, we);
+        }
+    }
+    if (ex >= 0 && (ey >= 0 || !store_y)) return;
+    if (ex >= 0 || ey >= 0) {
+        // the one normal section on both lanes
+        const bool xn = ex < 0;
+        lx = xn ? lx : ly;
+        ox = xn ? ox : oy;
+        gx = xn ? gx : gy;
+        Sx = xn ? Sx : Sy;
+        Gx = xn ? Gx : Gy;
+        ly = lx;
+        oy = ox;
+        gy = gx;
+        Sy = Sx;
+        Gy = Gx;
+        store_y = false;
+    }
+    float2 A[NT], B[NT];
+    double wx[NT], wy[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        const float2 abx = a.w2[gx * NT + k], aby = a.w2[gy * NT + k];
+        A[k] = make_float2(abx.x, aby.x);
+        B[k] = make_float2(abx.y, aby.y);
+    }
+    // tap 0 of the first cell of each section, and the ring of split taps
+    int qx = ox + c0 + a.base[gx], qy = oy + c0 + a.base[gy];
+    if (qx >= n1) qx -= n1;
+    if (qy >= n1) qy -= n1;
+    const int qx0 = qx, qy0 = qy;
+    float4 T[NT];
+    uint32_t bad = 0;
+#pragma unroll
+    for (int k = 0; k < NT - 1; ++k) {
+        bad = (bad << 1) | (ds_split2(make_double2(Sx[qx], Sy[qy]), T[k]) ? 0u : 1u);
+        qx = qx + 1 == n1 ? 0 : qx + 1;
+        qy = qy + 1 == n1 ? 0 : qy + 1;
+    }
+    bool any_bad = false;
+    int i = 0;
+    auto row = [&](auto u_c) {
+        constexpr int u = decltype(u_c)::value;
+        bad = ((bad << 1) | (ds_split2(make_double2(Sx[qx], Sy[qy]), T[(u + NT - 1) % NT]) ? 0u : 1u)) &
+              ((1u << NT) - 1u);
+        qx = qx + 1 == n1 ? 0 : qx + 1;
+        qy = qy + 1 == n1 ? 0 : qy + 1;
+        const double2 r = ds_stencil<NT>(T, u, A, B);
+        any_bad = any_bad || bad != 0u;
+        Gx[i] = r.x;
+        if (store_y) Gy[i] = r.y;
+        ++i;
+    };
+    for (; i + NT <= cnt;) {
+        row(std::integral_constant<int, 0>{});
+        row(std::integral_constant<int, 1>{});
+        row(std::integral_constant<int, 2>{});
+        row(std::integral_constant<int, 3>{});
+        if constexpr (NT > 4) {
+            row(std::integral_constant<int, 4 % NT>{});
+            row(std::integral_constant<int, 5 % NT>{});
+        }
+    }
+    if (i < cnt) row(std::integral_constant<int, 0>{});
+    if (i < cnt) row(std::integral_constant<int, 1>{});
+    if (i < cnt) row(std::integral_constant<int, 2>{});
+    if constexpr (NT > 4) {
+        if (i < cnt) row(std::integral_constant<int, 3>{});
+        if (i < cnt) row(std::integral_constant<int, 4 % NT>{});
+    }
+    if (any_bad) {
+        // windows holding a tap the pair cannot carry: FP64 arithmetic (the
+        // staged kernel's) for both sections' cells of those windows
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            wx[k] = a.w[gx * NT + k];
+            wy[k] = a.w[gy * NT + k];
+        }
+        int px = qx0, py = qy0;
+        for (int c = 0; c < cnt; ++c) {
+            double fx[NT], fy[NT];
+            bool okx = true, oky = true;
+            int tx = px, ty = py;
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                fx[k] = Sx[tx];
+                fy[k] = Sy[ty];
+                okx = okx && ds_splittable(fx[k]);
+                oky = oky && ds_splittable(fy[k]);
+                tx = tx + 1 == n1 ? 0 : tx + 1;
+                ty = ty + 1 == n1 ? 0 : ty + 1;
+            }
+            // each lane's cell by its own window
+            if (!okx) Gx[c] = stencil_cell<double, NT>(fx, 1, wx);
+            if (!oky && store_y) Gy[c] = stencil_cell<double, NT>(fy, 1, wy);
+            px = px + 1 == n1 ? 0 : px + 1;
+            py = py + 1 == n1 ? 0 : py + 1;
+        }
     }
 }
 
@@ -409,13 +600,33 @@ bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst
            adv_ds_rows_smem(p, R) <= (size_t)227 * 1024 - 16;  // + the static barrier
 }
 
-int adv_ds_rows_default_r(const AdvPlanImpl &p) {
-    // about 4096 cells (32 KB of shared memory) per CTA, whole lines
-    const int64_t r = std::max<int64_t>(1, 4096 / p.desc.n1);
-    return (int)std::min<int64_t>(r, p.lines);
+bool adv_ds_runs_ok(const AdvPlanImpl &p, int R) {
+    return adv_ds_rows_shape_ok(p) && p.desc.n1 >= 512 && (R == 1 || (R % 2 == 0 && R <= 16));
 }
 
-cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int R, cudaStream_t st) {
+void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
+    // long lines: the run-based kernel with about 8192 cells (64 KB) per CTA
+    // (an even number of lines, or one line from 8192 cells on), when that
+    // leaves at least two CTAs per SM; otherwise the 4-cell kernel with
+    // about 4096 cells (32 KB) per CTA (512 x 1024 x 1: 55.5 GCells/s against
+    // 44.5 for 64 CTAs of 8 lines)
+    const int64_t n1 = p.desc.n1;
+    if (n1 >= 512) {
+        int64_t r = n1 >= 8192 ? 1 : std::max<int64_t>(2, (8192 / n1) & ~int64_t(1));
+        r = std::min<int64_t>(r, p.lines);
+        if (r > 1 && r % 2) --r;
+        if ((p.lines + r - 1) / r >= 2 * 152 && adv_ds_runs_ok(p, (int)r)) {
+            *W = 2;
+            *R = (int)r;
+            return;
+        }
+    }
+    *W = 1;
+    *R = (int)std::min<int64_t>(std::max<int64_t>(1, 4096 / n1), p.lines);
+}
+
+cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W, int R,
+                               cudaStream_t st) {
     AdvDsRowsArgs a;
     a.src = (const double *)src;
     a.dst = (double *)dst;
@@ -430,6 +641,18 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int R
     a.status = p.d_status;
     a.spin_limit = p.wait_polls;
     const size_t smem = adv_ds_rows_smem(p, R);
+    if (W == 2 && adv_ds_runs_ok(p, R)) {
+        // long lines: runs of an odd length along two sections per thread
+        const int runs_pp = R == 1 ? kDsRunsThreads : kDsRunsThreads / (R / 2);
+        const int64_t seclen = R == 1 ? p.desc.n1 / 2 : p.desc.n1;
+        const int rl = (int)((seclen + runs_pp - 1) / runs_pp) | 1;
+        auto kern = p.npts == 6 ? adv_ds_runs<6> : adv_ds_runs<4>;
+        cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid_x((p.lines + R - 1) / R), kDsRunsThreads, smem, st>>>(a, rl);
+        return cudaGetLastError();
+    }
     auto kern = p.npts == 6 ? adv_ds_rows<6> : adv_ds_rows<4>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

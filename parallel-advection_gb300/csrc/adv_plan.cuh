@@ -169,12 +169,16 @@ size_t adv_ds_smem(const AdvPlanImpl &p, int W);
 int adv_ds_threads(int W);
 cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cudaStream_t st);
 // The same arithmetic on contiguous lines (FP64, n2 = 1, n1 % 4 == 0, n1 >=
-// 16, degree 3 or 5): R whole lines per CTA, 4 cells per thread (path 5).
+// 16, degree 3 or 5; path 5): R whole lines per CTA; W = 1: 4 cells per
+// thread, W = 2: runs along two line sections per thread (n1 >= 512, R = 1 or
+// an even R <= 16: adv_ds_runs_ok). Both give the same bits.
 bool adv_ds_rows_shape_ok(const AdvPlanImpl &p);
 bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R);
+bool adv_ds_runs_ok(const AdvPlanImpl &p, int R);
 size_t adv_ds_rows_smem(const AdvPlanImpl &p, int R);
-int adv_ds_rows_default_r(const AdvPlanImpl &p);
-cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int R, cudaStream_t st);
+void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R);
+cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W, int R,
+                               cudaStream_t st);
 // The same arithmetic streamed down column pairs (adv_stream_ds.cu, path 6;
 // FP64, degree 3 or 5, even n2, ds_stream_ok); segs_mode as the FP32
 // streamed form's row-segment mode; exception lines are left to the staged pass.

@@ -407,3 +407,84 @@ def test_ds_short_lines_stay_on_the_staged_kernel(bkma, cuda):
                               maxVx=p.maxVx)
     assert plan.info()["path"] == 0, plan.info()
     assert plan.set_tile(4, 1, 128, 4)["path"] == 4
+
+
+@pytest.mark.parametrize("R", [1, 2, 8, 16])
+def test_ds_runs_bit_identical_to_quads(bkma, cuda, R):
+    """The run-based kernel (W = 2: pairs of lines, or the two halves of one
+    line per CTA; an odd last line pairs with itself) gives the 4-cell
+    kernel's bits (W = 1)."""
+    import torch
+    p = AdvParams(21, 1024, 1, 0.0013, 0.0, 1.0, -2.0, 2.0)
+    f0 = _init(p, 19)
+    quad, _ = _rows_plans(bkma, p)
+    quad.set_tile(1, 3, 256, 5)
+    runs, _ = _rows_plans(bkma, p)
+    assert runs.set_tile(2, R, 256, 5)["tile_cols"] == 2
+    a, b = torch.tensor(f0, device=cuda), torch.tensor(f0, device=cuda)
+    quad.step(a, nsteps=3)
+    runs.step(b, nsteps=3)
+    runs.status()
+    assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("value", [1e200, float("inf")])
+def test_ds_runs_unsplittable_value_runs_fp64(bkma, cuda, value):
+    import torch
+    p = AdvParams(4, 1024, 1, 0.003, 0.0, 1.0, -1.0, 1.0)
+    ds, st = _rows_plans(bkma, p)
+    ds.set_tile(2, 4, 256, 5)
+    f0 = _init(p, 20)
+    i0, r_bad = 2, 700
+    f0[i0, r_bad, 0] = value
+    a, b = torch.tensor(f0, device=cuda), torch.tensor(f0, device=cuda)
+    ds.step(a)
+    st.step(b)
+    ds.status()
+    offs, _ = ds.line_table()
+    rows = [r for r in range(p.n1) if (r_bad - (r + int(offs[i0]))) % p.n1 < 6]
+    hit = torch.zeros_like(a, dtype=torch.bool)
+    hit[i0, rows, 0] = True
+    assert torch.allclose(a[hit], b[hit], rtol=0, atol=0, equal_nan=True)
+    other = ~hit & torch.isfinite(b)
+    assert (a - b)[other].abs().max().item() <= TOL * b[other].abs().max().item()
+
+
+def test_ds_runs_exception_lines(bkma, cuda, oracle):
+    """Pairs of lines where one or both are exception lines: the exception
+    lines get the staged kernel's bits, their partners the pair arithmetic,
+    the same bits as on the 4-cell kernel."""
+    import torch
+    p = AdvParams(6, 1000, 1, 0.001, 0.0, 1.0, -2.0, 3.0)
+    vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
+    runs, st = _rows_plans(bkma, p, velocity=vel)
+    runs.set_tile(2, 2, 256, 5)
+    quad, _ = _rows_plans(bkma, p, velocity=vel)
+    quad.set_tile(1, 3, 256, 5)
+    f0 = _init(p, 29)
+    a, b, c = (torch.tensor(f0, device=cuda) for _ in range(3))
+    runs.step(a, nsteps=2)
+    quad.step(b, nsteps=2)
+    st.step(c, nsteps=2)
+    runs.status()
+    assert torch.equal(a, b)
+    exc = [i0 for i0 in range(p.n0)
+           if len({(oracle.departure(p, i1, vel[i0])[0] - i1) % p.n1 for i1 in range(p.n1)}) > 1]
+    assert exc and len(exc) < p.n0
+    for i0 in exc:
+        assert torch.equal(a[i0], c[i0]), i0
+
+
+def test_ds_runs_timeout_reported(bkma, cuda):
+    import torch
+    p = AdvParams(*ROWS_CASES[0])
+    ds, _ = _rows_plans(bkma, p)
+    ds.set_tile(2, 8, 256, 5)
+    f0 = torch.tensor(_init(p, 30), device=cuda)
+    a = f0.clone()
+    ds.set_wait_limit(0)
+    ds.step(a)
+    with pytest.raises(bkma.BkmaError) as e:
+        ds.status()
+    assert e.value.status == 4
+    assert torch.equal(a, f0)
