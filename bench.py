@@ -42,8 +42,9 @@ PROFILE_JSON = {1: os.path.join(ROOT, "profiles", "adv_tma_f32_2048x1024x512.jso
 
 
 def velocities(n0: int):
+    """v_i = -1 + 2 i / (n0 - 1); a single line (profiling shapes) moves at -1."""
     import numpy as np
-    return -1.0 + 2.0 * np.arange(n0, dtype=np.float64) / (n0 - 1)
+    return -1.0 + 2.0 * np.arange(n0, dtype=np.float64) / max(n0 - 1, 1)
 
 
 def peaks():

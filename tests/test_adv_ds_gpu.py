@@ -410,16 +410,18 @@ def test_ds_short_lines_stay_on_the_staged_kernel(bkma, cuda):
 
 
 @pytest.mark.parametrize("R", [1, 2, 8, 16])
-def test_ds_runs_bit_identical_to_quads(bkma, cuda, R):
+@pytest.mark.parametrize("degree", [5, 3])
+def test_ds_runs_bit_identical_to_quads(bkma, cuda, R, degree):
     """The run-based kernel (W = 2: pairs of lines, or the two halves of one
     line per CTA; an odd last line pairs with itself) gives the 4-cell
     kernel's bits (W = 1)."""
     import torch
     p = AdvParams(21, 1024, 1, 0.0013, 0.0, 1.0, -2.0, 2.0)
     f0 = _init(p, 19)
-    quad, _ = _rows_plans(bkma, p)
+    kw = dict(degree=degree, weights="reference" if degree == 5 else "lagrange")
+    quad, _ = _rows_plans(bkma, p, **kw)
     quad.set_tile(1, 3, 256, 5)
-    runs, _ = _rows_plans(bkma, p)
+    runs, _ = _rows_plans(bkma, p, **kw)
     assert runs.set_tile(2, R, 256, 5)["tile_cols"] == 2
     a, b = torch.tensor(f0, device=cuda), torch.tensor(f0, device=cuda)
     quad.step(a, nsteps=3)
