@@ -147,6 +147,9 @@ cudaError_t adv_rows_launch(const AdvPlanImpl &p, const void *src, void *dst, in
 size_t adv_stream_smem();  // static shared memory per CTA of the streamed kernel
 // All fields of `d_fields` (device array, ascending cta0) have npts taps;
 // nctas = the sum of their CTA counts.
+// Fields of 4 and of 6 taps mixed, in one launch.
+cudaError_t adv_stream_launch_fields_46(const StreamField *d_fields, int nfields, int64_t nctas,
+                                        cudaStream_t st);
 cudaError_t adv_stream_launch_fields(int npts, const StreamField *d_fields, int nfields,
                                      int64_t nctas, cudaStream_t st);
 

@@ -221,6 +221,28 @@ __global__ void __launch_bounds__(kWarps * 32) adv_stream_f32(StreamField one,
     stream_group<NT>(F, group, warp % F.segs, seams);
 }
 
+// Fields of 4 and of 6 taps in one launch (batches): the CTAs of a field all
+// take its tap count, so the switch is uniform per CTA, and the batch has one
+// last wave instead of one per tap count.
+__global__ void __launch_bounds__(kWarps * 32) adv_stream_f32_46(const StreamField *__restrict__ many,
+                                                                  int nfields) {
+    __shared__ float seams[kWarps][kSeamRows * kPitch];
+    int lo = 0, hi = nfields - 1;  // last field with cta0 <= blockIdx.x
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (many[mid].cta0 <= (int64_t)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const StreamField F = many[lo];
+    const int warp = threadIdx.x >> 5;
+    const int per_cta = kWarps / F.segs;
+    const int64_t group = ((int64_t)blockIdx.x - F.cta0) * per_cta + warp / F.segs;
+    if (F.npts == 4)
+        stream_group<4>(F, group, warp % F.segs, seams);
+    else
+        stream_group<6>(F, group, warp % F.segs, seams);
+}
+
 template <int NT>
 cudaError_t launch_stream(StreamField one, const StreamField *many, int nfields, int64_t ctas,
                           cudaStream_t st) {
@@ -283,6 +305,13 @@ cudaError_t adv_stream_launch(AdvPlanImpl &p, const void *src, void *dst, int se
     const int s = adv_stream_segs(p.desc.n1, adv_stream_groups(p), segs);
     return launch_stream_npts(p.npts, adv_stream_field(p, src, dst, s), nullptr, 1,
                               adv_stream_ctas(p, s), st);
+}
+
+cudaError_t adv_stream_launch_fields_46(const StreamField *d_fields, int nfields, int64_t nctas,
+                                        cudaStream_t st) {
+    if (nctas == 0) return cudaSuccess;
+    adv_stream_f32_46<<<grid_x(nctas), kWarps * 32, 0, st>>>(d_fields, nfields);
+    return cudaGetLastError();
 }
 
 cudaError_t adv_stream_launch_fields(int npts, const StreamField *d_fields, int nfields,

@@ -76,7 +76,8 @@ struct BatchImpl {
     void *d_fields = nullptr;  // staged work list entries
     int nstaged = 0;
     unsigned long long *d_counter = nullptr;
-    // streamed fields, one group per tap count (4, 6, 10)
+    // streamed fields: group 0 the 4- and 6-tap fields (one launch), group 2
+    // the 10-tap ones (group 1 unused)
     StreamField *d_stream[3] = {nullptr, nullptr, nullptr};
     int nstream[3] = {0, 0, 0};
     int64_t items[3] = {0, 0, 0};  // CTAs of each streamed launch
@@ -114,7 +115,9 @@ struct BatchImpl {
     }
 };
 
-int stream_group(int npts) { return npts == 4 ? 0 : npts == 6 ? 1 : 2; }
+// Streamed launch of a field: 4 and 6 taps share one (adv_stream_f32_46),
+// 10 taps have their own.
+int stream_group(int npts) { return npts == 10 ? 2 : 0; }
 
 // Streamed when every line allows it and rows have at least 8 columns: with
 // fewer, a warp's 32 lanes spread over many lines and rows stop coalescing,
@@ -268,11 +271,12 @@ bkma_status build_batch(BatchImpl &b, cudaStream_t st) {
         ++b.launches;
         ++nb;
     }
-    const int npts_of[3] = {4, 6, 10};
     for (int k = 0; k < 3; ++k) {
         if (b.items[k] == 0) continue;
-        adv_stream_launch_fields(npts_of[k], b.d_stream[k], b.nstream[k], b.items[k],
-                                 branch[nb % 3]);
+        if (k == 0)
+            adv_stream_launch_fields_46(b.d_stream[0], b.nstream[0], b.items[0], branch[nb % 3]);
+        else
+            adv_stream_launch_fields(10, b.d_stream[k], b.nstream[k], b.items[k], branch[nb % 3]);
         ++b.launches;
         ++nb;
     }
