@@ -520,16 +520,27 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
     for (int64_t l = 0; l < p.lines && p.stream_ok; ++l)
         if (p.exc_index[(size_t)l] < 0 && !stream_line_ok(p.base[(size_t)l], n1, NT))
             p.stream_ok = false;
-    if (d.dtype == BKMA_F64) {
-        // the streamed FP32-pair form loads 2 NT rows ahead of its stores
+    if (d.dtype == BKMA_F64 && d.n2 % 2 == 0) {
+        // the streamed FP32-pair form: each 64-column group (32 column pairs
+        // of the (line, i2) space) walks up its rows, loading 2 NT rows ahead
+        // of its stores (d > -2 NT on all its lines), or down (d <= NT); seams
+        // of at most 32 rows each way
+        constexpr int kWin = 32;
         p.ds_stream_ok = n1 >= kStreamMinN1;
-        p.ds_sa = p.ds_sb = 0;
-        for (int64_t l = 0; l < p.lines && p.ds_stream_ok; ++l) {
-            if (p.exc_index[(size_t)l] >= 0) continue;
-            const int dd = stream_offset(p.base[(size_t)l], n1);
-            if (!stream_line_ok(p.base[(size_t)l], n1, NT) || dd <= -2 * NT) p.ds_stream_ok = false;
-            p.ds_sa = std::max(p.ds_sa, dd + NT - 1);
-            p.ds_sb = std::max(p.ds_sb, -dd);
+        p.ds_sr = 0;
+        const int64_t cols = p.lines * d.n2, ngroups = (cols + 63) / 64;
+        for (int64_t g = 0; g < ngroups && p.ds_stream_ok; ++g) {
+            const int64_t l0 = g * 64 / d.n2, l1 = std::min(g * 64 + 63, cols - 1) / d.n2;
+            bool up = true, down = true;
+            for (int64_t l = l0; l <= l1; ++l) {
+                if (p.exc_index[(size_t)l] >= 0) continue;
+                const int dd = stream_offset(p.base[(size_t)l], n1);
+                if (dd < -kWin || dd + NT - 1 > kWin) p.ds_stream_ok = false;
+                up = up && dd > -2 * NT;
+                down = down && dd <= NT;
+                p.ds_sr = std::max(p.ds_sr, std::max(dd + NT - 1, 0) + std::max(-dd, 0));
+            }
+            if (!up && !down) p.ds_stream_ok = false;
         }
     }
     if (d.dtype == BKMA_F32) return upload_tables<float>(p);

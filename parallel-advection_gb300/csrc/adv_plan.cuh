@@ -35,10 +35,11 @@ struct AdvPlanImpl {
     // every non-exception line can stream (FP32 tables, see stream_line_ok)
     bool stream_ok = false;
     // FP64 plans: every non-exception line can stream in FP32-pair arithmetic
-    // (adv_stream_ds.cu: d > -2 npts), with seams of ds_sa rows above and
-    // ds_sb rows below a segment
+    // (adv_stream_ds.cu: |d| <= 32, and every 64-column group walks up, d >
+    // -2 npts on all its lines, or down, d <= npts), with ds_sr seam rows per
+    // column pair (max(d + npts - 1, 0) + max(-d, 0), the largest over lines)
     bool ds_stream_ok = false;
-    int ds_sa = 0, ds_sb = 0;
+    int ds_sr = 0;
     // launch shape: path 0 = cp.async staging (any shape), 1 = TMA staging,
     // 2 = streamed columns (+ staged exception lines), 3 = contiguous lines
     // (n2 = 1, R lines per CTA), 4 = FP64 in FP32-pair arithmetic (TMA tiles),

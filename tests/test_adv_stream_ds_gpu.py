@@ -3,8 +3,9 @@ through the C ABI.
 
 The streamed form computes every cell with the same operations as the staged
 column-pair kernel (path 4), so the two give the same bits wherever both
-apply; it is the default for column pairs the staged form cannot take (lines
-too tall for a shared-memory strip, rows 1 MB or more apart). Tolerances as
+apply, walking up the rows or, for lines shifted 2 npts or more rows down,
+down them; it is the default for column pairs the staged form cannot take
+(lines too tall for a shared-memory strip, rows 1 MB or more apart). Tolerances as
 in test_adv_ds_gpu.py: 2e-13 max|f| per step against the FP64 staged kernel,
 1e-11 against the oracle; windows the FP32 pair cannot carry, exception lines
 and fields off the 16-byte grid run the staged kernel's FP64 arithmetic.
@@ -181,6 +182,86 @@ def test_stream_ds_misaligned_field_runs_fp64(bkma, cuda):
     b = torch.tensor(f0, device=cuda)
     st.step(b, nsteps=2)
     assert torch.equal(d, b)
+
+
+# per-line velocities whose shifts run from -12.6 to +26.6 cells (n1 = 1024,
+# dt = 0.001): tap-0 offsets d from about +10 down to -29; each 64-column group
+# is one line (n2 = 64), and the lines with d <= -2 npts walk down their rows
+FAR_VEL = np.array([-12.3, -6.0, 0.3, 5.0, 9.0, 13.0, 20.0, 26.0])
+
+
+@pytest.mark.parametrize("degree", [5, 3])
+def test_stream_ds_large_shifts_walk_down(bkma, cuda, oracle, degree):
+    """Lines shifted 12 or more rows down stream walking down their rows: the
+    same bits as the column-pair kernel, in place as out of place."""
+    import torch
+    p = AdvParams(8, 1024, 64, 0.001, 0.0, 1.0, -1.0, 1.0)
+    weights = "reference" if degree == 5 else "lagrange"
+    kw = dict(velocity=FAR_VEL, degree=degree, weights=weights)
+    s6 = _plan(bkma, p, **kw)
+    s6.set_tile(8, 0, 256, 6)
+    s4 = _plan(bkma, p, **kw)
+    s4.set_tile(4, 1, 128, 4)
+    oop = _plan(bkma, p, inplace=False, **kw)
+    oop.set_tile(8, 0, 256, 6)
+    f0 = _init(p, 29)
+    a, b, src = (torch.tensor(f0, device=cuda) for _ in range(3))
+    s6.step(a, nsteps=3)
+    s4.step(b, nsteps=3)
+    s6.status()
+    assert torch.equal(a, b)
+    out = torch.empty_like(src)
+    oop.step(src, out=out, nsteps=3)
+    assert torch.equal(a, out)
+    want = oracle.adv_step(p, f0.copy(), 3, degree=degree, ref_weights=degree == 5,
+                           velocity=FAR_VEL)
+    assert np.abs(a.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_stream_ds_group_votes_one_direction(bkma, cuda):
+    """A 64-column group spanning 8 lines (n2 = 8) whose shifts straddle the
+    up/down limit walks down as a whole: the column-pair kernel's bits."""
+    import torch
+    p = AdvParams(16, 512, 8, 0.002, 0.0, 1.0, -1.0, 1.0)
+    vel = np.linspace(2.0, 14.0, 16)  # shifts 2.0 .. 14.3 cells
+    s6 = _plan(bkma, p, velocity=vel)
+    s6.set_tile(8, 0, 256, 6)
+    s4 = _plan(bkma, p, velocity=vel)
+    s4.set_tile(4, 1, 128, 4)
+    f0 = _init(p, 30)
+    a, b = torch.tensor(f0, device=cuda), torch.tensor(f0, device=cuda)
+    s6.step(a, nsteps=2)
+    s4.step(b, nsteps=2)
+    s6.status()
+    assert torch.equal(a, b)
+
+
+def test_stream_ds_refuses_groups_with_no_direction(bkma, cuda):
+    """Lines 12 rows down and 12 rows up in one group (n2 = 2: 32 lines per
+    group) suit neither walk: the plan keeps the staged kernels."""
+    p = AdvParams(64, 1024, 2, 0.001, 0.0, 1.0, -1.0, 1.0)
+    vel = np.where(np.arange(64) % 2 == 0, 14.0, -14.0)
+    plan = _plan(bkma, p, velocity=vel)
+    assert plan.info()["path"] != 6
+    with pytest.raises(bkma.BkmaError):
+        plan.set_tile(8, 0, 256, 6)
+
+
+def test_stream_ds_long_lines_large_shifts_default(bkma, cuda, oracle):
+    """The reference's 1024 x 16384 x 128 sweep shape shifts lines by up to 16
+    cells per step (16384 cells, dt = 0.001, v in [-1, 1]): its slabs stream,
+    the last of these four walking down (shifts -16.4, -4.9, 6.6, 16.4)."""
+    import torch
+    p = AdvParams(4, 16384, 128, 0.001, 0.0, 1.0, -1.0, 1.0)
+    vel = np.array([-1.0, -0.3, 0.4, 1.0])
+    plan = _plan(bkma, p, velocity=vel)
+    assert plan.info()["path"] == 6, plan.info()
+    f0 = _init(p, 31)
+    a = torch.tensor(f0, device=cuda)
+    plan.step(a, nsteps=2)
+    plan.status()
+    want = oracle.adv_step(p, f0.copy(), 2, velocity=vel)
+    assert np.abs(a.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
 
 
 def test_stream_ds_zero_field_stays_zero(bkma, cuda):
