@@ -54,8 +54,9 @@ typedef enum bkma_dtype { BKMA_F32 = 0, BKMA_F64 = 1, BKMA_BF16 = 2 } bkma_dtype
 /* AUTO and STAGED run the fastest kernel for the shape. For FP64 fields that
  * is, wherever the shape allows it (degree 3 or 5; column pairs of an even
  * n2 with n1 >= 128, staged in shared memory or, for strips too tall or rows
- * 1 MB or more apart, streamed; or n2 = 1 with n1 % 4 == 0; a 16-byte
- * aligned field), a kernel that
+ * 1 MB or more apart, streamed; whole slabs of lines shorter than 128 rows
+ * with an even n2; or n2 = 1 with n1 % 4 == 0; a 16-byte aligned field), a
+ * kernel that
  * keeps FP64 in HBM but sums the stencil in FP32-pair arithmetic (GB300's
  * FP64 rate would otherwise bound the step near 100 GCells/s): it agrees with
  * FP64 arithmetic to about 2e-13 max|f| per step. bkma_adv_plan_set_tile
@@ -105,7 +106,8 @@ typedef struct bkma_adv_plan_info {
     int32_t path;              /* 0: cp.async staging, 1: TMA (cp.async.bulk.tensor) staging,
                                   2: streamed columns, 3: contiguous lines (n2 = 1),
                                   4: FP64 in FP32-pair arithmetic (TMA staging),
-                                  5: FP64 contiguous lines (n2 = 1) in FP32-pair arithmetic,
+                                  5: FP64 contiguous lines (n2 = 1) or whole slabs (even n2)
+                                     in FP32-pair arithmetic,
                                   6: FP64 column pairs streamed in FP32-pair arithmetic */
     int32_t reserved;
 } bkma_adv_plan_info;
@@ -141,9 +143,10 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * same tiles), or path 5: FP64 contiguous lines in FP32-pair arithmetic (FP64,
  * degree 3 or 5, n2 = 1, n1 % 4 == 0, n1 >= 16; R whole lines per CTA; W = 1:
  * 4 cells per thread, W = 2: runs along two line sections per thread, for
- * n1 >= 512 and R = 1 or an even R <= 16, the same bits; `threads` ignored:
- * 256; a field off the 16-byte grid runs the FP64 staged kernel on whole
- * rows), or path 6: FP64 column pairs streamed in FP32-pair
+ * n1 >= 512 and R = 1 or an even R <= 16, the same bits; or with an even n2,
+ * R whole slabs per CTA and W <= 64 runs of rows per column pair, the same
+ * bits as path 4; `threads` ignored: 256; a field off the 16-byte grid runs
+ * the FP64 staged kernel on whole rows or 8-column strips), or path 6: FP64 column pairs streamed in FP32-pair
  * arithmetic (FP64, degree 3 or 5, even n2, n1 >= 64, every line's tap-0
  * offset d within -32 <= d <= 33 - npts, and in each group of 64 consecutive
  * columns of the (line, i2) space either d > -2 npts on every line, walked up

@@ -213,9 +213,11 @@ void default_tile(AdvPlanImpl &p) {
         // FP64 staged kernel near 100 GCells/s): 4-column TMA tiles, six CTAs
         // of 128 threads per SM (2048 x 1024 x 512: 333 GCells/s; 8-column
         // tiles, three CTAs of 256 threads: 289). Lines shorter than 128 rows
-        // leave runs of one or two rows that re-split most taps and stay on
-        // the staged kernel (x 128 columns, 2^27 cells, GCells/s pair / staged:
-        // n1 = 16 33 / 100, 64 97 / 100, 128 151 / 98, 256 216 / 99)
+        // leave runs of one or two rows that re-split most taps: they take
+        // whole slabs below (x 128 columns, 2^27 cells, GCells/s column pairs
+        // / slabs / staged: n1 = 16 33 / 311 / 100, 64 97 / 311 / 91; 128
+        // 151 / - / 98, 256 216 / - / 99, slabs of 128 KB and more leaving
+        // one CTA per SM)
         p.path = 4;
         p.W = 4;
         p.R = 1;
@@ -231,13 +233,15 @@ void default_tile(AdvPlanImpl &p) {
         p.R = 0;                              // row-segment mode: from the size
         p.threads = 256;
     }
-    if (adv_ds_rows_shape_ok(p)) {
-        // FP64 contiguous lines (n2 = 1) in the same FP32-pair arithmetic
+    if (adv_ds_rows_shape_ok(p) && (n2 == 1 || (p.path == 0 && p.desc.n1 < 128))) {
+        // FP64 contiguous lines (n2 = 1), or whole slabs of lines too short
+        // for the column-pair kernel, in the same FP32-pair arithmetic
         int W = 1, R = 1;
         adv_ds_rows_default(p, &W, &R);
         if (adv_ds_rows_smem(p, R) <= kMaxSmem) {
             p.path = 5;
-            p.W = W;  // 1: 4 cells per thread, 2: runs along two sections
+            p.W = W;  // lines: 1 = 4 cells per thread, 2 = runs along two
+                      // sections; slabs: runs of rows per column pair
             p.R = R;
             p.threads = 256;  // the kernels' fixed CTA
         }
@@ -401,8 +405,10 @@ cudaError_t launch_once(AdvPlanImpl &p, const void *src, void *dst, int W, int R
         if (path == 3 && adv_rows_eligible(p, src, dst, R)) return adv_rows_launch(p, src, dst, R, st);
         if (path == 5 && adv_ds_rows_eligible(p, src, dst, R))
             return adv_ds_rows_launch(p, src, dst, W, R, st);
-        // unaligned field: the generic staged kernel on whole rows
-        W = 1;
+        // unaligned field: the generic staged kernel on whole rows (n2 = 1)
+        // or on 8-column strips of single lines
+        W = (int)std::min<int64_t>(8, p.desc.n2);
+        if (W > 1) R = 1;
         while (R > 1 && p.smem_bytes(W, R) > kMaxSmem) R /= 2;
     }
     if (p.desc.impl == BKMA_ADV_PLAIN)
@@ -568,9 +574,10 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     std::vector<TuneVal> cands{{p.W, p.R, p.threads, p.path}};
     const int64_t n2 = p.desc.n2;
     const int ths[3] = {128, 256, 512};
-    if (p.path == 4 || p.path == 6) {
+    if (p.path == 4 || p.path == 6 || (p.path == 5 && n2 > 1)) {
         // the other forms of the same arithmetic per cell (same bits): tile
-        // widths of the staged column-pair kernel, row segments of the streamed one
+        // widths of the staged column-pair kernel, row segments of the
+        // streamed one, slabs per CTA of the whole-slab one
         for (int W : {4, 8})
             if ((p.path != 4 || W != p.W) && adv_ds_shape_ok(p, W) && p.desc.n1 >= 16)
                 cands.push_back({W, 1, adv_ds_threads(W), 4});
@@ -578,6 +585,13 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
             for (int segs : {0, 1, 2, 4, 8})
                 if (p.path != 6 || segs != p.R)
                     cands.push_back({(int)std::min<int64_t>(8, n2), segs, 256, 6});
+        if (p.desc.n1 < 128)
+            for (int R = 1; R <= 1024 && R <= p.lines; R *= 2)
+                for (int runs : {1, 2, 4, 8})
+                    if ((p.path != 5 || R != p.R || runs != p.W) && runs <= p.desc.n1 &&
+                        adv_ds_rows_eligible(p, field, field, R) &&
+                        (int64_t)R * (n2 / 2) * runs <= 1024)
+                        cands.push_back({runs, R, 256, 5});
     } else if (p.path == 5) {
         // other line counts per CTA of the same kernel
         for (int R = 1; R <= 1024 && R <= p.lines; R *= 2)
@@ -819,11 +833,16 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                        "path 6 needs an FP64 plan of degree 3 or 5 with an even n2, n1 >= 64 and "
                        "every line's per-step shift within the streamed window");
     } else if (path == 5) {
-        BKMA_CHECK_ARG(adv_ds_rows_shape_ok(p) && (W == 1 || (W == 2 && adv_ds_runs_ok(p, R))) &&
+        const bool slabs = p.desc.n2 > 1;
+        BKMA_CHECK_ARG(adv_ds_rows_shape_ok(p) &&
+                           (slabs ? W <= 64
+                                  : (W == 1 || (W == 2 && adv_ds_runs_ok(p, R)))) &&
                            adv_ds_rows_smem(p, R) <= kMaxSmem,
                        "path 5 needs an FP64 plan of degree 3 or 5 with n2 = 1, n1 % 4 == 0, "
                        "n1 >= 16, R lines that fit shared memory and W = 1 (4 cells per thread) "
-                       "or W = 2 (runs along two sections: n1 >= 512, R = 1 or an even R <= 16)");
+                       "or W = 2 (runs along two sections: n1 >= 512, R = 1 or an even R <= 16); "
+                       "or with an even n2, R whole slabs that fit shared memory and W <= 64 "
+                       "runs of rows per column pair");
     }
     p.W = W;
     p.R = R;

@@ -215,8 +215,9 @@ constexpr int kDsRowsThreads = 256;
 struct AdvDsRowsArgs {
     const double *src;
     double *dst;
-    int64_t n1, lines;
+    int64_t n1, n2, lines;     // n2: 1 (lines), or even (slabs: adv_ds_slabs)
     int R;                     // lines per CTA
+    int runs;                  // slabs: runs of rows per column pair (threads per pair)
     const int32_t *base;       // [lines]
     const double *w;           // [lines][NT]
     const float2 *w2;          // [lines][NT] FP32-pair weights
@@ -345,6 +346,173 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows(AdvDsRowsArgs a) {
         }
         *reinterpret_cast<double2 *>(G + i) = make_double2(o[0], o[1]);
         *reinterpret_cast<double2 *>(G + i + 2) = make_double2(o[2], o[3]);
+    }
+}
+
+// Short lines with an even n2 > 1: whole slabs. A line of the field is a
+// slab of n1 rows x n2 columns, n1 * n2 consecutive doubles, and R
+// consecutive slabs are one contiguous block: a CTA stages them with one bulk
+// copy (bounded wait), then each thread takes a run of rows of one column
+// pair (`runs` runs per pair: 1 for lines of 16 rows, more for longer lines,
+// so that a CTA has about 256 threads) with the column-pair kernel's register
+// ring (every tap split once, the same stencil per cell and the same FP64
+// redo of windows the pair cannot carry: the same bits as adv_ds_f64), the
+// periodic wrap taken by the tap pointer. That kernel spreads 64 runs over
+// the rows of each column pair, which leaves lines shorter than 128 rows runs
+// of one or two rows.
+constexpr int kDsSlabThreads = 256;
+
+template <int NT>
+__global__ void __launch_bounds__(kDsSlabThreads, 3) adv_ds_slabs(AdvDsRowsArgs a) {
+    extern __shared__ __align__(16) double Sd[];
+    __shared__ __align__(8) uint64_t bar;
+    const int n1 = (int)a.n1;
+    const int P2 = (int)(a.n2 / 2);  // column pairs per row
+    const int64_t slab = a.n1 * a.n2;
+    const int64_t line0 = (int64_t)blockIdx.x * a.R;
+    const int nl = (int)min((int64_t)a.R, a.lines - line0);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(&bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)(nl * slab) * 8u;
+        asm volatile(
+            "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
+                smem_u32addr(&bar)),
+            "r"(bytes)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                "r"(smem_u32addr(Sd)),
+            "l"(a.src + line0 * slab), "r"(bytes), "r"(smem_u32addr(&bar))
+            : "memory");
+    }
+    if (!__syncthreads_and(staging_wait(&bar, a.spin_limit))) {
+        if (threadIdx.x == 0) {
+            atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
+            staging_wait(&bar, kWaitPolls);  // let the copy land before the CTA leaves
+        }
+        return;
+    }
+    const int RP = a.runs;
+    const int RL = (n1 + RP - 1) / RP;
+    const int units = nl * RP * P2;
+    // consecutive threads: consecutive column pairs of one run
+    auto unit = [&](int t, int &l, int &g, int &r0, int &cnt) {
+        const int lj = t / P2;
+        g = t - lj * P2;
+        l = lj / RP;
+        r0 = (lj - l * RP) * RL;
+        cnt = min(n1 - r0, RL);
+    };
+    bool any_bad = false;
+    for (int t = threadIdx.x; t < units; t += kDsSlabThreads) {
+        int l, g, r0, cnt;
+        unit(t, l, g, r0, cnt);
+        if (cnt <= 0) continue;
+        const int64_t line = line0 + l;
+        // row 0 of the thread's column pair
+        const double2 *S0 = reinterpret_cast<const double2 *>(Sd + (size_t)l * slab) + g;
+        double *G = a.dst + line * slab + 2 * g;
+        const int exc = a.exc_index ? a.exc_index[line] : -1;
+        if (exc >= 0) {
+            // per-cell stencils of an exception line, FP64 arithmetic
+            const AdvExcCell<double> *cells = a.exc + (int64_t)exc * n1;
+            for (int r = r0; r < r0 + cnt; ++r) {
+                const AdvExcCell<double> &e = cells[r];
+                int q = r + e.base;
+                if (q >= n1) q -= n1;
+                double fx[NT], fy[NT], we[NT];
+#pragma unroll
+                for (int k = 0; k < NT; ++k) {
+                    const double2 x = S0[(size_t)q * P2];
+                    fx[k] = x.x;
+                    fy[k] = x.y;
+                    we[k] = e.w[k];
+                    q = q + 1 == n1 ? 0 : q + 1;
+                }
+                *reinterpret_cast<double2 *>(G + (int64_t)r * a.n2) =
+                    make_double2(stencil_cell<double, NT>(fx, 1, we), stencil_cell<double, NT>(fy, 1, we));
+            }
+            continue;
+        }
+        float2 A[NT], B[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            const float2 ab = a.w2[line * NT + k];
+            A[k] = make_float2(ab.x, ab.x);
+            B[k] = make_float2(ab.y, ab.y);
+        }
+        int q0 = a.base[line] + r0;  // row of output row r0's tap 0
+        if (q0 >= n1) q0 -= n1;
+        const double2 *P = S0 + (size_t)q0 * P2;
+        int left = n1 - q0;  // rows before the tap pointer wraps to row 0
+        float4 T[NT];
+        bool bad = false;
+        auto advance = [&]() {
+            P += P2;
+            if (--left == 0) {
+                P = S0;
+                left = n1;
+            }
+        };
+#pragma unroll
+        for (int k = 0; k < NT - 1; ++k) {
+            bad |= !ds_split2(*P, T[k]);
+            advance();
+        }
+        double *Gr = G + (int64_t)r0 * a.n2;
+        auto row = [&](int u) {
+            bad |= !ds_split2(*P, T[(u + NT - 1) % NT]);
+            advance();
+            *reinterpret_cast<double2 *>(Gr) = ds_stencil<NT>(T, u, A, B);
+            Gr += a.n2;
+        };
+        int i = 0;
+        for (; i + NT <= cnt; i += NT) {
+#pragma unroll
+            for (int u = 0; u < NT; ++u) row(u);
+        }
+#pragma unroll
+        for (int u = 0; u < NT - 1; ++u)
+            if (i + u < cnt) row(u);
+        any_bad |= bad;
+    }
+    if (!any_bad) return;
+    // a tap the split cannot carry: redo the pairs whose window holds one in
+    // FP64 (the staged kernel's arithmetic); this thread wrote them
+    for (int t = threadIdx.x; t < units; t += kDsSlabThreads) {
+        int l, g, r0, cnt;
+        unit(t, l, g, r0, cnt);
+        const int64_t line = line0 + l;
+        if (cnt <= 0 || (a.exc_index && a.exc_index[line] >= 0)) continue;
+        const double2 *S0 = reinterpret_cast<const double2 *>(Sd + (size_t)l * slab) + g;
+        double *G = a.dst + line * slab + 2 * g;
+        double w64[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) w64[k] = a.w[line * NT + k];
+        int q = a.base[line] + r0;
+        if (q >= n1) q -= n1;
+        for (int r = r0; r < r0 + cnt; ++r) {
+            int qk = q;
+            double fx[NT], fy[NT];
+            bool ok = true;
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                const double2 x = S0[(size_t)qk * P2];
+                fx[k] = x.x;
+                fy[k] = x.y;
+                ok = ok && ds_splittable(x.x) && ds_splittable(x.y);
+                qk = qk + 1 == n1 ? 0 : qk + 1;
+            }
+            q = q + 1 == n1 ? 0 : q + 1;
+            if (ok) continue;
+            *reinterpret_cast<double2 *>(G + (int64_t)r * a.n2) =
+                make_double2(stencil_cell<double, NT>(fx, 1, w64), stencil_cell<double, NT>(fy, 1, w64));
+        }
     }
 }
 
@@ -585,26 +753,43 @@ cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cud
 }
 
 size_t adv_ds_rows_smem(const AdvPlanImpl &p, int R) {
-    return (size_t)R * (size_t)p.desc.n1 * sizeof(double);
+    return (size_t)R * (size_t)p.desc.n1 * (size_t)p.desc.n2 * sizeof(double);
 }
 
 bool adv_ds_rows_shape_ok(const AdvPlanImpl &p) {
+    const int64_t n1 = p.desc.n1, n2 = p.desc.n2;
+    const bool lines = n2 == 1 && n1 % 4 == 0 && n1 >= 16;
+    const bool slabs = n2 >= 2 && n2 % 2 == 0;
     return p.desc.dtype == BKMA_F64 && p.desc.impl != BKMA_ADV_PLAIN && p.d_w2 != nullptr &&
-           p.desc.n2 == 1 && p.desc.n1 % 4 == 0 && p.desc.n1 >= 16 &&
-           (p.npts == 4 || p.npts == 6) && p.lines * p.desc.n1 < (1ll << 40);
+           (lines || slabs) && (p.npts == 4 || p.npts == 6) && p.lines * n1 * n2 < (1ll << 40);
 }
 
 bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R) {
+    // one bulk copy per CTA, within the barrier's transaction count
     return adv_ds_rows_shape_ok(p) && R >= 1 && ((uintptr_t)src % 16) == 0 &&
-           ((uintptr_t)dst % 16) == 0 && (int64_t)R * p.desc.n1 <= (1 << 20) &&
+           ((uintptr_t)dst % 16) == 0 && adv_ds_rows_smem(p, R) < (1 << 20) &&
            adv_ds_rows_smem(p, R) <= (size_t)227 * 1024 - 16;  // + the static barrier
 }
 
 bool adv_ds_runs_ok(const AdvPlanImpl &p, int R) {
-    return adv_ds_rows_shape_ok(p) && p.desc.n1 >= 512 && (R == 1 || (R % 2 == 0 && R <= 16));
+    return adv_ds_rows_shape_ok(p) && p.desc.n2 == 1 && p.desc.n1 >= 512 &&
+           (R == 1 || (R % 2 == 0 && R <= 16));
 }
 
 void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
+    if (p.desc.n2 > 1) {
+        // slabs: up to 256 column pairs and 64 KB (three CTAs per SM) per
+        // CTA, then runs of >= 16 rows per pair up to about 256 threads
+        const int64_t pairs = p.desc.n2 / 2, bytes = p.desc.n1 * p.desc.n2 * 8;
+        const int64_t r = std::min<int64_t>(
+            std::max<int64_t>(1, std::min(kDsSlabThreads / pairs, 65536 / bytes)), p.lines);
+        int runs = 1;
+        while (runs < 8 && r * pairs * runs * 2 <= kDsSlabThreads && p.desc.n1 / (runs * 2) >= 16)
+            runs *= 2;
+        *W = runs;
+        *R = (int)r;
+        return;
+    }
     // long lines: the run-based kernel with about 8192 cells (64 KB) per CTA
     // (an even number of lines, or one line from 8192 cells on), when that
     // leaves at least two CTAs per SM; otherwise the 4-cell kernel with
@@ -631,6 +816,7 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
     a.src = (const double *)src;
     a.dst = (double *)dst;
     a.n1 = p.desc.n1;
+    a.n2 = p.desc.n2;
     a.lines = p.lines;
     a.R = R;
     a.base = p.d_base;
@@ -641,6 +827,15 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
     a.status = p.d_status;
     a.spin_limit = p.wait_polls;
     const size_t smem = adv_ds_rows_smem(p, R);
+    a.runs = std::max(1, W);
+    if (p.desc.n2 > 1) {
+        auto kern = p.npts == 6 ? adv_ds_slabs<6> : adv_ds_slabs<4>;
+        cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid_x((p.lines + R - 1) / R), kDsSlabThreads, smem, st>>>(a);
+        return cudaGetLastError();
+    }
     if (W == 2 && adv_ds_runs_ok(p, R)) {
         // long lines: runs of an odd length along two sections per thread
         const int runs_pp = R == 1 ? kDsRunsThreads : kDsRunsThreads / (R / 2);

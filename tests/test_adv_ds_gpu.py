@@ -1,7 +1,7 @@
 """FP64 advection in FP32-pair arithmetic (the FP64 plans' default kernels
 where the shape allows it: degree 3 or 5 with column pairs of an even n2 >= 4
-and n1 >= 128, or contiguous lines of n2 = 1 with n1 % 4 == 0), through the
-C ABI.
+and n1 >= 128, whole slabs of shorter lines with an even n2, or contiguous
+lines of n2 = 1 with n1 % 4 == 0), through the C ABI.
 
 Tolerances:
   - against the staged FP64 kernel (FP64 direct form sum_k w_k f_k, the same
@@ -399,14 +399,151 @@ def test_ds_rows_autotune_keeps_the_kernel(bkma, cuda):
     assert torch.equal(a, b)
 
 
-def test_ds_short_lines_stay_on_the_staged_kernel(bkma, cuda):
-    """Below 128 rows the column-pair kernel's runs are too short: the default
-    is the FP64-arithmetic staged kernel; path 4 can still be chosen."""
-    p = AdvParams(64, 64, 128, 0.001, 0.0, 1.0, -1.0, 1.0)
-    plan = bkma.AdvectionPlan(p.n0, p.n1, p.n2, dtype="f64", dt=p.dt, minVx=p.minVx,
-                              maxVx=p.maxVx)
-    assert plan.info()["path"] == 0, plan.info()
-    assert plan.set_tile(4, 1, 128, 4)["path"] == 4
+# ---- whole slabs of short lines (n1 < 128, even n2): column pairs down
+# whole lines (path 5 with n2 > 1), the column-pair kernel's bits
+
+SLAB_CASES = [
+    # n0, n1, n2, dt, minX, maxX, minVx, maxVx
+    (64, 16, 128, 0.001, 0.0, 1.0, -1.0, 1.0),   # the reference's 2^20 x 16 x 128 sweep shape
+    (17, 64, 24, 0.004, 0.0, 1.0, -2.0, 2.0),    # a last CTA with fewer slabs
+    (40, 48, 6, 0.01, 0.0, 1.0, -3.0, 3.0),      # three pairs per slab: a warp spans slabs
+    (9, 100, 4, 0.02, -0.5, 1.5, -1.0, 1.0),     # shifts of several cells
+]
+
+
+def _slab_plans(bkma, p, **kw):
+    ds, st = _plans(bkma, p, **kw)
+    col = bkma.AdvectionPlan(p.n0, p.n1, p.n2, dt=p.dt, minX=p.minX, maxX=p.maxX,
+                             minVx=p.minVx, maxVx=p.maxVx, dtype="f64", **kw)
+    col.set_tile(4, 1, 128, 4)
+    return ds, st, col
+
+
+@pytest.mark.parametrize("case", SLAB_CASES)
+@pytest.mark.parametrize("degree", [5, 3])
+def test_ds_slabs_equal_column_pair_kernel(bkma, cuda, oracle, case, degree):
+    """Lines shorter than 128 rows with an even n2 default to whole slabs:
+    the column-pair kernel's bits, within the bound of the staged FP64
+    kernel and the oracle."""
+    import torch
+    p = AdvParams(*case)
+    weights = "reference" if degree == 5 else "lagrange"
+    ds, st, col = _slab_plans(bkma, p, degree=degree, weights=weights)
+    assert ds.info()["path"] == 5, ds.info()
+    f0 = _init(p, 32)
+    steps = 3
+    a, b, c = (torch.tensor(f0, device=cuda) for _ in range(3))
+    ds.step(a, nsteps=steps)
+    col.step(b, nsteps=steps)
+    st.step(c, nsteps=steps)
+    ds.status()
+    assert torch.equal(a, b)
+    assert (a - c).abs().max().item() <= TOL * steps * c.abs().max().item()
+    want = oracle.adv_step(p, f0.copy(), steps, degree=degree, ref_weights=degree == 5)
+    assert np.abs(a.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_ds_slabs_per_cta_bit_identical(bkma, cuda):
+    """Any number of slabs per CTA and of runs per column pair (W), in place
+    or out of place: the same bits."""
+    import torch
+    p = AdvParams(*SLAB_CASES[1])
+    f0 = _init(p, 33)
+    ref = None
+    for R, runs in ((1, 1), (2, 1), (3, 2), (8, 4), (1, 8), (5, 3), (2, 64)):
+        ds, _, _ = _slab_plans(bkma, p)
+        ds.set_tile(runs, R, 256, 5)
+        d = torch.tensor(f0, device=cuda)
+        ds.step(d, nsteps=2)
+        ds.status()
+        ref = d if ref is None else ref
+        assert torch.equal(d, ref), (R, runs)
+    oop, _, _ = _slab_plans(bkma, p, inplace=False)
+    src = torch.tensor(f0, device=cuda)
+    out = torch.empty_like(src)
+    oop.step(src, out=out, nsteps=2)
+    assert torch.equal(out, ref)
+
+
+@pytest.mark.parametrize("value", [1e200, 1e-30, float("inf")])
+def test_ds_slabs_unsplittable_value_runs_fp64(bkma, cuda, value):
+    import torch
+    p = AdvParams(*SLAB_CASES[1])
+    ds, _, col = _slab_plans(bkma, p)
+    f0 = _init(p, 34)
+    f0[3, 40, 11] = value
+    a, b = torch.tensor(f0, device=cuda), torch.tensor(f0, device=cuda)
+    ds.step(a)
+    col.step(b)
+    ds.status()
+    assert torch.allclose(a, b, rtol=0, atol=0, equal_nan=True)
+
+
+def test_ds_slabs_exception_lines_bit_identical(bkma, cuda):
+    """n1 = 100 with whole-cell displacements: exception lines run the staged
+    kernel's per-cell FP64 arithmetic."""
+    import torch
+    p = AdvParams(6, 100, 8, 0.01, 0.0, 1.0, -2.0, 3.0)
+    vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
+    ds, st, col = _slab_plans(bkma, p, velocity=vel)
+    assert ds.info()["exception_lines"] > 0 and ds.info()["path"] == 5
+    f0 = _init(p, 35)
+    a, b, c = (torch.tensor(f0, device=cuda) for _ in range(3))
+    ds.step(a, nsteps=2)
+    col.step(b, nsteps=2)
+    st.step(c, nsteps=2)
+    ds.status()
+    assert torch.equal(a, b)
+    assert (a - c).abs().max().item() <= TOL * 2 * c.abs().max().item()
+
+
+def test_ds_slabs_misaligned_field_runs_fp64(bkma, cuda):
+    import torch
+    p = AdvParams(*SLAB_CASES[0])
+    ds, st, _ = _slab_plans(bkma, p)
+    f0 = _init(p, 36)
+    buf = torch.empty(f0.size + 1, dtype=torch.float64, device=cuda)
+    d = buf[1:].view(f0.shape)  # 8 bytes past a 16-byte boundary
+    d.copy_(torch.tensor(f0, device=cuda))
+    ds.step(d, nsteps=2)
+    b = torch.tensor(f0, device=cuda)
+    st.step(b, nsteps=2)
+    assert torch.equal(d, b)
+
+
+def test_ds_slabs_timeout_reported(bkma, cuda):
+    import torch
+    p = AdvParams(*SLAB_CASES[0])
+    ds, _, col = _slab_plans(bkma, p)
+    f0 = torch.tensor(_init(p, 37), device=cuda)
+    a = f0.clone()
+    ds.set_wait_limit(0)
+    ds.step(a)
+    with pytest.raises(bkma.BkmaError) as e:
+        ds.status()
+    assert e.value.status == 4
+    assert torch.equal(a, f0)
+    ds.set_wait_limit(1 << 22)
+    ds.step(a)
+    ds.status()
+    b = f0.clone()
+    col.step(b)
+    assert torch.equal(a, b)
+
+
+def test_ds_slabs_autotune_keeps_the_bits(bkma, cuda):
+    """The tuner picks among slabs per CTA and the column-pair kernels: the
+    same bits whichever wins."""
+    import torch
+    p = AdvParams(*SLAB_CASES[0])
+    ds, _, col = _slab_plans(bkma, p)
+    f0 = torch.tensor(_init(p, 38), device=cuda)
+    info = ds.autotune(f0.clone())
+    assert info["path"] in (4, 5, 6), info
+    a, b = f0.clone(), f0.clone()
+    ds.step(a, nsteps=2)
+    col.step(b, nsteps=2)
+    assert torch.equal(a, b)
 
 
 @pytest.mark.parametrize("R", [1, 2, 8, 16])

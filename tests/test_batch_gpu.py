@@ -56,10 +56,10 @@ def test_batch_bit_identical_to_single_plans(bkma, cuda, dtype):
         plan = bkma.AdvectionPlan(n0, n1, n2, dtype=dtype, degree=f["degree"], weights=f["weights"],
                                   dt=f["dt"], minVx=f["minVx"], maxVx=f["maxVx"], velocity=v)
         path = plan.info()["path"]
-        if path in (4, 5):
+        if path in (4, 5, 6):
             # the batch runs FP64 fields in FP64 arithmetic (staged tiles), the
             # plans' defaults in FP32-pair arithmetic
-            if path == 4:
+            if path in (4, 6):
                 plan.set_tile(8, 1, 256, 0)
             else:
                 plan.set_tile(1, 8, 256, 0)
