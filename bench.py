@@ -321,8 +321,8 @@ def config1_block(bkma_gb300, dev, cores: int):
     It is L2-resident (4 MiB): a parity workload, not a roofline one. Reports
     the plain FP64 kernel (the reference's per-cell math), the staged FP64
     kernel (FP64 arithmetic), the FP64 default (contiguous lines in FP32-pair
-    arithmetic) and the FP32 kernels (GCells/s over 10-step runs, median of
-    5), their error
+    arithmetic), the FP32 kernels, and the 10 steps fused in one launch for
+    each arithmetic (GCells/s over 10-step runs, median of 5), their error
     against the plain form after the 10 steps, and the oracle on the host
     cores on the whole workload."""
     import numpy as np
@@ -348,10 +348,14 @@ def config1_block(bkma_gb300, dev, cores: int):
                  "fp32": (bkma_gb300.AdvectionPlan(n0, n1, n2, dtype="f32", **kw),
                           torch.float32)}
         # the 10 steps in one launch, each line held in shared memory: the
-        # same bits as one step per launch (FP64 staged arithmetic; FP32)
+        # same bits as one step per launch (FP64 staged arithmetic, FP32-pair
+        # arithmetic of the FP64 default, FP32)
         for name, tdt, dt_name in (("staged_fp64_fused", torch.float64, "f64"),
+                                   ("pair_fp64_fused", torch.float64, "f64"),
                                    ("fp32_fused", torch.float32, "f32")):
             pl = bkma_gb300.AdvectionPlan(n0, n1, n2, dtype=dt_name, **kw)
+            if name == "staged_fp64_fused":
+                pl.set_tile(1, 5, 256, 0)
             pl.set_fusion(steps)
             plans[name] = (pl, tdt)
         st = torch.cuda.current_stream()
@@ -372,11 +376,16 @@ def config1_block(bkma_gb300, dev, cores: int):
             res[name] = d
             out[name] = {"gcells_s": n0 * n1 * n2 * steps / (statistics.median(times) / 1e3) / 1e9}
         ref = res["plain_fp64"]
-        for name in ("staged_fp64", "pair_fp64", "fp32", "staged_fp64_fused", "fp32_fused"):
+        for name in ("staged_fp64", "pair_fp64", "fp32", "staged_fp64_fused", "pair_fp64_fused",
+                     "fp32_fused"):
             e = plans["plain_fp64"][0].error_norms(res[name], ref)
             out[name]["max_rel_vs_plain"] = e["max_rel"]
         out["staged_fp64_fused"]["bit_equal_to_one_step_per_launch"] = bool(
             torch.equal(res["staged_fp64_fused"], res["staged_fp64"]))
+        out["pair_fp64_fused"]["bit_equal_to_one_step_per_launch"] = bool(
+            torch.equal(res["pair_fp64_fused"], res["pair_fp64"]))
+        out["pair_fp64_fused"]["kernel"] = ("adv_ds_rows_fused (the 10 steps in one launch, "
+                                            "two shared-memory copies of each line)")
         out["fp32_fused"]["bit_equal_to_one_step_per_launch"] = bool(
             torch.equal(res["fp32_fused"], res["fp32"]))
         out["speedup_staged_vs_plain"] = (out["staged_fp64"]["gcells_s"]
@@ -385,6 +394,8 @@ def config1_block(bkma_gb300, dev, cores: int):
                                               / out["plain_fp64"]["gcells_s"])
         out["speedup_pair_vs_plain"] = (out["pair_fp64"]["gcells_s"]
                                         / out["plain_fp64"]["gcells_s"])
+        out["speedup_pair_fused_vs_plain"] = (out["pair_fp64_fused"]["gcells_s"]
+                                              / out["plain_fp64"]["gcells_s"])
         out["pair_fp64"]["kernel"] = ("adv_ds_rows (FP64 contiguous lines, FP32-pair "
                                       "arithmetic; the FP64 plans' default for n2 = 1)")
         v, c, el = cpu_adv_fields_sample(

@@ -160,7 +160,11 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
  * kernel launch on column strips held in shared memory (the last launch of
  * a call runs the remainder), 1 = one step per launch (default). Results
  * are bit-identical to one step per launch of the staged kernels (FP32; for
- * FP64 the FP64-arithmetic staged kernel, path 0); HBM traffic per cell-step
+ * FP64 the FP64-arithmetic staged kernel, path 0), except for FP64 plans on
+ * contiguous lines in FP32-pair arithmetic (path 5 with n2 = 1, a 16-byte
+ * aligned field, two copies of about 2048 cells' lines in shared memory):
+ * those fuse in that arithmetic, bit-identical to one step per launch of
+ * path 5; HBM traffic per cell-step
  * falls by the factor. Out of place, `data` is left unchanged. Not for the plain
  * FP64 form; BKMA_ERR_UNSUPPORTED when a strip of the plan's n1 rows does
  * not fit shared memory, and for FP32 lines longer than 4608 rows (the strips

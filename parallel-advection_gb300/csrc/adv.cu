@@ -423,13 +423,18 @@ bkma_status adv_launch(AdvPlanImpl &p, void *data, void *out, int nsteps, cudaSt
     const bool inplace = (out == nullptr || out == data);
     if (p.fuse > 1 && nsteps > 0) {
         // k steps per launch; out of place the first launch reads `data` and
-        // writes `out`, later ones run in place on `out`
-        const int W = adv_fused_tile_w(p, kMaxSmem);
+        // writes `out`, later ones run in place on `out`. FP64 contiguous
+        // lines on the FP32-pair kernel fuse in the same arithmetic, the
+        // other plans on the staged kernel's.
         const void *src = data;
         void *dst = inplace ? data : out;
+        const int Rf = adv_ds_rows_fused_r(p);
+        const bool pair = p.path == 5 && adv_ds_rows_fused_ok(p, data, dst, Rf);
+        const int W = pair ? 0 : adv_fused_tile_w(p, kMaxSmem);
         for (int done = 0; done < nsteps;) {
             const int k = std::min(p.fuse, nsteps - done);
-            cudaError_t e = adv_fused_launch(p, src, dst, W, k, st);
+            cudaError_t e = pair ? adv_ds_rows_fused_launch(p, src, dst, Rf, k, st)
+                                 : adv_fused_launch(p, src, dst, W, k, st);
             if (e != cudaSuccess) return cuda_fail(e, "adv fused kernel launch");
             src = dst;
             done += k;

@@ -227,6 +227,124 @@ struct AdvDsRowsArgs {
     uint32_t spin_limit;
 };
 
+// Stage `bytes` contiguous bytes from global memory into S by one bulk copy
+// completed on the barrier *bar (initialised here). Every thread of the CTA
+// calls it; false when the bounded wait gave up (the status is set, the copy
+// has been waited for again so that nothing lands after the CTA leaves):
+// the CTA then returns.
+__device__ __forceinline__ bool stage_block(double *S, const double *src, uint32_t bytes,
+                                            uint64_t *bar, int *status, uint32_t polls) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile(
+            "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
+                smem_u32addr(bar)),
+            "r"(bytes)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                "r"(smem_u32addr(S)),
+            "l"(src), "r"(bytes), "r"(smem_u32addr(bar))
+            : "memory");
+    }
+    if (__syncthreads_and(staging_wait(bar, polls))) return true;
+    if (threadIdx.x == 0) {
+        atomicExch(status, (int)BKMA_ERR_TIMEOUT);
+        staging_wait(bar, kWaitPolls);  // let the copy land before the CTA leaves
+    }
+    return false;
+}
+
+// Cells c0 .. c0 + 3 (c0 % 4 == 0) of line `line` after one step, from its
+// n1 staged values Sl: two packed pairs of the column-pair kernel's stencil
+// from NT + 3 taps split once; a cell whose own window holds a tap the pair
+// cannot carry, and exception lines, in FP64 arithmetic.
+template <int NT>
+__device__ __forceinline__ void ds_quad(const AdvDsRowsArgs &a, const double *Sl, int n1,
+                                        int64_t line, int c0, double (&o)[4]) {
+    constexpr int NW = NT + 3;            // taps of 4 consecutive cells
+    constexpr int NV = (NW + 2) / 2;      // double2s covering them from an even start
+    const int exc = a.exc_index ? a.exc_index[line] : -1;
+    if (exc < 0) {
+        int q = c0 + a.base[line];
+        if (q >= n1) q -= n1;
+        double v[2 * NV];
+        int q2 = q & ~1;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            const double2 t = *reinterpret_cast<const double2 *>(Sl + q2);
+            v[2 * j] = t.x;
+            v[2 * j + 1] = t.y;
+            q2 = q2 + 2 == n1 ? 0 : q2 + 2;
+        }
+        double f[NW];
+        const bool odd = (q & 1) != 0;  // the same for every thread of a line
+#pragma unroll
+        for (int j = 0; j < NW; ++j) f[j] = odd ? v[j + 1] : v[j];
+        float h[NW], lo[NW];
+        bool ok = true;
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            ds_split(f[j], h[j], lo[j]);
+            ok = ok && ds_splittable(f[j]);
+        }
+        float2 A[NT], B[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            const float2 ab = a.w2[line * NT + k];
+            A[k] = make_float2(ab.x, ab.x);
+            B[k] = make_float2(ab.y, ab.y);
+        }
+#pragma unroll
+        for (int pr = 0; pr < 2; ++pr) {
+            float4 T[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k)
+                T[k] = make_float4(h[2 * pr + k], h[2 * pr + k + 1], lo[2 * pr + k],
+                                   lo[2 * pr + k + 1]);
+            const double2 r = ds_stencil<NT>(T, 0, A, B);
+            o[2 * pr] = r.x;
+            o[2 * pr + 1] = r.y;
+        }
+        if (!ok) {
+            // a cell whose own window holds a tap the pair cannot carry:
+            // FP64 direct form, the staged kernel's arithmetic
+            double w64[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k) w64[k] = a.w[line * NT + k];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                bool own = true;
+#pragma unroll
+                for (int k = 0; k < NT; ++k) own = own && ds_splittable(f[m + k]);
+                if (!own) o[m] = stencil_cell<double, NT>(f + m, 1, w64);
+            }
+        }
+    } else {
+        // per-cell stencils of an exception line, FP64 arithmetic
+        const AdvExcCell<double> *cells = a.exc + (int64_t)exc * n1;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const AdvExcCell<double> &e = cells[c0 + m];
+            int q = c0 + m + e.base;
+            if (q >= n1) q -= n1;
+            double f[NT], we[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                f[k] = Sl[q];
+                we[k] = e.w[k];
+                q = q + 1 == n1 ? 0 : q + 1;
+            }
+            o[m] = stencil_cell<double, NT>(f, 1, we);
+        }
+    }
+}
+
 template <int NT>
 __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows(AdvDsRowsArgs a) {
     extern __shared__ __align__(16) double Sd[];
@@ -235,117 +353,48 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows(AdvDsRowsArgs a) {
     const int64_t line0 = (int64_t)blockIdx.x * a.R;
     const int nl = (int)min((int64_t)a.R, a.lines - line0);
     const int total = nl * n1;  // a multiple of 4
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(&bar)));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t bytes = (uint32_t)total * 8u;
-        asm volatile(
-            "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
-                smem_u32addr(&bar)),
-            "r"(bytes)
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-                "r"(smem_u32addr(Sd)),
-            "l"(a.src + line0 * a.n1), "r"(bytes), "r"(smem_u32addr(&bar))
-            : "memory");
-    }
-    if (!__syncthreads_and(staging_wait(&bar, a.spin_limit))) {
-        if (threadIdx.x == 0) {
-            atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
-            staging_wait(&bar, kWaitPolls);  // let the copy land before the CTA leaves
-        }
+    if (!stage_block(Sd, a.src + line0 * a.n1, (uint32_t)total * 8u, &bar, a.status, a.spin_limit))
         return;
-    }
-    constexpr int NW = NT + 3;            // taps of 4 consecutive cells
-    constexpr int NV = (NW + 2) / 2;      // double2s covering them from an even start
     double *G = a.dst + line0 * a.n1;
     for (int i = (int)threadIdx.x * 4; i < total; i += kDsRowsThreads * 4) {
         const int l = i / n1;
-        const int c0 = i - l * n1;
-        const int64_t line = line0 + l;
-        const double *Sl = Sd + (size_t)l * n1;
-        const int exc = a.exc_index ? a.exc_index[line] : -1;
         double o[4];
-        if (exc < 0) {
-            int q = c0 + a.base[line];
-            if (q >= n1) q -= n1;
-            double v[2 * NV];
-            int q2 = q & ~1;
-#pragma unroll
-            for (int j = 0; j < NV; ++j) {
-                const double2 t = *reinterpret_cast<const double2 *>(Sl + q2);
-                v[2 * j] = t.x;
-                v[2 * j + 1] = t.y;
-                q2 = q2 + 2 == n1 ? 0 : q2 + 2;
-            }
-            double f[NW];
-            const bool odd = (q & 1) != 0;  // the same for every thread of a line
-#pragma unroll
-            for (int j = 0; j < NW; ++j) f[j] = odd ? v[j + 1] : v[j];
-            float h[NW], lo[NW];
-            bool ok = true;
-#pragma unroll
-            for (int j = 0; j < NW; ++j) {
-                ds_split(f[j], h[j], lo[j]);
-                ok = ok && ds_splittable(f[j]);
-            }
-            float2 A[NT], B[NT];
-#pragma unroll
-            for (int k = 0; k < NT; ++k) {
-                const float2 ab = a.w2[line * NT + k];
-                A[k] = make_float2(ab.x, ab.x);
-                B[k] = make_float2(ab.y, ab.y);
-            }
-#pragma unroll
-            for (int pr = 0; pr < 2; ++pr) {
-                float4 T[NT];
-#pragma unroll
-                for (int k = 0; k < NT; ++k)
-                    T[k] = make_float4(h[2 * pr + k], h[2 * pr + k + 1], lo[2 * pr + k],
-                                       lo[2 * pr + k + 1]);
-                const double2 r = ds_stencil<NT>(T, 0, A, B);
-                o[2 * pr] = r.x;
-                o[2 * pr + 1] = r.y;
-            }
-            if (!ok) {
-                // a cell whose own window holds a tap the pair cannot carry:
-                // FP64 direct form, the staged kernel's arithmetic
-                double w64[NT];
-#pragma unroll
-                for (int k = 0; k < NT; ++k) w64[k] = a.w[line * NT + k];
-#pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    bool own = true;
-#pragma unroll
-                    for (int k = 0; k < NT; ++k) own = own && ds_splittable(f[m + k]);
-                    if (!own) o[m] = stencil_cell<double, NT>(f + m, 1, w64);
-                }
-            }
-        } else {
-            // per-cell stencils of an exception line, FP64 arithmetic
-            const AdvExcCell<double> *cells = a.exc + (int64_t)exc * n1;
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                const AdvExcCell<double> &e = cells[c0 + m];
-                int q = c0 + m + e.base;
-                if (q >= n1) q -= n1;
-                double f[NT], we[NT];
-#pragma unroll
-                for (int k = 0; k < NT; ++k) {
-                    f[k] = Sl[q];
-                    we[k] = e.w[k];
-                    q = q + 1 == n1 ? 0 : q + 1;
-                }
-                o[m] = stencil_cell<double, NT>(f, 1, we);
-            }
-        }
+        ds_quad<NT>(a, Sd + (size_t)l * n1, n1, line0 + l, i - l * n1, o);
         *reinterpret_cast<double2 *>(G + i) = make_double2(o[0], o[1]);
         *reinterpret_cast<double2 *>(G + i + 2) = make_double2(o[2], o[3]);
+    }
+}
+
+// k steps in one launch on contiguous lines (n2 = 1): the CTA stages its R
+// lines once, then each step computes every cell with ds_quad (the one-step
+// kernels' arithmetic, so the same bits as k steps of them) from one
+// shared-memory copy into the other, a CTA barrier between steps; the last
+// step stores to global memory. HBM traffic is 16 / k bytes per cell-step.
+template <int NT>
+__global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows_fused(AdvDsRowsArgs a, int ksteps) {
+    extern __shared__ __align__(16) double Sd[];  // [2][R * n1]
+    __shared__ __align__(8) uint64_t bar;
+    const int n1 = (int)a.n1;
+    const int64_t line0 = (int64_t)blockIdx.x * a.R;
+    const int nl = (int)min((int64_t)a.R, a.lines - line0);
+    const int total = nl * n1;  // a multiple of 4
+    if (!stage_block(Sd, a.src + line0 * a.n1, (uint32_t)total * 8u, &bar, a.status, a.spin_limit))
+        return;
+    double *cur = Sd, *nxt = Sd + (size_t)a.R * n1;
+    double *G = a.dst + line0 * a.n1;
+    for (int step = 0; step < ksteps; ++step) {
+        double *out = step + 1 == ksteps ? G : nxt;
+        for (int i = (int)threadIdx.x * 4; i < total; i += kDsRowsThreads * 4) {
+            const int l = i / n1;
+            double o[4];
+            ds_quad<NT>(a, cur + (size_t)l * n1, n1, line0 + l, i - l * n1, o);
+            *reinterpret_cast<double2 *>(out + i) = make_double2(o[0], o[1]);
+            *reinterpret_cast<double2 *>(out + i + 2) = make_double2(o[2], o[3]);
+        }
+        __syncthreads();  // the step's cells are written before the next reads them
+        double *t = cur;
+        cur = nxt;
+        nxt = t;
     }
 }
 
@@ -371,32 +420,9 @@ __global__ void __launch_bounds__(kDsSlabThreads, 3) adv_ds_slabs(AdvDsRowsArgs 
     const int64_t slab = a.n1 * a.n2;
     const int64_t line0 = (int64_t)blockIdx.x * a.R;
     const int nl = (int)min((int64_t)a.R, a.lines - line0);
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(&bar)));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t bytes = (uint32_t)(nl * slab) * 8u;
-        asm volatile(
-            "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
-                smem_u32addr(&bar)),
-            "r"(bytes)
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-                "r"(smem_u32addr(Sd)),
-            "l"(a.src + line0 * slab), "r"(bytes), "r"(smem_u32addr(&bar))
-            : "memory");
-    }
-    if (!__syncthreads_and(staging_wait(&bar, a.spin_limit))) {
-        if (threadIdx.x == 0) {
-            atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
-            staging_wait(&bar, kWaitPolls);  // let the copy land before the CTA leaves
-        }
+    if (!stage_block(Sd, a.src + line0 * slab, (uint32_t)(nl * slab) * 8u, &bar, a.status,
+                     a.spin_limit))
         return;
-    }
     const int RP = a.runs;
     const int RL = (n1 + RP - 1) / RP;
     const int units = nl * RP * P2;
@@ -533,32 +559,9 @@ __global__ void __launch_bounds__(kDsRunsThreads, 3) adv_ds_runs(AdvDsRowsArgs a
     const int n1 = (int)a.n1;
     const int64_t line0 = (int64_t)blockIdx.x * a.R;
     const int nl = (int)min((int64_t)a.R, a.lines - line0);
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(&bar)));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t bytes = (uint32_t)nl * (uint32_t)n1 * 8u;
-        asm volatile(
-            "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
-                smem_u32addr(&bar)),
-            "r"(bytes)
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-                "r"(smem_u32addr(Sd)),
-            "l"(a.src + line0 * a.n1), "r"(bytes), "r"(smem_u32addr(&bar))
-            : "memory");
-    }
-    if (!__syncthreads_and(staging_wait(&bar, a.spin_limit))) {
-        if (threadIdx.x == 0) {
-            atomicExch(a.status, (int)BKMA_ERR_TIMEOUT);
-            staging_wait(&bar, kWaitPolls);  // let the copy land before the CTA leaves
-        }
+    if (!stage_block(Sd, a.src + line0 * a.n1, (uint32_t)nl * (uint32_t)n1 * 8u, &bar, a.status,
+                     a.spin_limit))
         return;
-    }
     // sections: pairs of lines (an odd last line pairs with itself and stores
     // once), or the two halves of the CTA's single line
     const bool halves = a.R == 1;
@@ -810,8 +813,9 @@ void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
     *R = (int)std::min<int64_t>(std::max<int64_t>(1, 4096 / n1), p.lines);
 }
 
-cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W, int R,
-                               cudaStream_t st) {
+namespace {
+
+AdvDsRowsArgs rows_args(const AdvPlanImpl &p, const void *src, void *dst, int R) {
     AdvDsRowsArgs a;
     a.src = (const double *)src;
     a.dst = (double *)dst;
@@ -819,6 +823,7 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
     a.n2 = p.desc.n2;
     a.lines = p.lines;
     a.R = R;
+    a.runs = 1;
     a.base = p.d_base;
     a.w = (const double *)p.d_w;
     a.w2 = p.d_w2;
@@ -826,6 +831,39 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
     a.exc = (const AdvExcCell<double> *)p.d_exc;
     a.status = p.d_status;
     a.spin_limit = p.wait_polls;
+    return a;
+}
+
+}  // namespace
+
+int adv_ds_rows_fused_r(const AdvPlanImpl &p) {
+    // about 2048 cells per CTA: two 4-cell groups per thread and step (10
+    // steps per launch, x 1024 x 1, GCells/s for 512 / 2048 / 16384 lines:
+    // 1024 cells 108 / 159 / 181, 2048 cells 107 / 169 / 197, 4096 cells
+    // 98 / 154 / 208)
+    return (int)std::min<int64_t>(std::max<int64_t>(1, 2048 / p.desc.n1), p.lines);
+}
+
+bool adv_ds_rows_fused_ok(const AdvPlanImpl &p, const void *src, const void *dst, int R) {
+    // two copies of the CTA's lines in shared memory
+    return adv_ds_rows_shape_ok(p) && p.desc.n2 == 1 && R >= 1 && ((uintptr_t)src % 16) == 0 &&
+           ((uintptr_t)dst % 16) == 0 && 2 * adv_ds_rows_smem(p, R) <= (size_t)227 * 1024 - 16;
+}
+
+cudaError_t adv_ds_rows_fused_launch(AdvPlanImpl &p, const void *src, void *dst, int R, int k,
+                                     cudaStream_t st) {
+    const AdvDsRowsArgs a = rows_args(p, src, dst, R);
+    const size_t smem = 2 * adv_ds_rows_smem(p, R);
+    auto kern = p.npts == 6 ? adv_ds_rows_fused<6> : adv_ds_rows_fused<4>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid_x((p.lines + R - 1) / R), kDsRowsThreads, smem, st>>>(a, k);
+    return cudaGetLastError();
+}
+
+cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W, int R,
+                               cudaStream_t st) {
+    AdvDsRowsArgs a = rows_args(p, src, dst, R);
     const size_t smem = adv_ds_rows_smem(p, R);
     a.runs = std::max(1, W);
     if (p.desc.n2 > 1) {

@@ -183,6 +183,13 @@ size_t adv_ds_rows_smem(const AdvPlanImpl &p, int R);
 void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R);
 cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W, int R,
                                cudaStream_t st);
+// k fused steps per launch on contiguous lines (n2 = 1) in the same
+// arithmetic (the bits of k steps of adv_ds_rows_launch): R lines per CTA,
+// two copies of them in shared memory.
+int adv_ds_rows_fused_r(const AdvPlanImpl &p);
+bool adv_ds_rows_fused_ok(const AdvPlanImpl &p, const void *src, const void *dst, int R);
+cudaError_t adv_ds_rows_fused_launch(AdvPlanImpl &p, const void *src, void *dst, int R, int k,
+                                     cudaStream_t st);
 // The same arithmetic streamed down column pairs (adv_stream_ds.cu, path 6;
 // FP64, degree 3 or 5, even n2, ds_stream_ok); segs_mode as the FP32
 // streamed form's row-segment mode; exception lines are left to the staged pass.

@@ -399,6 +399,106 @@ def test_ds_rows_autotune_keeps_the_kernel(bkma, cuda):
     assert torch.equal(a, b)
 
 
+# ---- contiguous lines, k steps per launch in the same arithmetic
+
+
+@pytest.mark.parametrize("case", ROWS_CASES)
+@pytest.mark.parametrize("degree", [5, 3])
+def test_ds_rows_fused_bit_identical(bkma, cuda, case, degree):
+    """k fused steps per launch (two shared-memory copies of each line) give
+    the bits of one step per launch of the FP32-pair kernel, for any k and a
+    step count k does not divide; out of place, the input stays as it was."""
+    import torch
+    p = AdvParams(*case)
+    weights = "reference" if degree == 5 else "lagrange"
+    one, _ = _rows_plans(bkma, p, degree=degree, weights=weights)
+    assert one.info()["path"] == 5
+    f0 = _init(p, 40)
+    ref = torch.tensor(f0, device=cuda)
+    one.step(ref, nsteps=7)
+    for k in (2, 3, 7, 10):
+        fz, _ = _rows_plans(bkma, p, degree=degree, weights=weights)
+        fz.set_fusion(k)
+        d = torch.tensor(f0, device=cuda)
+        fz.step(d, nsteps=7)
+        fz.status()
+        assert torch.equal(d, ref), k
+    oop, _ = _rows_plans(bkma, p, degree=degree, weights=weights, inplace=False)
+    oop.set_fusion(3)
+    src = torch.tensor(f0, device=cuda)
+    out = torch.zeros_like(src)
+    oop.step(src, out=out, nsteps=7)
+    assert torch.equal(out, ref)
+    assert torch.equal(src, torch.tensor(f0, device=cuda))
+
+
+def test_ds_rows_fused_exception_lines_and_unsplittable(bkma, cuda, oracle):
+    """Exception lines and windows the pair cannot carry take the FP64
+    arithmetic in every fused step, as in one step per launch."""
+    import torch
+    p = AdvParams(6, 1000, 1, 0.001, 0.0, 1.0, -2.0, 3.0)
+    vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
+    one, _ = _rows_plans(bkma, p, velocity=vel)
+    assert one.info()["exception_lines"] > 0
+    f0 = _init(p, 41)
+    f0[1, 500, 0] = 1e200
+    ref = torch.tensor(f0, device=cuda)
+    one.step(ref, nsteps=5)
+    fz, _ = _rows_plans(bkma, p, velocity=vel)
+    fz.set_fusion(5)
+    d = torch.tensor(f0, device=cuda)
+    fz.step(d, nsteps=5)
+    fz.status()
+    assert torch.allclose(d, ref, rtol=0, atol=0, equal_nan=True)
+    f1 = _init(p, 42)
+    want = oracle.adv_step(p, f1.copy(), 5, velocity=vel)
+    e = torch.tensor(f1, device=cuda)
+    fz.step(e, nsteps=5)
+    assert np.abs(e.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_ds_rows_fused_misaligned_field_runs_fp64(bkma, cuda):
+    """A field off the 16-byte grid runs the FP64 staged arithmetic, fused or
+    not: the same bits either way."""
+    import torch
+    p = AdvParams(*ROWS_CASES[0])
+    one, _ = _rows_plans(bkma, p)
+    fz, _ = _rows_plans(bkma, p)
+    fz.set_fusion(4)
+    f0 = _init(p, 43)
+    views = []
+    for _ in range(2):
+        buf = torch.empty(f0.size + 1, dtype=torch.float64, device=cuda)
+        d = buf[1:].view(f0.shape)  # 8 bytes past a 16-byte boundary
+        d.copy_(torch.tensor(f0, device=cuda))
+        views.append(d)
+    one.step(views[0], nsteps=4)
+    fz.step(views[1], nsteps=4)
+    assert torch.equal(views[0], views[1])
+
+
+def test_ds_rows_fused_timeout_reported(bkma, cuda):
+    import torch
+    p = AdvParams(*ROWS_CASES[0])
+    fz, _ = _rows_plans(bkma, p)
+    fz.set_fusion(4)
+    f0 = torch.tensor(_init(p, 44), device=cuda)
+    a = f0.clone()
+    fz.set_wait_limit(0)
+    fz.step(a, nsteps=4)
+    with pytest.raises(bkma.BkmaError) as e:
+        fz.status()
+    assert e.value.status == 4
+    assert torch.equal(a, f0)
+    fz.set_wait_limit(1 << 22)
+    fz.step(a, nsteps=4)
+    fz.status()
+    one, _ = _rows_plans(bkma, p)
+    b = f0.clone()
+    one.step(b, nsteps=4)
+    assert torch.equal(a, b)
+
+
 # ---- whole slabs of short lines (n1 < 128, even n2): column pairs down
 # whole lines (path 5 with n2 > 1), the column-pair kernel's bits
 
