@@ -299,6 +299,10 @@ bkma_status upload_tables(AdvPlanImpl &p) {
                 stencil_weights(p.desc.weights, NT, d, wd);
                 AdvExcCell<T> &e = cells[(size_t)(slot * n1 + i1)];
                 e.base = (int32_t)b;
+                int64_t dev = (b - p.base[(size_t)l]) % n1;
+                if (dev < 0) dev += n1;
+                dev = std::min(dev, n1 - dev);
+                p.exc_dev = (int)std::max<int64_t>(p.exc_dev, dev);
                 for (int k = 0; k < kMaxTaps; ++k) e.w[k] = k < NT ? (T)wd[k] : T(0);
             }
         }
@@ -604,6 +608,8 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
                 if ((R != p.R || W != p.W) && adv_ds_rows_eligible(p, field, field, R) &&
                     (W == 1 || adv_ds_runs_ok(p, R)))
                     cands.push_back({W, R, 256, 5});
+        if (p.W != 3 && adv_ds_halves_ok(p) && ((uintptr_t)field % 16) == 0)
+            cands.push_back({3, 1, 256, 5});
     } else if (n2 >= 8) {
         for (int W : {8, 16, 32, 64})
             if (W <= n2 || W == 8)
@@ -635,7 +641,9 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
                             : c.path == 4 ? adv_ds_smem(p, c.W)
                             : c.path == 2 || c.path == 6 ? (c.path == 6 ? adv_stream_ds_smem(p) : 0)
                             : c.path == 3 ? adv_rows_smem(p, c.R)
-                            : c.path == 5 ? adv_ds_rows_smem(p, c.R) : p.smem_bytes(c.W, c.R);
+                            : c.path == 5 ? (c.W == 3 && p.desc.n2 == 1 ? adv_ds_halves_smem(p)
+                                                                         : adv_ds_rows_smem(p, c.R))
+                                          : p.smem_bytes(c.W, c.R);
         if (need > kMaxSmem) continue;
         cudaError_t err = launch_once(p, field, field, c.W, c.R, c.threads, c.path, st);  // warm-up
         if (err != cudaSuccess) {
@@ -772,12 +780,15 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
                                  : p.path == 4 ? adv_ds_smem(p, p.W)
                                  : p.path == 2 ? adv_stream_smem()
                                  : p.path == 3 ? adv_rows_smem(p, p.R)
-                                 : p.path == 5 ? adv_ds_rows_smem(p, p.R)
+                                 : p.path == 5 ? (p.W == 3 && p.desc.n2 == 1 ? adv_ds_halves_smem(p)
+                                                                             : adv_ds_rows_smem(p, p.R))
                                  : p.path == 6 ? adv_stream_ds_smem(p)
                                                : p.smem_bytes(p.W, p.R));
     info->npts = p.npts;
     info->autotuned = p.autotuned ? 1 : 0;
-    info->tiles = (p.path == 3 || p.path == 5) ? (p.lines + p.R - 1) / p.R : p.tiles(p.W, p.R);
+    info->tiles = (p.path == 5 && p.W == 3 && p.desc.n2 == 1) ? 2 * p.lines
+                  : (p.path == 3 || p.path == 5)             ? (p.lines + p.R - 1) / p.R
+                                                              : p.tiles(p.W, p.R);
     info->path = p.path;
     return BKMA_OK;
 } BKMA_ABI_CATCH("bkma_adv_plan_info_get")
@@ -840,12 +851,15 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
     } else if (path == 5) {
         const bool slabs = p.desc.n2 > 1;
         BKMA_CHECK_ARG(adv_ds_rows_shape_ok(p) &&
-                           (slabs ? W <= 64
-                                  : (W == 1 || (W == 2 && adv_ds_runs_ok(p, R)))) &&
-                           adv_ds_rows_smem(p, R) <= kMaxSmem,
+                           (slabs ? W <= 64 && adv_ds_rows_smem(p, R) <= kMaxSmem
+                                  : (W == 1 && adv_ds_rows_smem(p, R) <= kMaxSmem) ||
+                                        (W == 2 && adv_ds_runs_ok(p, R) &&
+                                         adv_ds_rows_smem(p, R) <= kMaxSmem) ||
+                                        (W == 3 && R == 1 && adv_ds_halves_ok(p))),
                        "path 5 needs an FP64 plan of degree 3 or 5 with n2 = 1, n1 % 4 == 0, "
                        "n1 >= 16, R lines that fit shared memory and W = 1 (4 cells per thread) "
-                       "or W = 2 (runs along two sections: n1 >= 512, R = 1 or an even R <= 16); "
+                       "or W = 2 (runs along two sections: n1 >= 512, R = 1 or an even R <= 16) "
+                       "or W = 3 (half lines in 2-CTA clusters: n1 >= 8192, R = 1); "
                        "or with an even n2, R whole slabs that fit shared memory and W <= 64 "
                        "runs of rows per column pair");
     }

@@ -227,13 +227,14 @@ struct AdvDsRowsArgs {
     uint32_t spin_limit;
 };
 
-// Stage `bytes` contiguous bytes from global memory into S by one bulk copy
-// completed on the barrier *bar (initialised here). Every thread of the CTA
-// calls it; false when the bounded wait gave up (the status is set, the copy
-// has been waited for again so that nothing lands after the CTA leaves):
-// the CTA then returns.
-__device__ __forceinline__ bool stage_block(double *S, const double *src, uint32_t bytes,
-                                            uint64_t *bar, int *status, uint32_t polls) {
+// Stage bytes0 bytes from src0, then bytes1 bytes from src1 (0: none), into
+// S by bulk copies completed on the barrier *bar (initialised here). Every
+// thread of the CTA calls it; false when the bounded wait gave up (the status
+// is set, and the copies have been waited for again so that nothing lands
+// after the CTA leaves).
+__device__ __forceinline__ bool stage_block2(double *S, const double *src0, uint32_t bytes0,
+                                             const double *src1, uint32_t bytes1, uint64_t *bar,
+                                             int *status, uint32_t polls) {
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32addr(bar)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -244,20 +245,32 @@ __device__ __forceinline__ bool stage_block(double *S, const double *src, uint32
         asm volatile(
             "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
                 smem_u32addr(bar)),
-            "r"(bytes)
+            "r"(bytes0 + bytes1)
             : "memory");
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
                 "r"(smem_u32addr(S)),
-            "l"(src), "r"(bytes), "r"(smem_u32addr(bar))
+            "l"(src0), "r"(bytes0), "r"(smem_u32addr(bar))
             : "memory");
+        if (bytes1)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                    "r"(smem_u32addr(S) + bytes0),
+                "l"(src1), "r"(bytes1), "r"(smem_u32addr(bar))
+                : "memory");
     }
     if (__syncthreads_and(staging_wait(bar, polls))) return true;
     if (threadIdx.x == 0) {
         atomicExch(status, (int)BKMA_ERR_TIMEOUT);
-        staging_wait(bar, kWaitPolls);  // let the copy land before the CTA leaves
+        staging_wait(bar, kWaitPolls);  // let the copies land before the CTA leaves
     }
     return false;
+}
+
+// One contiguous block by one bulk copy.
+__device__ __forceinline__ bool stage_block(double *S, const double *src, uint32_t bytes,
+                                            uint64_t *bar, int *status, uint32_t polls) {
+    return stage_block2(S, src, bytes, src, 0u, bar, status, polls);
 }
 
 // Cells c0 .. c0 + 3 (c0 % 4 == 0) of line `line` after one step, from its
@@ -551,6 +564,9 @@ __global__ void __launch_bounds__(kDsSlabThreads, 3) adv_ds_slabs(AdvDsRowsArgs 
 // kernel's scheme). Windows the pair cannot carry and exception lines run the
 // staged kernel's FP64 arithmetic from the staged lines.
 constexpr int kDsRunsThreads = 256;
+// cells either side of a line's offset that its exception cells' offsets may
+// take (the staged window of a half line; the plan checks it)
+constexpr int kDsHalfMargin = 2;
 
 template <int NT>
 __global__ void __launch_bounds__(kDsRunsThreads, 3) adv_ds_runs(AdvDsRowsArgs a, int rl) {
@@ -704,6 +720,143 @@ __global__ void __launch_bounds__(kDsRunsThreads, 3) adv_ds_runs(AdvDsRowsArgs a
     }
 }
 
+// Lines of 8192 cells and more (64 KB and more: one or two CTAs per SM with
+// the whole line staged) split between the two CTAs of a cluster. CTA h of a
+// line stages only the cells its half's stencils read - [h n1/2 + base - M,
+// (h + 1) n1/2 + base + NT - 1 + M) modulo n1, M = kDsHalfMargin cells for
+// the offsets of exception lines, in at most two bulk copies - and computes
+// its half's cells as the run kernel does, the two lanes of the packed
+// stencil on the half's two quarters. A cluster barrier after the staging
+// orders every read of the line's original values before either CTA writes,
+// so in place is legal; every thread of both CTAs reaches it once, also after
+// a staging timeout. The same per-cell arithmetic as adv_ds_runs: the same bits.
+template <int NT>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kDsRunsThreads, 3)
+    adv_ds_halves(AdvDsRowsArgs a, int rl, int win) {
+    extern __shared__ __align__(16) double Sd[];  // [win] cells of the line from cell w0
+    __shared__ __align__(8) uint64_t bar;
+    const int n1 = (int)a.n1;
+    const int h = n1 / 2, q = n1 / 4;
+    const int64_t line = blockIdx.x >> 1;
+    const int s0 = (int)(blockIdx.x & 1) * h;  // first cell of this CTA's half
+    const int base = a.base[line];
+    // first staged cell, even (16-byte aligned copies)
+    int w0 = (s0 + base - kDsHalfMargin) % n1;
+    if (w0 < 0) w0 += n1;
+    w0 &= ~1;
+    const int first = min(win, n1 - w0);
+    const double *L = a.src + line * a.n1;
+    const bool staged = stage_block2(Sd, L + w0, (uint32_t)first * 8u, L, (uint32_t)(win - first) * 8u,
+                                     &bar, a.status, a.spin_limit);
+    // both halves of the line are staged before either CTA writes to it
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    if (!staged) return;
+    auto local = [&](int g) {  // staged index of cell g of the line
+        int t = g - w0;
+        if (t < 0) t += n1;
+        return t;
+    };
+    const int j = (int)threadIdx.x;
+    const int c0 = j * rl;
+    const int cnt = min(rl, q - c0);
+    if (cnt <= 0) return;
+    double *Gx = a.dst + line * a.n1 + s0 + c0, *Gy = Gx + q;
+    const int e = a.exc_index ? a.exc_index[line] : -1;
+    if (e >= 0) {
+        // an exception line: per-cell stencils in FP64 arithmetic
+        for (int s2 = 0; s2 < 2; ++s2) {
+            const int o = s0 + s2 * q + c0;
+            double *G = s2 ? Gy : Gx;
+            for (int i = 0; i < cnt; ++i) {
+                const AdvExcCell<double> &ec = a.exc[(int64_t)e * n1 + o + i];
+                int g = o + i + ec.base;
+                if (g >= n1) g -= n1;
+                int t = local(g);
+                double f[NT], we[NT];
+#pragma unroll
+                for (int k = 0; k < NT; ++k) {
+                    f[k] = Sd[t + k];
+                    we[k] = ec.w[k];
+                }
+                G[i] = stencil_cell<double, NT>(f, 1, we);
+            }
+        }
+        return;
+    }
+    float2 A[NT], B[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        const float2 ab = a.w2[line * NT + k];
+        A[k] = make_float2(ab.x, ab.x);
+        B[k] = make_float2(ab.y, ab.y);
+    }
+    // tap 0 of the run's first cell in each quarter; the window never wraps
+    int gx = s0 + c0 + base;
+    if (gx >= n1) gx -= n1;
+    const int qx0 = local(gx), qy0 = qx0 + q;
+    int qx = qx0, qy = qy0;
+    float4 T[NT];
+    uint32_t bad = 0;
+#pragma unroll
+    for (int k = 0; k < NT - 1; ++k) {
+        bad = (bad << 1) | (ds_split2(make_double2(Sd[qx], Sd[qy]), T[k]) ? 0u : 1u);
+        ++qx;
+        ++qy;
+    }
+    bool any_bad = false;
+    int i = 0;
+    auto row = [&](auto u_c) {
+        constexpr int u = decltype(u_c)::value;
+        bad = ((bad << 1) | (ds_split2(make_double2(Sd[qx], Sd[qy]), T[(u + NT - 1) % NT]) ? 0u : 1u)) &
+              ((1u << NT) - 1u);
+        ++qx;
+        ++qy;
+        const double2 r = ds_stencil<NT>(T, u, A, B);
+        any_bad = any_bad || bad != 0u;
+        Gx[i] = r.x;
+        Gy[i] = r.y;
+        ++i;
+    };
+    for (; i + NT <= cnt;) {
+        row(std::integral_constant<int, 0>{});
+        row(std::integral_constant<int, 1>{});
+        row(std::integral_constant<int, 2>{});
+        row(std::integral_constant<int, 3>{});
+        if constexpr (NT > 4) {
+            row(std::integral_constant<int, 4 % NT>{});
+            row(std::integral_constant<int, 5 % NT>{});
+        }
+    }
+    if (i < cnt) row(std::integral_constant<int, 0>{});
+    if (i < cnt) row(std::integral_constant<int, 1>{});
+    if (i < cnt) row(std::integral_constant<int, 2>{});
+    if constexpr (NT > 4) {
+        if (i < cnt) row(std::integral_constant<int, 3>{});
+        if (i < cnt) row(std::integral_constant<int, 4 % NT>{});
+    }
+    if (any_bad) {
+        // windows holding a tap the pair cannot carry: each lane's cell by
+        // its own window in FP64 arithmetic (the staged kernel's)
+        double w64[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) w64[k] = a.w[line * NT + k];
+        for (int c = 0; c < cnt; ++c) {
+            double fx[NT], fy[NT];
+            bool okx = true, oky = true;
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                fx[k] = Sd[qx0 + c + k];
+                fy[k] = Sd[qy0 + c + k];
+                okx = okx && ds_splittable(fx[k]);
+                oky = oky && ds_splittable(fy[k]);
+            }
+            if (!okx) Gx[c] = stencil_cell<double, NT>(fx, 1, w64);
+            if (!oky) Gy[c] = stencil_cell<double, NT>(fy, 1, w64);
+        }
+    }
+}
+
 }  // namespace
 
 size_t adv_ds_smem(const AdvPlanImpl &p, int W) {
@@ -799,6 +952,13 @@ void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
     // about 4096 cells (32 KB) per CTA (512 x 1024 x 1: 55.5 GCells/s against
     // 44.5 for 64 CTAs of 8 lines)
     const int64_t n1 = p.desc.n1;
+    if (n1 > 8192 && 2 * p.lines >= 2 * 152 && adv_ds_halves_ok(p)) {
+        // a whole line would leave one CTA per SM, its staging not overlapped
+        // with any arithmetic: half lines in 2-CTA clusters
+        *W = 3;
+        *R = 1;
+        return;
+    }
     if (n1 >= 512) {
         int64_t r = n1 >= 8192 ? 1 : std::max<int64_t>(2, (8192 / n1) & ~int64_t(1));
         r = std::min<int64_t>(r, p.lines);
@@ -836,6 +996,29 @@ AdvDsRowsArgs rows_args(const AdvPlanImpl &p, const void *src, void *dst, int R)
 
 }  // namespace
 
+namespace {
+
+int halves_win(const AdvPlanImpl &p) {
+    // a half line's cells, its stencils' NT - 1 further taps, the margin
+    // either side and one cell of alignment, rounded up to an even count
+    return (int)((p.desc.n1 / 2 + p.npts + 2 * kDsHalfMargin + 1) & ~int64_t(1));
+}
+
+int halves_rl(const AdvPlanImpl &p) {
+    // odd runs over a quarter line
+    return (int)((p.desc.n1 / 4 + kDsRunsThreads - 1) / kDsRunsThreads) | 1;
+}
+
+}  // namespace
+
+size_t adv_ds_halves_smem(const AdvPlanImpl &p) { return (size_t)halves_win(p) * sizeof(double); }
+
+bool adv_ds_halves_ok(const AdvPlanImpl &p) {
+    return adv_ds_rows_shape_ok(p) && p.desc.n2 == 1 && p.desc.n1 >= 8192 &&
+           p.desc.n1 < (1 << 28) && p.lines < (1 << 30) && p.exc_dev <= kDsHalfMargin &&
+           adv_ds_halves_smem(p) <= (size_t)227 * 1024 - 16;
+}
+
 int adv_ds_rows_fused_r(const AdvPlanImpl &p) {
     // about 2048 cells per CTA: two 4-cell groups per thread and step (10
     // steps per launch, x 1024 x 1, GCells/s for 512 / 2048 / 16384 lines:
@@ -872,6 +1055,16 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         kern<<<grid_x((p.lines + R - 1) / R), kDsSlabThreads, smem, st>>>(a);
+        return cudaGetLastError();
+    }
+    if (W == 3 && adv_ds_halves_ok(p)) {
+        // half lines, one per CTA of a 2-CTA cluster
+        const size_t hs = adv_ds_halves_smem(p);
+        auto kern = p.npts == 6 ? adv_ds_halves<6> : adv_ds_halves<4>;
+        cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hs);
+        if (e != cudaSuccess) return e;
+        kern<<<grid_x(2 * p.lines), kDsRunsThreads, hs, st>>>(a, halves_rl(p), halves_win(p));
         return cudaGetLastError();
     }
     if (W == 2 && adv_ds_runs_ok(p, R)) {

@@ -24,6 +24,9 @@ struct AdvPlanImpl {
     std::vector<double> w64;         // per line weights
     std::vector<int32_t> exc_index;  // per line, -1 or exception slot
     int64_t n_exc = 0;
+    // largest distance (cells) of an exception cell's tap offset from its
+    // line's offset at i1 = 0
+    int exc_dev = 0;
     // device tables
     int32_t *d_base = nullptr;
     void *d_w = nullptr;  // T weights
@@ -186,6 +189,10 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
 // k fused steps per launch on contiguous lines (n2 = 1) in the same
 // arithmetic (the bits of k steps of adv_ds_rows_launch): R lines per CTA,
 // two copies of them in shared memory.
+// W = 3 on path 5: lines of 8192 cells and more split between the two CTAs
+// of a cluster (adv_ds_halves), the same bits.
+bool adv_ds_halves_ok(const AdvPlanImpl &p);
+size_t adv_ds_halves_smem(const AdvPlanImpl &p);
 int adv_ds_rows_fused_r(const AdvPlanImpl &p);
 bool adv_ds_rows_fused_ok(const AdvPlanImpl &p, const void *src, const void *dst, int R);
 cudaError_t adv_ds_rows_fused_launch(AdvPlanImpl &p, const void *src, void *dst, int R, int k,

@@ -237,7 +237,9 @@ def _rows_plans(bkma, p, **kw):
     args.update(kw)
     ds = bkma.AdvectionPlan(p.n0, p.n1, p.n2, **args)
     st = bkma.AdvectionPlan(p.n0, p.n1, p.n2, **args)
-    st.set_tile(1, 8, 256, 0)  # the FP64-arithmetic staged kernel on whole rows
+    # the FP64-arithmetic staged kernel on whole rows (8 lines per CTA, fewer
+    # for lines longer than 2048 cells)
+    st.set_tile(1, max(1, min(8, 16384 // p.n1)), 256, 0)
     return ds, st
 
 
@@ -396,6 +398,102 @@ def test_ds_rows_autotune_keeps_the_kernel(bkma, cuda):
     ds.step(a, nsteps=2)
     fresh, _ = _rows_plans(bkma, p)
     fresh.step(b, nsteps=2)
+    assert torch.equal(a, b)
+
+
+# ---- lines of 8192 cells and more: half lines in 2-CTA clusters (W = 3)
+
+
+@pytest.mark.parametrize("n1", [8192, 16384])
+@pytest.mark.parametrize("degree", [5, 3])
+def test_ds_halves_bit_identical(bkma, cuda, oracle, n1, degree):
+    """Each CTA of a cluster stages only its half line's window and writes
+    its half after the cluster barrier: the 4-cell and run kernels' bits, in
+    place and out of place."""
+    import torch
+    p = AdvParams(7, n1, 1, 0.0013, 0.0, 1.0, -2.0, 2.0)
+    weights = "reference" if degree == 5 else "lagrange"
+    f0 = _init(p, 45)
+    outs = []
+    for W, R in ((3, 1), (1, 1), (2, 1)):
+        ds, _ = _rows_plans(bkma, p, degree=degree, weights=weights)
+        info = ds.set_tile(W, R, 256, 5)
+        if W == 3:
+            assert info["tile_cols"] == 3 and info["tiles"] == 2 * p.n0, info
+        d = torch.tensor(f0, device=cuda)
+        ds.step(d, nsteps=3)
+        ds.status()
+        outs.append(d)
+    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
+    oop, _ = _rows_plans(bkma, p, degree=degree, weights=weights, inplace=False)
+    oop.set_tile(3, 1, 256, 5)
+    src = torch.tensor(f0, device=cuda)
+    out = torch.empty_like(src)
+    oop.step(src, out=out, nsteps=3)
+    assert torch.equal(out, outs[0])
+    want = oracle.adv_step(p, f0.copy(), 3, degree=degree, ref_weights=degree == 5)
+    assert np.abs(outs[0].cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_ds_halves_default_for_long_lines(bkma, cuda):
+    """Lines of 16384 cells (128 KB, one CTA per SM whole) default to half
+    lines once there are enough lines to fill the GPU."""
+    p = AdvParams(160, 16384, 1, 0.001, 0.0, 1.0, -1.0, 1.0)
+    ds, _ = _rows_plans(bkma, p)
+    info = ds.info()
+    assert info["path"] == 5 and info["tile_cols"] == 3, info
+
+
+def test_ds_halves_exception_lines_and_unsplittable(bkma, cuda, oracle):
+    """Exception lines (offsets one cell either side of the line's) stay
+    within the staged window; windows the pair cannot carry take FP64."""
+    import torch
+    n1 = 16384
+    # dx = 1.1 / n1 is inexact: the lines shifted by whole cells (v = -2, 3)
+    # have offsets one cell apart along n1
+    p = AdvParams(6, n1, 1, 1.1 / n1, 0.0, 1.1, -2.0, 3.0)
+    vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
+    hv, _ = _rows_plans(bkma, p, velocity=vel)
+    hv.set_tile(3, 1, 256, 5)
+    assert hv.info()["exception_lines"] > 0
+    q, _ = _rows_plans(bkma, p, velocity=vel)
+    q.set_tile(1, 1, 256, 5)
+    f0 = _init(p, 46)
+    f0[2, 8190, 0] = 1e200  # near the seam between the two halves
+    a, b = torch.tensor(f0, device=cuda), torch.tensor(f0, device=cuda)
+    hv.step(a, nsteps=2)
+    q.step(b, nsteps=2)
+    hv.status()
+    assert torch.allclose(a, b, rtol=0, atol=0, equal_nan=True)
+    f1 = _init(p, 47)
+    c = torch.tensor(f1, device=cuda)
+    hv.step(c, nsteps=2)
+    want = oracle.adv_step(p, f1.copy(), 2, velocity=vel)
+    assert np.abs(c.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_ds_halves_timeout_reported(bkma, cuda):
+    """A staging wait that gives up still reaches the cluster barrier: the
+    call returns, the status reports the timeout and the field is untouched."""
+    import torch
+    p = AdvParams(4, 16384, 1, 0.001, 0.0, 1.0, -1.0, 1.0)
+    hv, _ = _rows_plans(bkma, p)
+    hv.set_tile(3, 1, 256, 5)
+    f0 = torch.tensor(_init(p, 48), device=cuda)
+    a = f0.clone()
+    hv.set_wait_limit(0)
+    hv.step(a)
+    with pytest.raises(bkma.BkmaError) as e:
+        hv.status()
+    assert e.value.status == 4
+    assert torch.equal(a, f0)
+    hv.set_wait_limit(1 << 22)
+    hv.step(a)
+    hv.status()
+    q, _ = _rows_plans(bkma, p)
+    q.set_tile(1, 1, 256, 5)
+    b = f0.clone()
+    q.step(b)
     assert torch.equal(a, b)
 
 
