@@ -411,6 +411,125 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows_fused(AdvDsRowsArg
     }
 }
 
+// Contiguous lines in runs of 4-cell groups (path 5, W = 4): each thread
+// walks rq consecutive groups of 4 cells of one line. The NT + 3 taps of a
+// group's windows slide by 4 cells from one group to the next, so a group
+// loads two aligned 16-byte pairs and splits 4 new taps (one per cell, as
+// the ring kernels do), and it stores its cells as two 16-byte pairs, 32
+// contiguous bytes per lane (adv_ds_runs stores 8 bytes per lane, one L2
+// sector per cell: 4x the output in L2 write transactions). The two packed
+// pairs are ds_quad's (cells c, c + 1 and c + 2, c + 3 with the same split
+// taps), so the bits are the 4-cell kernel's; a group whose window holds a
+// tap the pair cannot carry, and exception lines, go through ds_quad itself.
+//
+// Rings of 12 slots: raw value i of a run (cell q2 + i, q2 = the first
+// group's tap 0 rounded down to even) in slot i % 12, split tap m (cell
+// q + m) in slot m % 12. Group u covers raw values 4u .. 4u + NT + 3 and taps
+// 4u .. 4u + NT + 2, so with the groups unrolled by three every slot index is
+// a compile-time constant (4 (u % 3) + i) % 12; the line's parity (q odd)
+// selects between two neighbouring raw slots.
+constexpr int kDsQrunsThreads = 256;
+
+template <int NT>
+__global__ void __launch_bounds__(kDsQrunsThreads, 2) adv_ds_qruns(AdvDsRowsArgs a, int rq) {
+    extern __shared__ __align__(16) double Sd[];
+    __shared__ __align__(8) uint64_t bar;
+    constexpr int NW = NT + 3;  // taps of a group
+    constexpr int E = NW - 4;   // a group's first new tap
+    constexpr int RA = NW - 3;  // a group's first new raw value (even)
+    constexpr int NS = 12;      // ring slots
+    const int n1 = (int)a.n1;
+    const int64_t line0 = (int64_t)blockIdx.x * a.R;
+    const int nl = (int)min((int64_t)a.R, a.lines - line0);
+    if (!stage_block(Sd, a.src + line0 * a.n1, (uint32_t)nl * (uint32_t)n1 * 8u, &bar, a.status,
+                     a.spin_limit))
+        return;
+    const int groups = n1 / 4;
+    const int runs_pl = (groups + rq - 1) / rq;
+    for (int t = (int)threadIdx.x; t < nl * runs_pl; t += kDsQrunsThreads) {
+        const int l = t / runs_pl, j = t - l * runs_pl;
+        const int g0 = j * rq, gn = min(rq, groups - g0);
+        const int64_t line = line0 + l;
+        const double *Sl = Sd + (size_t)l * n1;
+        double *G = a.dst + line * a.n1 + 4 * g0;
+        const int exc = a.exc_index ? a.exc_index[line] : -1;
+        if (exc >= 0) {
+            for (int u = 0; u < gn; ++u) {
+                double o[4];
+                ds_quad<NT>(a, Sl, n1, line, 4 * (g0 + u), o);
+                *reinterpret_cast<double2 *>(G + 4 * u) = make_double2(o[0], o[1]);
+                *reinterpret_cast<double2 *>(G + 4 * u + 2) = make_double2(o[2], o[3]);
+            }
+            continue;
+        }
+        float2 A[NT], B[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            const float2 ab = a.w2[line * NT + k];
+            A[k] = make_float2(ab.x, ab.x);
+            B[k] = make_float2(ab.y, ab.y);
+        }
+        int q = 4 * g0 + a.base[line];
+        if (q >= n1) q -= n1;
+        const bool odd = (q & 1) != 0;
+        int pn = q & ~1;  // cell of the next aligned pair to load
+        double raw[NS];
+        float H[NS], L[NS];
+        uint32_t bad = 0;  // bit m: tap (newest - m) cannot be split
+        auto load2 = [&](int slot) {
+            const double2 v = *reinterpret_cast<const double2 *>(Sl + pn);
+            raw[slot % NS] = v.x;
+            raw[(slot + 1) % NS] = v.y;
+            pn = pn + 2 == n1 ? 0 : pn + 2;
+        };
+        auto split = [&](int m, int i) {  // tap slot m from raw slot i (parity applied)
+            const double f = odd ? raw[(i + 1) % NS] : raw[i % NS];
+            ds_split(f, H[m % NS], L[m % NS]);
+            bad = (bad << 1) | (ds_splittable(f) ? 0u : 1u);
+        };
+        // the first group's raw values 0 .. RA - 1 and taps 0 .. E - 1
+#pragma unroll
+        for (int i = 0; i < RA; i += 2) load2(i);
+#pragma unroll
+        for (int m = 0; m < E; ++m) split(m, m);
+        auto group = [&](auto ph_c, int u) {
+            constexpr int b = 4 * decltype(ph_c)::value;  // 4 (u % 3)
+            // raw values 4u + RA .. 4u + NW, taps 4u + E .. 4u + NW - 1
+            load2(b + RA);
+            load2(b + RA + 2);
+#pragma unroll
+            for (int m = E; m < NW; ++m) split(b + m, b + m);
+            double o[4];
+            if ((bad & ((1u << NW) - 1u)) == 0u) {
+#pragma unroll
+                for (int pr = 0; pr < 2; ++pr) {
+                    float4 T[NT];
+#pragma unroll
+                    for (int k = 0; k < NT; ++k) {
+                        const int s0 = (b + 2 * pr + k) % NS, s1 = (b + 2 * pr + k + 1) % NS;
+                        T[k] = make_float4(H[s0], H[s1], L[s0], L[s1]);
+                    }
+                    const double2 r = ds_stencil<NT>(T, 0, A, B);
+                    o[2 * pr] = r.x;
+                    o[2 * pr + 1] = r.y;
+                }
+            } else {
+                ds_quad<NT>(a, Sl, n1, line, 4 * (g0 + u), o);
+            }
+            *reinterpret_cast<double2 *>(G + 4 * u) = make_double2(o[0], o[1]);
+            *reinterpret_cast<double2 *>(G + 4 * u + 2) = make_double2(o[2], o[3]);
+        };
+        int u = 0;
+        for (; u + 3 <= gn; u += 3) {
+            group(std::integral_constant<int, 0>{}, u);
+            group(std::integral_constant<int, 1>{}, u + 1);
+            group(std::integral_constant<int, 2>{}, u + 2);
+        }
+        if (u < gn) group(std::integral_constant<int, 0>{}, u);
+        if (u + 1 < gn) group(std::integral_constant<int, 1>{}, u + 1);
+    }
+}
+
 // Short lines with an even n2 > 1: whole slabs. A line of the field is a
 // slab of n1 rows x n2 columns, n1 * n2 consecutive doubles, and R
 // consecutive slabs are one contiguous block: a CTA stages them with one bulk
@@ -959,6 +1078,20 @@ void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
         *R = 1;
         return;
     }
+    if (n1 >= 256 && n1 <= 8192) {
+        // runs of 4-cell groups with about 12288 cells (96 KB: two CTAs per
+        // SM) per CTA (x 1 lines, 2^27 cells and more, GCells/s, run kernel
+        // or 4-cell kernel -> group runs: n1 = 256 210 -> 235, 512 203 ->
+        // 222, 1024 208 -> 244, 2048 205 -> 226, 4096 209 -> 245, 8192 205
+        // -> 212; 8192 cells per CTA: 186-212; at n1 = 64 and 128 the 4-cell
+        // kernel stays ahead, 202 / 204 against 198 / 189)
+        const int64_t r = std::min<int64_t>(std::max<int64_t>(1, 12288 / n1), p.lines);
+        if ((p.lines + r - 1) / r >= 2 * 152) {
+            *W = 4;
+            *R = (int)r;
+            return;
+        }
+    }
     if (n1 >= 512) {
         int64_t r = n1 >= 8192 ? 1 : std::max<int64_t>(2, (8192 / n1) & ~int64_t(1));
         r = std::min<int64_t>(r, p.lines);
@@ -1055,6 +1188,18 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         kern<<<grid_x((p.lines + R - 1) / R), kDsSlabThreads, smem, st>>>(a);
+        return cudaGetLastError();
+    }
+    if (W == 4 && p.desc.n2 == 1) {
+        // runs of 4-cell groups: about one run per thread, an odd number of
+        // groups per run (the lanes' 16-byte loads then use 4 of the 8 bank groups)
+        const int64_t groups = (int64_t)R * (p.desc.n1 / 4);
+        const int rq = (int)std::max<int64_t>(1, (groups + kDsQrunsThreads - 1) / kDsQrunsThreads) | 1;
+        auto kern = p.npts == 6 ? adv_ds_qruns<6> : adv_ds_qruns<4>;
+        cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid_x((p.lines + R - 1) / R), kDsQrunsThreads, smem, st>>>(a, rq);
         return cudaGetLastError();
     }
     if (W == 3 && adv_ds_halves_ok(p)) {

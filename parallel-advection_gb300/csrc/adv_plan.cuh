@@ -178,7 +178,9 @@ cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cud
 // The same arithmetic on contiguous lines (FP64, n2 = 1, n1 % 4 == 0, n1 >=
 // 16, degree 3 or 5; path 5): R whole lines per CTA; W = 1: 4 cells per
 // thread, W = 2: runs along two line sections per thread (n1 >= 512, R = 1 or
-// an even R <= 16: adv_ds_runs_ok). Both give the same bits.
+// an even R <= 16: adv_ds_runs_ok), W = 3: half lines (adv_ds_halves_ok),
+// W = 4: runs of 4-cell groups. All give the same bits; with an even n2 > 1,
+// whole slabs with W runs of rows per column pair.
 bool adv_ds_rows_shape_ok(const AdvPlanImpl &p);
 bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R);
 bool adv_ds_runs_ok(const AdvPlanImpl &p, int R);

@@ -401,6 +401,76 @@ def test_ds_rows_autotune_keeps_the_kernel(bkma, cuda):
     assert torch.equal(a, b)
 
 
+# ---- runs of 4-cell groups (W = 4): the 4-cell kernel's bits
+
+
+@pytest.mark.parametrize("case", ROWS_CASES + [(3, 4096, 1, 0.0009, 0.0, 1.0, -1.0, 1.0)])
+@pytest.mark.parametrize("degree", [5, 3])
+def test_ds_group_runs_bit_identical(bkma, cuda, case, degree):
+    """Each thread walks consecutive 4-cell groups with sliding rings of
+    raw and split taps: the 4-cell kernel's bits for any lines per CTA (runs
+    of 1 to many groups, lines of 16 to 4096 cells, odd and even offsets), in
+    place and out of place."""
+    import torch
+    p = AdvParams(*case)
+    weights = "reference" if degree == 5 else "lagrange"
+    f0 = _init(p, 49)
+    ref, _ = _rows_plans(bkma, p, degree=degree, weights=weights)
+    ref.set_tile(1, 1, 256, 5)
+    want = torch.tensor(f0, device=cuda)
+    ref.step(want, nsteps=3)
+    for R in sorted({1, 3, 8, min(64, p.n0)}):
+        if R > p.n0 or R * p.n1 * 8 > 200 * 1024:
+            continue
+        g, _ = _rows_plans(bkma, p, degree=degree, weights=weights)
+        info = g.set_tile(4, R, 256, 5)
+        assert info["path"] == 5 and info["tile_cols"] == 4
+        d = torch.tensor(f0, device=cuda)
+        g.step(d, nsteps=3)
+        g.status()
+        assert torch.equal(d, want), R
+    oop, _ = _rows_plans(bkma, p, degree=degree, weights=weights, inplace=False)
+    oop.set_tile(4, 1, 256, 5)
+    src = torch.tensor(f0, device=cuda)
+    out = torch.empty_like(src)
+    oop.step(src, out=out, nsteps=3)
+    assert torch.equal(out, want)
+
+
+def test_ds_group_runs_exception_lines_and_unsplittable(bkma, cuda):
+    import torch
+    p = AdvParams(6, 1000, 1, 0.001, 0.0, 1.0, -2.0, 3.0)
+    vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
+    g, _ = _rows_plans(bkma, p, velocity=vel)
+    g.set_tile(4, 2, 256, 5)
+    assert g.info()["exception_lines"] > 0
+    q, _ = _rows_plans(bkma, p, velocity=vel)
+    q.set_tile(1, 2, 256, 5)
+    f0 = _init(p, 50)
+    f0[1, 501, 0] = 1e200
+    f0[3, 7, 0] = 5e-324
+    a, b = torch.tensor(f0, device=cuda), torch.tensor(f0, device=cuda)
+    g.step(a, nsteps=2)
+    q.step(b, nsteps=2)
+    g.status()
+    assert torch.allclose(a, b, rtol=0, atol=0, equal_nan=True)
+
+
+def test_ds_group_runs_timeout_reported(bkma, cuda):
+    import torch
+    p = AdvParams(*ROWS_CASES[0])
+    g, _ = _rows_plans(bkma, p)
+    g.set_tile(4, 8, 256, 5)
+    f0 = torch.tensor(_init(p, 51), device=cuda)
+    a = f0.clone()
+    g.set_wait_limit(0)
+    g.step(a)
+    with pytest.raises(bkma.BkmaError) as e:
+        g.status()
+    assert e.value.status == 4
+    assert torch.equal(a, f0)
+
+
 # ---- lines of 8192 cells and more: half lines in 2-CTA clusters (W = 3)
 
 
