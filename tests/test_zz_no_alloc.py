@@ -121,3 +121,38 @@ def test_noalloc_large_batch_matches_plan(bkma, cuda):
     assert _noalloc(lib, x, w, b, stream) == 0, lib.bkma_last_error().decode()
     torch.cuda.synchronize()
     assert torch.equal(x, want)
+
+
+def test_noalloc_replays_in_a_cuda_graph(bkma, cuda):
+    """After one call outside a capture (it resolves the fixed array's
+    address), the entry point records into a CUDA graph on a side stream:
+    replays over new inputs written into the same buffers equal bkma_conv_run,
+    and a replay allocates nothing."""
+    import torch
+    lib = bkma.load()
+    B, Ch, L, K = 4, 128, 4096, 7
+    x, w, b = _inputs(cuda, 11, B, Ch, L, K)
+    assert _noalloc(lib, x.clone(), w, b, torch.cuda.current_stream().cuda_stream) == 0
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        rc = _noalloc(lib, x, w, b, side.cuda_stream)
+    assert rc == 0, lib.bkma_last_error().decode()
+    plan = bkma.Conv1dPlan(B, Ch, Ch, L, K, dtype="bf16", impl="tensor")
+    for seed in (12, 13):
+        x2, w2, b2 = _inputs(cuda, seed, B, Ch, L, K)
+        want = x2.clone()
+        plan.run(want, w2, b2)
+        plan.status()
+        x.copy_(x2)
+        w.copy_(w2)
+        b.copy_(b2)
+        torch.cuda.synchronize()
+        mem0 = torch.cuda.memory_allocated()
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.cuda.memory_allocated() == mem0
+        assert lib.bkma_conv1d_noalloc_status(C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+        assert torch.equal(x, want), seed
