@@ -179,3 +179,82 @@ def test_fuzz_fused_steps(bkma, cuda, case):
     for _ in range(5):
         x2.step(e, nsteps=1)
     assert torch.equal(e, ref)
+
+
+def _pair_cases(n=16, seed=909):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        if rng.integers(0, 2):
+            n1 = int(rng.choice([16, 20, 64, 100, 256, 300, 1000, 1024, 2048, 4096, 8192, 16384]))
+            n2 = 1
+        else:
+            n1 = int(rng.choice([12, 16, 40, 64, 100, 127, 128, 256, 1000]))
+            n2 = int(rng.choice([2, 4, 6, 8, 10, 24, 64, 130]))
+        n0 = int(rng.integers(1, max(2, min(24, 600000 // (n1 * n2)) + 1)))
+        deg = int(rng.choice([3, 5]))
+        vmax = float(rng.choice([0.5, 2.0, 8.0]))
+        dt = float(rng.choice([1e-4, 1e-3, 3e-3]))
+        out.append((n0, n1, n2, deg, vmax, dt, int(rng.integers(0, 1 << 30))))
+    # the long-line forms (half lines from 8192 cells, runs of 4-cell groups)
+    # and large shifts on streamed column pairs, whatever the draws gave
+    out += [(3, 16384, 1, 5, 2.0, 1e-3, 11), (2, 8192, 1, 3, 8.0, 3e-3, 12),
+            (4, 4096, 1, 5, 2.0, 1e-3, 13), (6, 64, 130, 5, 2.0, 1e-3, 14),
+            (5, 1024, 8, 5, 8.0, 3e-3, 15), (4, 2048, 64, 3, 3.0, 2e-3, 16)]
+    return out
+
+
+@pytest.mark.parametrize("case", _pair_cases())
+def test_fuzz_fp64_pair_forms_agree(bkma, cuda, case):
+    """Random FP64 shapes: every FP32-pair form the plan accepts (contiguous
+    lines: 4-cell groups, runs along two sections, half lines in clusters,
+    runs of 4-cell groups, any lines per CTA; even n2: whole slabs with any
+    runs per column pair, staged and streamed column pairs) gives the same
+    bits, lines shifted by whole cells (exception lines) included, and the
+    default plan stays within 1e-11 of the plain FP64 form (degree 5), or
+    2e-13 per step of the FP64-arithmetic staged kernel (degree 3)."""
+    import torch
+    n0, n1, n2, deg, vmax, dt, seed = case
+    rng = np.random.default_rng(seed)
+    vel = rng.uniform(-vmax, vmax, n0)
+    vel[:: 3] = np.round(vel[:: 3] * dt * n1) / (dt * n1)  # whole-cell shifts
+    kw = dict(dtype="f64", degree=deg, weights="reference" if deg == 5 else "lagrange", dt=dt,
+              minX=0.0, maxX=1.0, minVx=-vmax, maxVx=vmax, velocity=vel)
+    x = np.arange(n1) / n1
+    f0 = np.sin(2 * np.pi * x)[None, :, None] + 0.01 * rng.uniform(-1, 1, (n0, n1, n2))
+    if n2 == 1:
+        forms = [(W, R, 256, 5) for W in (1, 2, 3, 4) for R in (1, 2, 3, 8)]
+    else:
+        forms = ([(W, R, 256, 5) for W in (1, 2, 4) for R in (1, 3)]
+                 + [(4, 1, 128, 4), (8, 1, 256, 4), (8, 0, 256, 6), (8, 2, 256, 6)])
+    outs = []
+    for tile in forms:
+        plan = bkma.AdvectionPlan(n0, n1, n2, **kw)
+        try:
+            plan.set_tile(*tile)
+        except bkma.BkmaError:
+            continue  # not a form this shape takes
+        d = torch.tensor(f0, device=cuda)
+        plan.step(d, nsteps=2)
+        plan.status()
+        outs.append((tile, d))
+    if outs:
+        ref_tile, ref = outs[0]
+        for tile, d in outs[1:]:
+            assert torch.equal(d, ref), (ref_tile, tile)
+    auto = bkma.AdvectionPlan(n0, n1, n2, **kw)
+    d = torch.tensor(f0, device=cuda)
+    auto.step(d, nsteps=2)
+    auto.status()
+    r = torch.tensor(f0, device=cuda)
+    if deg == 5:
+        # the plain form: the reference's per-cell arithmetic
+        bkma.AdvectionPlan(n0, n1, n2, impl="plain", **kw).step(r, nsteps=2)
+        tol = 1e-11
+    else:
+        # the FP64-arithmetic staged kernel, same weights: 2e-13 per step
+        st = bkma.AdvectionPlan(n0, n1, n2, **kw)
+        st.set_tile(1, 1, 256, 0)
+        st.step(r, nsteps=2)
+        tol = 4e-13
+    assert ((d - r).abs().max() <= tol * r.abs().max()).item(), auto.info()
