@@ -145,7 +145,8 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * 4 cells per thread, W = 2: runs along two line sections per thread, for
  * n1 >= 512 and R = 1 or an even R <= 16, W = 3: half lines in the two CTAs
  * of a cluster, for n1 >= 8192 and R = 1, W = 4: runs of 4-cell groups per
- * thread, all the same bits; or with an even n2,
+ * thread, W = 5: lines of 16, 32, 64 or 128 cells shared by the lanes of a
+ * warp, all the same bits; or with an even n2,
  * R whole slabs per CTA and W <= 64 runs of rows per column pair, the same
  * bits as path 4; `threads` ignored: 256; a field off the 16-byte grid runs
  * the FP64 staged kernel on whole rows or 8-column strips), or path 6: FP64 column pairs streamed in FP32-pair

@@ -242,7 +242,8 @@ void default_tile(AdvPlanImpl &p) {
             p.path = 5;
             p.W = W;  // lines: 1 = 4 cells per thread, 2 = runs along two
                       // sections, 3 = half lines in 2-CTA clusters, 4 = runs
-                      // of 4-cell groups; slabs: runs of rows per column pair
+                      // of 4-cell groups, 5 = lines shared by a warp's lanes;
+                      // slabs: runs of rows per column pair
             p.R = R;
             p.threads = 256;  // the kernels' fixed CTA
         }
@@ -605,9 +606,9 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
     } else if (p.path == 5) {
         // other line counts per CTA of the same kernel
         for (int R = 1; R <= 1024 && R <= p.lines; R *= 2)
-            for (int W : {1, 2, 4})
+            for (int W : {1, 2, 4, 5})
                 if ((R != p.R || W != p.W) && adv_ds_rows_eligible(p, field, field, R) &&
-                    (W != 2 || adv_ds_runs_ok(p, R)))
+                    (W != 2 || adv_ds_runs_ok(p, R)) && (W != 5 || adv_ds_lineq_ok(p)))
                     cands.push_back({W, R, 256, 5});
         if (p.W != 3 && adv_ds_halves_ok(p) && ((uintptr_t)field % 16) == 0)
             cands.push_back({3, 1, 256, 5});
@@ -853,7 +854,8 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
         const bool slabs = p.desc.n2 > 1;
         BKMA_CHECK_ARG(adv_ds_rows_shape_ok(p) &&
                            (slabs ? W <= 64 && adv_ds_rows_smem(p, R) <= kMaxSmem
-                                  : ((W == 1 || W == 4) && adv_ds_rows_smem(p, R) <= kMaxSmem) ||
+                                  : ((W == 1 || W == 4 || (W == 5 && adv_ds_lineq_ok(p))) &&
+                                     adv_ds_rows_smem(p, R) <= kMaxSmem) ||
                                         (W == 2 && adv_ds_runs_ok(p, R) &&
                                          adv_ds_rows_smem(p, R) <= kMaxSmem) ||
                                         (W == 3 && R == 1 && adv_ds_halves_ok(p))),
@@ -861,7 +863,8 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                        "n1 >= 16, R lines that fit shared memory and W = 1 (4 cells per thread) "
                        "or W = 2 (runs along two sections: n1 >= 512, R = 1 or an even R <= 16) "
                        "or W = 3 (half lines in 2-CTA clusters: n1 >= 8192, R = 1) "
-                       "or W = 4 (runs of 4-cell groups); "
+                       "or W = 4 (runs of 4-cell groups) or W = 5 (lines of 16-128 cells shared "
+                       "by a warp's lanes); "
                        "or with an even n2, R whole slabs that fit shared memory and W <= 64 "
                        "runs of rows per column pair");
     }

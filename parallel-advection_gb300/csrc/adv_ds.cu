@@ -411,6 +411,100 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows_fused(AdvDsRowsArg
     }
 }
 
+// Short contiguous lines shared by the lanes of a warp (path 5, W = 5; n1 =
+// 4 G with G = 4, 8, 16 or 32): the G lanes of a line each take one group of
+// 4 cells. Lane u of a line loads and splits the line's taps 4u .. 4u + 3
+// (cells (q + 4u + e) mod n1, q the line's offset: runtime shared-memory
+// addresses, no parity selects) once, and takes the taps 4u + 4 .. 4u + NT + 2
+// of its group's windows from the next two lanes of the line by width-G warp
+// shuffles: 4 splits per 4 cells, where the 4-cell kernel splits NT + 3. The
+// two packed pairs are ds_quad's with the same split taps, so the bits are
+// the 4-cell kernel's; windows holding a tap the pair cannot carry, and
+// exception lines, go through ds_quad. Every lane of a warp runs every
+// shuffle (the loop covers whole warps; lanes past the CTA's lines compute
+// on line 0 and store nothing). A line's lanes take its groups rotated by
+// the line's index, so that the lines of a warp, which often share an
+// offset, read different banks.
+template <int NT, int G>
+__global__ void __launch_bounds__(kDsRowsThreads) adv_ds_lineq(AdvDsRowsArgs a) {
+    extern __shared__ __align__(16) double Sd[];
+    __shared__ __align__(8) uint64_t bar;
+    constexpr int n1 = 4 * G;
+    constexpr int NW = NT + 3;  // taps of a group
+    const int64_t line0 = (int64_t)blockIdx.x * a.R;
+    const int nl = (int)min((int64_t)a.R, a.lines - line0);
+    if (!stage_block(Sd, a.src + line0 * n1, (uint32_t)nl * (uint32_t)n1 * 8u, &bar, a.status,
+                     a.spin_limit))
+        return;
+    const int total = (nl * G + 31) & ~31;  // whole warps
+    for (int t = (int)threadIdx.x; t < total; t += kDsRowsThreads) {
+        const int l0 = t / G, j = t % G;
+        const bool valid = l0 < nl;
+        const int l = valid ? l0 : 0;
+        const int u = (j + l) & (G - 1);  // this lane's group of the line
+        const int64_t line = line0 + l;
+        const double *Sl = Sd + (size_t)l * n1;
+        const int q = a.base[line];
+        float h[4], lo[4];
+        uint32_t badm = 0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const double f = Sl[(q + 4 * u + e) & (n1 - 1)];
+            ds_split(f, h[e], lo[e]);
+            badm |= ds_splittable(f) ? 0u : (1u << e);
+        }
+        // the next two groups' taps sit with lanes j + 1 and j + 2 of the line
+        const int s1 = (j + 1) & (G - 1), s2 = (j + 2) & (G - 1);
+        float H[NW], L[NW];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            H[e] = h[e];
+            L[e] = lo[e];
+        }
+#pragma unroll
+        for (int e = 0; e < 4 && 4 + e < NW; ++e) {
+            H[4 + e] = __shfl_sync(0xFFFFFFFFu, h[e], s1, G);
+            L[4 + e] = __shfl_sync(0xFFFFFFFFu, lo[e], s1, G);
+        }
+#pragma unroll
+        for (int e = 0; 8 + e < NW; ++e) {
+            H[8 + e] = __shfl_sync(0xFFFFFFFFu, h[e], s2, G);
+            L[8 + e] = __shfl_sync(0xFFFFFFFFu, lo[e], s2, G);
+        }
+        const uint32_t b1 = __shfl_sync(0xFFFFFFFFu, badm, s1, G);
+        const uint32_t b2 = __shfl_sync(0xFFFFFFFFu, badm, s2, G);
+        if (!valid) continue;  // after every shuffle
+        const uint32_t bad = (badm | (b1 << 4) | (b2 << 8)) & ((1u << NW) - 1u);
+        const int exc = a.exc_index ? a.exc_index[line] : -1;
+        double o[4];
+        if (exc >= 0 || bad != 0u) {
+            ds_quad<NT>(a, Sl, n1, line, 4 * u, o);
+        } else {
+            float2 A[NT], B[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                const float2 ab = a.w2[line * NT + k];
+                A[k] = make_float2(ab.x, ab.x);
+                B[k] = make_float2(ab.y, ab.y);
+            }
+#pragma unroll
+            for (int pr = 0; pr < 2; ++pr) {
+                float4 T[NT];
+#pragma unroll
+                for (int k = 0; k < NT; ++k)
+                    T[k] = make_float4(H[2 * pr + k], H[2 * pr + k + 1], L[2 * pr + k],
+                                       L[2 * pr + k + 1]);
+                const double2 r = ds_stencil<NT>(T, 0, A, B);
+                o[2 * pr] = r.x;
+                o[2 * pr + 1] = r.y;
+            }
+        }
+        double *Gq = a.dst + line * n1 + 4 * u;
+        *reinterpret_cast<double2 *>(Gq) = make_double2(o[0], o[1]);
+        *reinterpret_cast<double2 *>(Gq + 2) = make_double2(o[2], o[3]);
+    }
+}
+
 // Contiguous lines in runs of 4-cell groups (path 5, W = 4): each thread
 // walks rq consecutive groups of 4 cells of one line. The NT + 3 taps of a
 // group's windows slide by 4 cells from one group to the next, so a group
@@ -1078,6 +1172,18 @@ void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
         *R = 1;
         return;
     }
+    if (adv_ds_lineq_ok(p)) {
+        // lines of 16-128 cells shared by a warp's lanes, 8192 cells (64 KB)
+        // per CTA (x 1 lines, 2^27 cells and more, GCells/s, 4-cell kernel ->
+        // shared lines: n1 = 16 201 -> 209, 32 200 -> 207, 64 203 -> 212,
+        // 128 205 -> 213; 4096 cells per CTA 195-203, 12288 161-167)
+        const int64_t r = std::min<int64_t>(8192 / n1, p.lines);
+        if ((p.lines + r - 1) / r >= 2 * 152) {
+            *W = 5;
+            *R = (int)r;
+            return;
+        }
+    }
     if (n1 >= 256 && n1 <= 8192) {
         // runs of 4-cell groups with about 12288 cells (96 KB: two CTAs per
         // SM) per CTA (x 1 lines, 2^27 cells and more, GCells/s, run kernel
@@ -1146,6 +1252,12 @@ int halves_rl(const AdvPlanImpl &p) {
 
 size_t adv_ds_halves_smem(const AdvPlanImpl &p) { return (size_t)halves_win(p) * sizeof(double); }
 
+bool adv_ds_lineq_ok(const AdvPlanImpl &p) {
+    const int64_t n1 = p.desc.n1;
+    return adv_ds_rows_shape_ok(p) && p.desc.n2 == 1 &&
+           (n1 == 16 || n1 == 32 || n1 == 64 || n1 == 128);
+}
+
 bool adv_ds_halves_ok(const AdvPlanImpl &p) {
     return adv_ds_rows_shape_ok(p) && p.desc.n2 == 1 && p.desc.n1 >= 8192 &&
            p.desc.n1 < (1 << 28) && p.lines < (1 << 30) && p.exc_dev <= kDsHalfMargin &&
@@ -1188,6 +1300,23 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         kern<<<grid_x((p.lines + R - 1) / R), kDsSlabThreads, smem, st>>>(a);
+        return cudaGetLastError();
+    }
+    if (W == 5 && adv_ds_lineq_ok(p)) {
+        // the lanes of a warp share each short line
+        auto pick = [&](auto g_c) {
+            constexpr int G = decltype(g_c)::value;
+            return p.npts == 6 ? adv_ds_lineq<6, G> : adv_ds_lineq<4, G>;
+        };
+        const int64_t n1 = p.desc.n1;
+        auto kern = n1 == 16   ? pick(std::integral_constant<int, 4>{})
+                    : n1 == 32 ? pick(std::integral_constant<int, 8>{})
+                    : n1 == 64 ? pick(std::integral_constant<int, 16>{})
+                               : pick(std::integral_constant<int, 32>{});
+        cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid_x((p.lines + R - 1) / R), kDsRowsThreads, smem, st>>>(a);
         return cudaGetLastError();
     }
     if (W == 4 && p.desc.n2 == 1) {

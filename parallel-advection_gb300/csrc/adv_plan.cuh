@@ -179,7 +179,8 @@ cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cud
 // 16, degree 3 or 5; path 5): R whole lines per CTA; W = 1: 4 cells per
 // thread, W = 2: runs along two line sections per thread (n1 >= 512, R = 1 or
 // an even R <= 16: adv_ds_runs_ok), W = 3: half lines (adv_ds_halves_ok),
-// W = 4: runs of 4-cell groups. All give the same bits; with an even n2 > 1,
+// W = 4: runs of 4-cell groups, W = 5: lines of 16-128 cells shared by a
+// warp's lanes (adv_ds_lineq_ok). All give the same bits; with an even n2 > 1,
 // whole slabs with W runs of rows per column pair.
 bool adv_ds_rows_shape_ok(const AdvPlanImpl &p);
 bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R);
@@ -194,6 +195,9 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
 // W = 3 on path 5: lines of 8192 cells and more split between the two CTAs
 // of a cluster (adv_ds_halves), the same bits.
 bool adv_ds_halves_ok(const AdvPlanImpl &p);
+// W = 5 on path 5: lines of 16, 32, 64 or 128 cells shared by the lanes of a
+// warp (adv_ds_lineq), the same bits.
+bool adv_ds_lineq_ok(const AdvPlanImpl &p);
 size_t adv_ds_halves_smem(const AdvPlanImpl &p);
 int adv_ds_rows_fused_r(const AdvPlanImpl &p);
 bool adv_ds_rows_fused_ok(const AdvPlanImpl &p, const void *src, const void *dst, int R);

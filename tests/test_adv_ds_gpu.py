@@ -471,6 +471,65 @@ def test_ds_group_runs_timeout_reported(bkma, cuda):
     assert torch.equal(a, f0)
 
 
+# ---- short lines shared by a warp's lanes (W = 5): the 4-cell kernel's bits
+
+
+@pytest.mark.parametrize("n1", [16, 32, 64, 128])
+@pytest.mark.parametrize("degree", [5, 3])
+def test_ds_lineq_bit_identical(bkma, cuda, n1, degree):
+    """The lanes of a line split its taps once each and exchange them by
+    shuffles: the 4-cell kernel's bits for any lines per CTA, with a ragged
+    last CTA (whole warps run the shuffles, lanes past the lines store
+    nothing), in place and out of place."""
+    import torch
+    p = AdvParams(37, n1, 1, 0.003, 0.0, 1.0, -2.0, 2.0)
+    weights = "reference" if degree == 5 else "lagrange"
+    f0 = _init(p, 52)
+    ref, _ = _rows_plans(bkma, p, degree=degree, weights=weights)
+    ref.set_tile(1, 1, 256, 5)
+    want = torch.tensor(f0, device=cuda)
+    ref.step(want, nsteps=3)
+    for R in (1, 3, 8, 37):
+        g, _ = _rows_plans(bkma, p, degree=degree, weights=weights)
+        info = g.set_tile(5, R, 256, 5)
+        assert info["path"] == 5 and info["tile_cols"] == 5
+        d = torch.tensor(f0, device=cuda)
+        g.step(d, nsteps=3)
+        g.status()
+        assert torch.equal(d, want), R
+    oop, _ = _rows_plans(bkma, p, degree=degree, weights=weights, inplace=False)
+    oop.set_tile(5, 8, 256, 5)
+    src = torch.tensor(f0, device=cuda)
+    out = torch.empty_like(src)
+    oop.step(src, out=out, nsteps=3)
+    assert torch.equal(out, want)
+
+
+def test_ds_lineq_exception_lines_and_unsplittable(bkma, cuda, oracle):
+    import torch
+    n1 = 64
+    # dx = 1.1 / n1 is inexact: whole-cell shifts give exception lines
+    p = AdvParams(9, n1, 1, 1.1 / n1, 0.0, 1.1, -2.0, 3.0)
+    vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77, 2.0, -1.0, 0.1])
+    g, _ = _rows_plans(bkma, p, velocity=vel)
+    g.set_tile(5, 4, 256, 5)
+    q, _ = _rows_plans(bkma, p, velocity=vel)
+    q.set_tile(1, 4, 256, 5)
+    f0 = _init(p, 53)
+    f0[4, 10, 0] = 1e200
+    f0[7, 63, 0] = float("inf")
+    a, b = torch.tensor(f0, device=cuda), torch.tensor(f0, device=cuda)
+    g.step(a, nsteps=2)
+    q.step(b, nsteps=2)
+    g.status()
+    assert torch.allclose(a, b, rtol=0, atol=0, equal_nan=True)
+    f1 = _init(p, 54)
+    c = torch.tensor(f1, device=cuda)
+    g.step(c, nsteps=2)
+    want = oracle.adv_step(p, f1.copy(), 2, velocity=vel)
+    assert np.abs(c.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
+
+
 # ---- lines of 8192 cells and more: half lines in 2-CTA clusters (W = 3)
 
 
