@@ -420,7 +420,8 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_rows_fused(AdvDsRowsArg
 // shuffles: 4 splits per 4 cells, where the 4-cell kernel splits NT + 3. The
 // two packed pairs are ds_quad's with the same split taps, so the bits are
 // the 4-cell kernel's; windows holding a tap the pair cannot carry, and
-// exception lines, go through ds_quad. Every lane of a warp runs every
+// exception lines, are redone by ds_quad after the loop (the same thread
+// wrote them). Every lane of a warp runs every
 // shuffle (the loop covers whole warps; lanes past the CTA's lines compute
 // on line 0 and store nothing). A line's lanes take its groups rotated by
 // the line's index, so that the lines of a warp, which often share an
@@ -437,6 +438,7 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_lineq(AdvDsRowsArgs a) 
                      a.spin_limit))
         return;
     const int total = (nl * G + 31) & ~31;  // whole warps
+    bool any_slow = false;
     for (int t = (int)threadIdx.x; t < total; t += kDsRowsThreads) {
         const int l0 = t / G, j = t % G;
         const bool valid = l0 < nl;
@@ -476,29 +478,39 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_lineq(AdvDsRowsArgs a) 
         if (!valid) continue;  // after every shuffle
         const uint32_t bad = (badm | (b1 << 4) | (b2 << 8)) & ((1u << NW) - 1u);
         const int exc = a.exc_index ? a.exc_index[line] : -1;
-        double o[4];
-        if (exc >= 0 || bad != 0u) {
-            ds_quad<NT>(a, Sl, n1, line, 4 * u, o);
-        } else {
-            float2 A[NT], B[NT];
+        // exception lines and windows holding a tap the pair cannot carry
+        // give garbage here and are redone after the loop
+        any_slow = any_slow || exc >= 0 || bad != 0u;
+        float2 A[NT], B[NT];
 #pragma unroll
-            for (int k = 0; k < NT; ++k) {
-                const float2 ab = a.w2[line * NT + k];
-                A[k] = make_float2(ab.x, ab.x);
-                B[k] = make_float2(ab.y, ab.y);
-            }
-#pragma unroll
-            for (int pr = 0; pr < 2; ++pr) {
-                float4 T[NT];
-#pragma unroll
-                for (int k = 0; k < NT; ++k)
-                    T[k] = make_float4(H[2 * pr + k], H[2 * pr + k + 1], L[2 * pr + k],
-                                       L[2 * pr + k + 1]);
-                const double2 r = ds_stencil<NT>(T, 0, A, B);
-                o[2 * pr] = r.x;
-                o[2 * pr + 1] = r.y;
-            }
+        for (int k = 0; k < NT; ++k) {
+            const float2 ab = a.w2[line * NT + k];
+            A[k] = make_float2(ab.x, ab.x);
+            B[k] = make_float2(ab.y, ab.y);
         }
+        double *Gq = a.dst + line * n1 + 4 * u;
+#pragma unroll
+        for (int pr = 0; pr < 2; ++pr) {
+            float4 T[NT];
+#pragma unroll
+            for (int k = 0; k < NT; ++k)
+                T[k] = make_float4(H[2 * pr + k], H[2 * pr + k + 1], L[2 * pr + k], L[2 * pr + k + 1]);
+            *reinterpret_cast<double2 *>(Gq + 2 * pr) = ds_stencil<NT>(T, 0, A, B);
+        }
+    }
+    if (!any_slow) return;
+    // this thread's groups that need ds_quad, over its own stores
+    for (int t = (int)threadIdx.x; t < nl * G; t += kDsRowsThreads) {
+        const int l = t / G;
+        const int u = (t % G + l) & (G - 1);
+        const int64_t line = line0 + l;
+        const double *Sl = Sd + (size_t)l * n1;
+        bool slow = a.exc_index && a.exc_index[line] >= 0;
+        const int q = a.base[line];
+        for (int m = 0; m < NW && !slow; ++m) slow = !ds_splittable(Sl[(q + 4 * u + m) & (n1 - 1)]);
+        if (!slow) continue;
+        double o[4];
+        ds_quad<NT>(a, Sl, n1, line, 4 * u, o);
         double *Gq = a.dst + line * n1 + 4 * u;
         *reinterpret_cast<double2 *>(Gq) = make_double2(o[0], o[1]);
         *reinterpret_cast<double2 *>(Gq + 2) = make_double2(o[2], o[3]);
@@ -516,12 +528,12 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_lineq(AdvDsRowsArgs a) 
 // taps), so the bits are the 4-cell kernel's; a group whose window holds a
 // tap the pair cannot carry, and exception lines, go through ds_quad itself.
 //
-// Rings of 12 slots: raw value i of a run (cell q2 + i, q2 = the first
-// group's tap 0 rounded down to even) in slot i % 12, split tap m (cell
-// q + m) in slot m % 12. Group u covers raw values 4u .. 4u + NT + 3 and taps
-// 4u .. 4u + NT + 2, so with the groups unrolled by three every slot index is
-// a compile-time constant (4 (u % 3) + i) % 12; the line's parity (q odd)
-// selects between two neighbouring raw slots.
+// The split taps sit in a ring of 12 register slots, tap m (cell q + m) in
+// slot m % 12. Group u reads taps 4u .. 4u + NT + 2, so with the groups
+// unrolled by three every slot index is a compile-time constant. The raw
+// values come in aligned pairs (raw value i is cell q2 + i, q2 = q rounded
+// down to even); the line's parity (q odd) picks a group's four new taps out
+// of its two pairs and one raw value carried from the group before.
 constexpr int kDsQrunsThreads = 256;
 
 template <int NT>
@@ -567,51 +579,55 @@ __global__ void __launch_bounds__(kDsQrunsThreads, 2) adv_ds_qruns(AdvDsRowsArgs
         if (q >= n1) q -= n1;
         const bool odd = (q & 1) != 0;
         int pn = q & ~1;  // cell of the next aligned pair to load
-        double raw[NS];
         float H[NS], L[NS];
         uint32_t bad = 0;  // bit m: tap (newest - m) cannot be split
-        auto load2 = [&](int slot) {
+        auto load2 = [&]() {
             const double2 v = *reinterpret_cast<const double2 *>(Sl + pn);
-            raw[slot % NS] = v.x;
-            raw[(slot + 1) % NS] = v.y;
             pn = pn + 2 == n1 ? 0 : pn + 2;
+            return v;
         };
-        auto split = [&](int m, int i) {  // tap slot m from raw slot i (parity applied)
-            const double f = odd ? raw[(i + 1) % NS] : raw[i % NS];
+        auto split = [&](int m, double f) {  // tap m (slot m % NS)
             ds_split(f, H[m % NS], L[m % NS]);
             bad = (bad << 1) | (ds_splittable(f) ? 0u : 1u);
         };
-        // the first group's raw values 0 .. RA - 1 and taps 0 .. E - 1
+        // raw value i of the run is cell q2 + i and tap m is raw value m + odd:
+        // the first group's raw values 0 .. RA - 1 give taps 0 .. E - 1, and
+        // each group's two pairs (raw 4u + RA .. 4u + RA + 3) its taps
+        // 4u + E .. 4u + NW - 1 with one raw value carried from the group before
+        double carry;
+        {
+            double r[RA];
 #pragma unroll
-        for (int i = 0; i < RA; i += 2) load2(i);
+            for (int i = 0; i < RA; i += 2) {
+                const double2 v = load2();
+                r[i] = v.x;
+                r[i + 1] = v.y;
+            }
 #pragma unroll
-        for (int m = 0; m < E; ++m) split(m, m);
+            for (int m = 0; m < E; ++m) split(m, odd ? r[m + 1] : r[m]);
+            carry = r[RA - 1];
+        }
+        bool any_bad = false;
         auto group = [&](auto ph_c, int u) {
             constexpr int b = 4 * decltype(ph_c)::value;  // 4 (u % 3)
-            // raw values 4u + RA .. 4u + NW, taps 4u + E .. 4u + NW - 1
-            load2(b + RA);
-            load2(b + RA + 2);
+            const double2 v0 = load2(), v1 = load2();
+            const double f[5] = {carry, v0.x, v0.y, v1.x, v1.y};
 #pragma unroll
-            for (int m = E; m < NW; ++m) split(b + m, b + m);
-            double o[4];
-            if ((bad & ((1u << NW) - 1u)) == 0u) {
+            for (int m = 0; m < NW - E; ++m) split(b + E + m, odd ? f[m + 1] : f[m]);
+            carry = v1.y;
+            // a window holding a tap the pair cannot carry gives garbage here
+            // and is redone after the run
+            any_bad = any_bad || (bad & ((1u << NW) - 1u)) != 0u;
 #pragma unroll
-                for (int pr = 0; pr < 2; ++pr) {
-                    float4 T[NT];
+            for (int pr = 0; pr < 2; ++pr) {
+                float4 T[NT];
 #pragma unroll
-                    for (int k = 0; k < NT; ++k) {
-                        const int s0 = (b + 2 * pr + k) % NS, s1 = (b + 2 * pr + k + 1) % NS;
-                        T[k] = make_float4(H[s0], H[s1], L[s0], L[s1]);
-                    }
-                    const double2 r = ds_stencil<NT>(T, 0, A, B);
-                    o[2 * pr] = r.x;
-                    o[2 * pr + 1] = r.y;
+                for (int k = 0; k < NT; ++k) {
+                    const int s0 = (b + 2 * pr + k) % NS, s1 = (b + 2 * pr + k + 1) % NS;
+                    T[k] = make_float4(H[s0], H[s1], L[s0], L[s1]);
                 }
-            } else {
-                ds_quad<NT>(a, Sl, n1, line, 4 * (g0 + u), o);
+                *reinterpret_cast<double2 *>(G + 4 * u + 2 * pr) = ds_stencil<NT>(T, 0, A, B);
             }
-            *reinterpret_cast<double2 *>(G + 4 * u) = make_double2(o[0], o[1]);
-            *reinterpret_cast<double2 *>(G + 4 * u + 2) = make_double2(o[2], o[3]);
         };
         int u = 0;
         for (; u + 3 <= gn; u += 3) {
@@ -621,6 +637,23 @@ __global__ void __launch_bounds__(kDsQrunsThreads, 2) adv_ds_qruns(AdvDsRowsArgs
         }
         if (u < gn) group(std::integral_constant<int, 0>{}, u);
         if (u + 1 < gn) group(std::integral_constant<int, 1>{}, u + 1);
+        if (!any_bad) continue;
+        // the groups whose window holds a tap the pair cannot carry: ds_quad,
+        // over this thread's own stores
+        for (int v = 0; v < gn; ++v) {
+            int c = 4 * (g0 + v) + a.base[line];
+            if (c >= n1) c -= n1;
+            bool ok = true;
+            for (int m = 0; m < NW; ++m) {
+                ok = ok && ds_splittable(Sl[c]);
+                c = c + 1 == n1 ? 0 : c + 1;
+            }
+            if (ok) continue;
+            double o[4];
+            ds_quad<NT>(a, Sl, n1, line, 4 * (g0 + v), o);
+            *reinterpret_cast<double2 *>(G + 4 * v) = make_double2(o[0], o[1]);
+            *reinterpret_cast<double2 *>(G + 4 * v + 2) = make_double2(o[2], o[3]);
+        }
     }
 }
 
@@ -1175,8 +1208,9 @@ void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
     if (adv_ds_lineq_ok(p)) {
         // lines of 16-128 cells shared by a warp's lanes, 8192 cells (64 KB)
         // per CTA (x 1 lines, 2^27 cells and more, GCells/s, 4-cell kernel ->
-        // shared lines: n1 = 16 201 -> 209, 32 200 -> 207, 64 203 -> 212,
-        // 128 205 -> 213; 4096 cells per CTA 195-203, 12288 161-167)
+        // shared lines: n1 = 16 201 -> 213, 32 200 -> 213, 64 203 -> 219,
+        // 128 205 -> 217; 4096 cells per CTA 199-206, 12288 165-173; runs of
+        // 4-cell groups 199-225)
         const int64_t r = std::min<int64_t>(8192 / n1, p.lines);
         if ((p.lines + r - 1) / r >= 2 * 152) {
             *W = 5;
@@ -1187,10 +1221,8 @@ void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
     if (n1 >= 256 && n1 <= 8192) {
         // runs of 4-cell groups with about 12288 cells (96 KB: two CTAs per
         // SM) per CTA (x 1 lines, 2^27 cells and more, GCells/s, run kernel
-        // or 4-cell kernel -> group runs: n1 = 256 210 -> 235, 512 203 ->
-        // 222, 1024 208 -> 244, 2048 205 -> 226, 4096 209 -> 245, 8192 205
-        // -> 212; 8192 cells per CTA: 186-212; at n1 = 64 and 128 the 4-cell
-        // kernel stays ahead, 202 / 204 against 198 / 189)
+        // or 4-cell kernel -> group runs: n1 = 256 210 -> 261, 1024 208 ->
+        // 270, 4096 209 -> 272, 8192 205 -> 230; 8192 cells per CTA: 222-248)
         const int64_t r = std::min<int64_t>(std::max<int64_t>(1, 12288 / n1), p.lines);
         if ((p.lines + r - 1) / r >= 2 * 152) {
             *W = 4;
