@@ -146,7 +146,8 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * n1 >= 512 and R = 1 or an even R <= 16, W = 3: half lines in the two CTAs
  * of a cluster, for n1 >= 8192 and R = 1, W = 4: runs of 4-cell groups per
  * thread, W = 5: lines of 16, 32, 64 or 128 cells shared by the lanes of a
- * warp, all the same bits; or with an even n2,
+ * warp, W = 6: half lines in clusters as W = 3, in runs of 4-cell groups as
+ * W = 4, all the same bits; or with an even n2,
  * R whole slabs per CTA and W <= 64 runs of rows per column pair, the same
  * bits as path 4; `threads` ignored: 256; a field off the 16-byte grid runs
  * the FP64 staged kernel on whole rows or 8-column strips), or path 6: FP64 column pairs streamed in FP32-pair

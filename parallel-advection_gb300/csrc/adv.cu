@@ -242,7 +242,8 @@ void default_tile(AdvPlanImpl &p) {
             p.path = 5;
             p.W = W;  // lines: 1 = 4 cells per thread, 2 = runs along two
                       // sections, 3 = half lines in 2-CTA clusters, 4 = runs
-                      // of 4-cell groups, 5 = lines shared by a warp's lanes;
+                      // of 4-cell groups, 5 = lines shared by a warp's lanes,
+                      // 6 = half lines in runs of 4-cell groups;
                       // slabs: runs of rows per column pair
             p.R = R;
             p.threads = 256;  // the kernels' fixed CTA
@@ -643,7 +644,7 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
                             : c.path == 4 ? adv_ds_smem(p, c.W)
                             : c.path == 2 || c.path == 6 ? (c.path == 6 ? adv_stream_ds_smem(p) : 0)
                             : c.path == 3 ? adv_rows_smem(p, c.R)
-                            : c.path == 5 ? (c.W == 3 && p.desc.n2 == 1 ? adv_ds_halves_smem(p)
+                            : c.path == 5 ? ((c.W == 3 || c.W == 6) && p.desc.n2 == 1 ? adv_ds_halves_smem(p)
                                                                          : adv_ds_rows_smem(p, c.R))
                                           : p.smem_bytes(c.W, c.R);
         if (need > kMaxSmem) continue;
@@ -782,13 +783,13 @@ bkma_status bkma_adv_plan_info_get(const bkma_adv_plan *plan, bkma_adv_plan_info
                                  : p.path == 4 ? adv_ds_smem(p, p.W)
                                  : p.path == 2 ? adv_stream_smem()
                                  : p.path == 3 ? adv_rows_smem(p, p.R)
-                                 : p.path == 5 ? (p.W == 3 && p.desc.n2 == 1 ? adv_ds_halves_smem(p)
+                                 : p.path == 5 ? ((p.W == 3 || p.W == 6) && p.desc.n2 == 1 ? adv_ds_halves_smem(p)
                                                                              : adv_ds_rows_smem(p, p.R))
                                  : p.path == 6 ? adv_stream_ds_smem(p)
                                                : p.smem_bytes(p.W, p.R));
     info->npts = p.npts;
     info->autotuned = p.autotuned ? 1 : 0;
-    info->tiles = (p.path == 5 && p.W == 3 && p.desc.n2 == 1) ? 2 * p.lines
+    info->tiles = (p.path == 5 && (p.W == 3 || p.W == 6) && p.desc.n2 == 1) ? 2 * p.lines
                   : (p.path == 3 || p.path == 5)             ? (p.lines + p.R - 1) / p.R
                                                               : p.tiles(p.W, p.R);
     info->path = p.path;
@@ -858,7 +859,7 @@ bkma_status bkma_adv_plan_set_tile(bkma_adv_plan *plan, int32_t W, int32_t R, in
                                      adv_ds_rows_smem(p, R) <= kMaxSmem) ||
                                         (W == 2 && adv_ds_runs_ok(p, R) &&
                                          adv_ds_rows_smem(p, R) <= kMaxSmem) ||
-                                        (W == 3 && R == 1 && adv_ds_halves_ok(p))),
+                                        ((W == 3 || W == 6) && R == 1 && adv_ds_halves_ok(p))),
                        "path 5 needs an FP64 plan of degree 3 or 5 with n2 = 1, n1 % 4 == 0, "
                        "n1 >= 16, R lines that fit shared memory and W = 1 (4 cells per thread) "
                        "or W = 2 (runs along two sections: n1 >= 512, R = 1 or an even R <= 16) "

@@ -1103,6 +1103,145 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kDsRunsThreads, 3)
     }
 }
 
+// Half lines in 2-CTA clusters (staged and ordered as in adv_ds_halves)
+// computed in runs of 4-cell groups (the rings of adv_ds_qruns, 32
+// contiguous bytes stored per lane and group): the half's window needs no
+// wrap, so the rings load plain staged indices. A cell whose own window holds
+// a tap the pair cannot carry is redone in FP64 after the run, as ds_quad
+// does; exception lines take per-cell FP64 stencils. The same bits.
+template <int NT>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kDsQrunsThreads, 2)
+    adv_ds_halves_q(AdvDsRowsArgs a, int rq, int win) {
+    extern __shared__ __align__(16) double Sd[];  // [win] cells of the line from cell w0
+    __shared__ __align__(8) uint64_t bar;
+    constexpr int NW = NT + 3;  // taps of a group
+    constexpr int E = NW - 4;   // a group's first new tap
+    constexpr int RA = NW - 3;  // a group's first new raw value (even)
+    constexpr int NS = 12;      // ring slots
+    const int n1 = (int)a.n1;
+    const int h = n1 / 2;
+    const int64_t line = blockIdx.x >> 1;
+    const int s0 = (int)(blockIdx.x & 1) * h;  // first cell of this CTA's half
+    const int base = a.base[line];
+    int w0 = (s0 + base - kDsHalfMargin) % n1;  // first staged cell, even
+    if (w0 < 0) w0 += n1;
+    w0 &= ~1;
+    const int first = min(win, n1 - w0);
+    const double *Lp = a.src + line * a.n1;
+    const bool staged = stage_block2(Sd, Lp + w0, (uint32_t)first * 8u, Lp,
+                                     (uint32_t)(win - first) * 8u, &bar, a.status, a.spin_limit);
+    // both halves of the line are staged before either CTA writes to it
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    if (!staged) return;
+    auto local = [&](int g) {  // staged index of cell g of the line
+        int t = g - w0;
+        if (t < 0) t += n1;
+        return t;
+    };
+    const int off = local(s0 + base >= n1 ? s0 + base - n1 : s0 + base);  // tap 0 of cell s0
+    const int groups = h / 4;
+    const int e = a.exc_index ? a.exc_index[line] : -1;
+    double *G = a.dst + line * a.n1 + s0;
+    float2 A[NT], B[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        const float2 ab = a.w2[line * NT + k];
+        A[k] = make_float2(ab.x, ab.x);
+        B[k] = make_float2(ab.y, ab.y);
+    }
+    for (int t = (int)threadIdx.x; t * rq < groups; t += kDsQrunsThreads) {
+        const int g0 = t * rq, gn = min(rq, groups - g0);
+        bool any_bad = e >= 0;
+        if (e < 0) {
+            const int q = off + 4 * g0;  // staged index of the run's tap 0
+            const bool odd = (q & 1) != 0;
+            int pn = q & ~1;
+            float H[NS], L[NS];
+            uint32_t bad = 0;
+            auto load2 = [&]() {
+                const double2 v = *reinterpret_cast<const double2 *>(Sd + pn);
+                pn += 2;
+                return v;
+            };
+            auto split = [&](int m, double f) {
+                ds_split(f, H[m % NS], L[m % NS]);
+                bad = (bad << 1) | (ds_splittable(f) ? 0u : 1u);
+            };
+            double carry;
+            {
+                double r[RA];
+#pragma unroll
+                for (int i = 0; i < RA; i += 2) {
+                    const double2 v = load2();
+                    r[i] = v.x;
+                    r[i + 1] = v.y;
+                }
+#pragma unroll
+                for (int m = 0; m < E; ++m) split(m, odd ? r[m + 1] : r[m]);
+                carry = r[RA - 1];
+            }
+            auto group = [&](auto ph_c, int u) {
+                constexpr int b = 4 * decltype(ph_c)::value;  // 4 (u % 3)
+                const double2 v0 = load2(), v1 = load2();
+                const double f[5] = {carry, v0.x, v0.y, v1.x, v1.y};
+#pragma unroll
+                for (int m = 0; m < NW - E; ++m) split(b + E + m, odd ? f[m + 1] : f[m]);
+                carry = v1.y;
+                any_bad = any_bad || (bad & ((1u << NW) - 1u)) != 0u;
+                double *Gq = G + 4 * (g0 + u);
+#pragma unroll
+                for (int pr = 0; pr < 2; ++pr) {
+                    float4 T[NT];
+#pragma unroll
+                    for (int k = 0; k < NT; ++k) {
+                        const int t0 = (b + 2 * pr + k) % NS, t1 = (b + 2 * pr + k + 1) % NS;
+                        T[k] = make_float4(H[t0], H[t1], L[t0], L[t1]);
+                    }
+                    *reinterpret_cast<double2 *>(Gq + 2 * pr) = ds_stencil<NT>(T, 0, A, B);
+                }
+            };
+            int u = 0;
+            for (; u + 3 <= gn; u += 3) {
+                group(std::integral_constant<int, 0>{}, u);
+                group(std::integral_constant<int, 1>{}, u + 1);
+                group(std::integral_constant<int, 2>{}, u + 2);
+            }
+            if (u < gn) group(std::integral_constant<int, 0>{}, u);
+            if (u + 1 < gn) group(std::integral_constant<int, 1>{}, u + 1);
+        }
+        if (!any_bad) continue;
+        // per cell in FP64: an exception line's cells with their own weights,
+        // otherwise the cells whose own window the pair cannot carry (this
+        // thread's own stores)
+        double w64[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) w64[k] = a.w[line * NT + k];
+        for (int c = 4 * g0; c < 4 * (g0 + gn); ++c) {
+            double fv[NT], we[NT];
+            int t0 = off + c;
+            if (e >= 0) {
+                const AdvExcCell<double> &ec = a.exc[(int64_t)e * n1 + s0 + c];
+                int g = s0 + c + ec.base;
+                if (g >= n1) g -= n1;
+                t0 = local(g);
+#pragma unroll
+                for (int k = 0; k < NT; ++k) we[k] = ec.w[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < NT; ++k) we[k] = w64[k];
+            }
+            bool ok = e < 0;
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                fv[k] = Sd[t0 + k];
+                ok = ok && ds_splittable(fv[k]);
+            }
+            if (!ok) G[c] = stencil_cell<double, NT>(fv, 1, we);
+        }
+    }
+}
+
 }  // namespace
 
 size_t adv_ds_smem(const AdvPlanImpl &p, int W) {
@@ -1200,8 +1339,12 @@ void adv_ds_rows_default(const AdvPlanImpl &p, int *W, int *R) {
     const int64_t n1 = p.desc.n1;
     if (n1 > 8192 && 2 * p.lines >= 2 * 152 && adv_ds_halves_ok(p)) {
         // a whole line would leave one CTA per SM, its staging not overlapped
-        // with any arithmetic: half lines in 2-CTA clusters
-        *W = 3;
+        // with any arithmetic: half lines in 2-CTA clusters, in runs of 4-cell
+        // groups (2^17 x 16384 x 1, GCells/s: whole lines 190, half lines
+        // with runs along the quarters 207, with runs of 4-cell groups 215;
+        // at 8192 cells the half lines' 32 KB leave too little in flight:
+        // 169 against 233 for whole lines in runs of 4-cell groups)
+        *W = 6;
         *R = 1;
         return;
     }
@@ -1361,6 +1504,18 @@ cudaError_t adv_ds_rows_launch(AdvPlanImpl &p, const void *src, void *dst, int W
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         kern<<<grid_x((p.lines + R - 1) / R), kDsQrunsThreads, smem, st>>>(a, rq);
+        return cudaGetLastError();
+    }
+    if (W == 6 && adv_ds_halves_ok(p)) {
+        // half lines in 2-CTA clusters, runs of 4-cell groups
+        const size_t hs = adv_ds_halves_smem(p);
+        const int groups = (int)(p.desc.n1 / 8);
+        const int rq = std::max(1, (groups + kDsQrunsThreads - 1) / kDsQrunsThreads) | 1;
+        auto kern = p.npts == 6 ? adv_ds_halves_q<6> : adv_ds_halves_q<4>;
+        cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hs);
+        if (e != cudaSuccess) return e;
+        kern<<<grid_x(2 * p.lines), kDsQrunsThreads, hs, st>>>(a, rq, halves_win(p));
         return cudaGetLastError();
     }
     if (W == 3 && adv_ds_halves_ok(p)) {

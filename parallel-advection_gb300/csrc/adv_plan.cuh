@@ -180,7 +180,8 @@ cudaError_t adv_ds_launch(AdvPlanImpl &p, const void *src, void *dst, int W, cud
 // thread, W = 2: runs along two line sections per thread (n1 >= 512, R = 1 or
 // an even R <= 16: adv_ds_runs_ok), W = 3: half lines (adv_ds_halves_ok),
 // W = 4: runs of 4-cell groups, W = 5: lines of 16-128 cells shared by a
-// warp's lanes (adv_ds_lineq_ok). All give the same bits; with an even n2 > 1,
+// warp's lanes (adv_ds_lineq_ok), W = 6: half lines in runs of 4-cell groups
+// (adv_ds_halves_ok). All give the same bits; with an even n2 > 1,
 // whole slabs with W runs of rows per column pair.
 bool adv_ds_rows_shape_ok(const AdvPlanImpl &p);
 bool adv_ds_rows_eligible(const AdvPlanImpl &p, const void *src, const void *dst, int R);

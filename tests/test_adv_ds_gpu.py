@@ -544,18 +544,19 @@ def test_ds_halves_bit_identical(bkma, cuda, oracle, n1, degree):
     weights = "reference" if degree == 5 else "lagrange"
     f0 = _init(p, 45)
     outs = []
-    for W, R in ((3, 1), (1, 1), (2, 1)):
+    for W, R in ((3, 1), (1, 1), (2, 1), (6, 1)):
         ds, _ = _rows_plans(bkma, p, degree=degree, weights=weights)
         info = ds.set_tile(W, R, 256, 5)
-        if W == 3:
-            assert info["tile_cols"] == 3 and info["tiles"] == 2 * p.n0, info
+        if W in (3, 6):
+            assert info["tile_cols"] == W and info["tiles"] == 2 * p.n0, info
         d = torch.tensor(f0, device=cuda)
         ds.step(d, nsteps=3)
         ds.status()
         outs.append(d)
-    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
+    for o in outs[1:]:
+        assert torch.equal(outs[0], o)
     oop, _ = _rows_plans(bkma, p, degree=degree, weights=weights, inplace=False)
-    oop.set_tile(3, 1, 256, 5)
+    oop.set_tile(6, 1, 256, 5)
     src = torch.tensor(f0, device=cuda)
     out = torch.empty_like(src)
     oop.step(src, out=out, nsteps=3)
@@ -570,12 +571,14 @@ def test_ds_halves_default_for_long_lines(bkma, cuda):
     p = AdvParams(160, 16384, 1, 0.001, 0.0, 1.0, -1.0, 1.0)
     ds, _ = _rows_plans(bkma, p)
     info = ds.info()
-    assert info["path"] == 5 and info["tile_cols"] == 3, info
+    assert info["path"] == 5 and info["tile_cols"] == 6, info
 
 
-def test_ds_halves_exception_lines_and_unsplittable(bkma, cuda, oracle):
+@pytest.mark.parametrize("W", [3, 6])
+def test_ds_halves_exception_lines_and_unsplittable(bkma, cuda, oracle, W):
     """Exception lines (offsets one cell either side of the line's) stay
-    within the staged window; windows the pair cannot carry take FP64."""
+    within the staged window; windows the pair cannot carry take FP64 (W = 3:
+    runs along the two quarters, W = 6: runs of 4-cell groups)."""
     import torch
     n1 = 16384
     # dx = 1.1 / n1 is inexact: the lines shifted by whole cells (v = -2, 3)
@@ -583,7 +586,7 @@ def test_ds_halves_exception_lines_and_unsplittable(bkma, cuda, oracle):
     p = AdvParams(6, n1, 1, 1.1 / n1, 0.0, 1.1, -2.0, 3.0)
     vel = np.array([1.0, 0.37, -2.0, 0.5, 3.0, -0.77])
     hv, _ = _rows_plans(bkma, p, velocity=vel)
-    hv.set_tile(3, 1, 256, 5)
+    hv.set_tile(W, 1, 256, 5)
     assert hv.info()["exception_lines"] > 0
     q, _ = _rows_plans(bkma, p, velocity=vel)
     q.set_tile(1, 1, 256, 5)
@@ -601,13 +604,14 @@ def test_ds_halves_exception_lines_and_unsplittable(bkma, cuda, oracle):
     assert np.abs(c.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
 
 
-def test_ds_halves_timeout_reported(bkma, cuda):
+@pytest.mark.parametrize("W", [3, 6])
+def test_ds_halves_timeout_reported(bkma, cuda, W):
     """A staging wait that gives up still reaches the cluster barrier: the
     call returns, the status reports the timeout and the field is untouched."""
     import torch
     p = AdvParams(4, 16384, 1, 0.001, 0.0, 1.0, -1.0, 1.0)
     hv, _ = _rows_plans(bkma, p)
-    hv.set_tile(3, 1, 256, 5)
+    hv.set_tile(W, 1, 256, 5)
     f0 = torch.tensor(_init(p, 48), device=cuda)
     a = f0.clone()
     hv.set_wait_limit(0)

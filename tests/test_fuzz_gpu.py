@@ -223,7 +223,7 @@ def test_fuzz_fp64_pair_forms_agree(bkma, cuda, case):
     x = np.arange(n1) / n1
     f0 = np.sin(2 * np.pi * x)[None, :, None] + 0.01 * rng.uniform(-1, 1, (n0, n1, n2))
     if n2 == 1:
-        forms = [(W, R, 256, 5) for W in (1, 2, 3, 4) for R in (1, 2, 3, 8)]
+        forms = [(W, R, 256, 5) for W in (1, 2, 3, 4, 5, 6) for R in (1, 2, 3, 8)]
     else:
         forms = ([(W, R, 256, 5) for W in (1, 2, 4) for R in (1, 3)]
                  + [(4, 1, 128, 4), (8, 1, 256, 4), (8, 0, 256, 6), (8, 2, 256, 6)])
