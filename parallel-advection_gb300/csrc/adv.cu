@@ -611,8 +611,9 @@ bkma_status adv_autotune(AdvPlanImpl &p, void *field, cudaStream_t st) {
                 if ((R != p.R || W != p.W) && adv_ds_rows_eligible(p, field, field, R) &&
                     (W != 2 || adv_ds_runs_ok(p, R)) && (W != 5 || adv_ds_lineq_ok(p)))
                     cands.push_back({W, R, 256, 5});
-        if (p.W != 3 && adv_ds_halves_ok(p) && ((uintptr_t)field % 16) == 0)
-            cands.push_back({3, 1, 256, 5});
+        if (adv_ds_halves_ok(p) && ((uintptr_t)field % 16) == 0)
+            for (int W : {3, 6})
+                if (W != p.W) cands.push_back({W, 1, 256, 5});
     } else if (n2 >= 8) {
         for (int W : {8, 16, 32, 64})
             if (W <= n2 || W == 8)
