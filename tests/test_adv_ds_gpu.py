@@ -604,6 +604,23 @@ def test_ds_halves_exception_lines_and_unsplittable(bkma, cuda, oracle, W):
     assert np.abs(c.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
 
 
+def test_ds_halves_autotune_keeps_the_bits(bkma, cuda):
+    """The tuner times every line form for 16384-cell lines (both half-line
+    cluster forms among them): whichever wins, the bits are the default's."""
+    import torch
+    p = AdvParams(4, 16384, 1, 0.0013, 0.0, 1.0, -2.0, 2.0)
+    ds, _ = _rows_plans(bkma, p)
+    f0 = torch.tensor(_init(p, 55), device=cuda)
+    info = ds.autotune(f0.clone())
+    assert info["path"] == 5, info
+    a, b = f0.clone(), f0.clone()
+    ds.step(a, nsteps=2)
+    ds.status()
+    fresh, _ = _rows_plans(bkma, p)
+    fresh.step(b, nsteps=2)
+    assert torch.equal(a, b), info
+
+
 @pytest.mark.parametrize("W", [3, 6])
 def test_ds_halves_timeout_reported(bkma, cuda, W):
     """A staging wait that gives up still reaches the cluster barrier: the
