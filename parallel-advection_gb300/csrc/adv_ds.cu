@@ -525,8 +525,10 @@ __global__ void __launch_bounds__(kDsRowsThreads) adv_ds_lineq(AdvDsRowsArgs a) 
 // contiguous bytes per lane (adv_ds_runs stores 8 bytes per lane, one L2
 // sector per cell: 4x the output in L2 write transactions). The two packed
 // pairs are ds_quad's (cells c, c + 1 and c + 2, c + 3 with the same split
-// taps), so the bits are the 4-cell kernel's; a group whose window holds a
-// tap the pair cannot carry, and exception lines, go through ds_quad itself.
+// taps), so the bits are the 4-cell kernel's; exception lines go through
+// ds_quad itself, and a group whose window holds a tap the pair cannot carry
+// is redone by ds_quad after the run (over the same thread's stores: inlined
+// in each of the three unrolled groups it made the hot loop 10 % slower).
 //
 // The split taps sit in a ring of 12 register slots, tap m (cell q + m) in
 // slot m % 12. Group u reads taps 4u .. 4u + NT + 2, so with the groups
