@@ -153,8 +153,8 @@ bkma_status bkma_adv_plan_autotune(bkma_adv_plan *plan, void *scratch_field, voi
  * the FP64 staged kernel on whole rows or 8-column strips), or path 6: FP64 column pairs streamed in FP32-pair
  * arithmetic (FP64, degree 3 or 5, even n2, n1 >= 64, every line's tap-0
  * offset d within -32 <= d <= 33 - npts, and in each group of 64 consecutive
- * columns of the (line, i2) space either d > -2 npts on every line, walked up
- * the rows, or d <= npts, walked down; R the row-segment mode as on
+ * columns of the (line, i2) space either d > -(npts + 2) on every line,
+ * walked up the rows, or d <= 2, walked down; R the row-segment mode as on
  * path 2, `threads` ignored: 256; the same bits as path 4; exception lines
  * and a field off the 16-byte grid run the FP64 staged kernel). R <= 1024 on
  * paths 0, 1, 3 and 5. */

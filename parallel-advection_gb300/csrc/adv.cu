@@ -540,9 +540,9 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
             p.stream_ok = false;
     if (d.dtype == BKMA_F64 && d.n2 % 2 == 0) {
         // the streamed FP32-pair form: each 64-column group (32 column pairs
-        // of the (line, i2) space) walks up its rows, loading 2 NT rows ahead
-        // of its stores (d > -2 NT on all its lines), or down (d <= NT); seams
-        // of at most 32 rows each way
+        // of the (line, i2) space) walks up its rows, loading NT + 2 rows
+        // ahead of its stores (d > -(NT + 2) on all its lines), or down
+        // (d <= 2); seams of at most 32 rows each way
         constexpr int kWin = 32;
         p.ds_stream_ok = n1 >= kStreamMinN1;
         p.ds_sr = 0;
@@ -554,8 +554,8 @@ bkma_status adv_precompute(AdvPlanImpl &p) {
                 if (p.exc_index[(size_t)l] >= 0) continue;
                 const int dd = stream_offset(p.base[(size_t)l], n1);
                 if (dd < -kWin || dd + NT - 1 > kWin) p.ds_stream_ok = false;
-                up = up && dd > -2 * NT;
-                down = down && dd <= NT;
+                up = up && dd > -(NT + 2);
+                down = down && dd <= 2;
                 p.ds_sr = std::max(p.ds_sr, std::max(dd + NT - 1, 0) + std::max(-dd, 0));
             }
             if (!up && !down) p.ds_stream_ok = false;

@@ -39,7 +39,7 @@ struct AdvPlanImpl {
     bool stream_ok = false;
     // FP64 plans: every non-exception line can stream in FP32-pair arithmetic
     // (adv_stream_ds.cu: |d| <= 32, and every 64-column group walks up, d >
-    // -2 npts on all its lines, or down, d <= npts), with ds_sr seam rows per
+    // -(npts + 2) on all its lines, or down, d <= 2), with ds_sr seam rows per
     // column pair (max(d + npts - 1, 0) + max(-d, 0), the largest over lines)
     bool ds_stream_ok = false;
     int ds_sr = 0;

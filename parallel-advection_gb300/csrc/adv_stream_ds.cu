@@ -9,20 +9,24 @@
 //  * work unit: a group of 32 column pairs (64 consecutive columns of the
 //    field's (line, i2) space, one 16-byte pair per lane; n2 is even, so a
 //    pair never straddles two lines) and a segment of its n1 rows, one warp;
-//  * every lane keeps two register rings: 2 npts raw rows (double2) and npts
-//    split taps (the FP32 pairs of the column-pair kernel). Row r's newest tap
-//    is split once when it is needed, the stencil is the column-pair kernel's
-//    (ds_stencil: the same operations per cell, so the same bits), the output
-//    is stored, and the raw slot of the row's oldest tap is reloaded with the
-//    row 2 npts further on: npts + 1 rows of loads in flight per lane, with an
-//    L2 prefetch further ahead;
+//  * every lane keeps two register rings: npts + 2 raw rows (double2) and
+//    npts split taps (the FP32 pairs of the column-pair kernel). Row r's
+//    newest tap is split once when it is needed, the stencil is the
+//    column-pair kernel's (ds_stencil: the same operations per cell, so the
+//    same bits), the output is stored, and the raw slot of the row's oldest
+//    tap is reloaded with the row npts + 2 further on: 3 rows of loads in
+//    flight per lane, the rows found in L2 by a prefetch 16 rows ahead. A raw
+//    row stays in its register until its last window's FP64 fallback could
+//    read it, so the ring's length sets the registers it holds (2 npts rows:
+//    e2 251, e8 256 GCells/s; npts + 4: 258 / 265; npts + 2: 266 / 277;
+//    npts + 1: 257 / 268);
 //  * a window holding a tap the split cannot carry runs the staged kernel's
 //    FP64 arithmetic from the raw ring (the same bits as the staged kernel);
 //  * in place: a lane loads every row before it overwrites it. Walking up
-//    the rows, its loads run 2 npts + d rows ahead of its stores, which holds
-//    for d > -2 npts; a warp whose lanes shift further down walks down the
-//    rows instead (the mirror image: loads run 2 npts - d - npts + 1 rows
-//    ahead, which holds for d <= npts), with its rings filled from the last
+//    the rows, its loads run npts + 2 + d rows ahead of its stores, which
+//    holds for d > -(npts + 2); a warp whose lanes shift further down walks
+//    down the rows instead (the mirror image: loads run 3 - d rows ahead,
+//    which holds for d <= 2), with its rings filled from the last
 //    tap down and the taps taken in the same order as walking up, so every
 //    cell gets the same operations. The plan allows this form only when
 //    every 64-column group has one direction that suits all its lines. Rows
@@ -66,7 +70,7 @@ __device__ __forceinline__ void stream_segment(const DsStreamArgs &a, int64_t li
                                                double *dst, int a0, int b0, int d,
                                                const double2 *above, const double2 *below, int M,
                                                int lane) {
-    constexpr int NR = 2 * NT;  // raw ring rows
+    constexpr int NR = NT + 2;  // raw ring rows
     const int64_t n2 = a.n2;
     const int len = b0 - a0;
     const int K = max(-d, 0);
@@ -93,10 +97,11 @@ __device__ __forceinline__ void stream_segment(const DsStreamArgs &a, int64_t li
         B[k] = make_float2(ab.y, ab.y);
     }
     const int y0 = REV ? b0 - 1 + d + NT - 1 : a0 + d;
-    // raw ring: slot j % NR holds ring row j; split ring: slot j % NT holds
-    // ring tap j; bad: bit k set when ring tap (newest - k) cannot be split
+    // raw ring: slot j % NR holds ring row j; split ring: slot j % NR holds
+    // ring tap j (NR slots, so that a block of NR rows maps every ring to the
+    // same slots); bad: bit k set when ring tap (newest - k) cannot be split
     double2 RR[NR];
-    float4 T[NT];
+    float4 T[NR];
     uint32_t bad = 0;
 #pragma unroll
     for (int j = 0; j < NR; ++j) RR[j] = ld(y0 + sg * j);
@@ -113,12 +118,12 @@ __device__ __forceinline__ void stream_segment(const DsStreamArgs &a, int64_t li
         for (int i = 0; i < NR; ++i) {
             const int u = u0 + i;
             // newest tap of output u: ring tap u + NT - 1, raw slot (i + NT - 1) % NR
-            bad = ((bad << 1) | (ds_split2(RR[(i + NT - 1) % NR], T[(i + NT - 1) % NT]) ? 0u : 1u)) &
+            bad = ((bad << 1) | (ds_split2(RR[(i + NT - 1) % NR], T[(i + NT - 1) % NR]) ? 0u : 1u)) &
                   ((1u << NT) - 1u);
             if (u < len) {
                 double2 o;
                 if (bad == 0u) {
-                    o = ds_stencil<NT, REV>(T, i % NT, A, B);
+                    o = ds_stencil<NT, REV>(T, i, A, B);
                 } else {
                     // FP64 direct form, the staged kernel's arithmetic; tap k
                     // is ring tap k (up) or NT - 1 - k (down)
@@ -174,7 +179,7 @@ __global__ void __launch_bounds__(kDsWarps * 32, 2) adv_stream_ds(DsStreamArgs a
     }
     // walk up unless a lane shifts too far down for it (the plan checked that
     // walking down then suits every lane of the group)
-    const bool up = __all_sync(0xFFFFFFFFu, !ok || d > -2 * NT);
+    const bool up = __all_sync(0xFFFFFFFFu, !ok || d > -(NT + 2));
     // seams of a lane: rows 0 .. M-1 are the segment's first M rows (read by
     // the segment below it), rows M .. M+K-1 its last K rows (read by the one
     // above); a neighbour's same lane has the same line, so the same M and K

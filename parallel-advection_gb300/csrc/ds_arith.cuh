@@ -70,20 +70,22 @@ __device__ __forceinline__ void two_sum2(float2 a, float2 b, float2 &t, float2 &
     err = __fadd2_rn(ea, eb);
 }
 
-// sum_k w_k x_k of a column pair from its NT split taps T[(u + k) % NT]
-// (u: ring position of tap 0), or T[(u + NT - 1 - k) % NT] when REV (a ring
-// filled from the last tap down); two FP64 results. The high products a h are
+// sum_k w_k x_k of a column pair from its NT split taps T[(u + k) % NS]
+// (u: ring position of tap 0, NS >= NT ring slots), or T[(u + NT - 1 - k) %
+// NS] when REV (a ring filled from the last tap down); two FP64 results. The
+// high products a h are
 // summed exactly by a pairwise TwoSum tree (taps (0,1), (2,3), (4,5), then
 // the partial sums); the low-order terms (a l, b h, the product errors and
 // the tree's errors) are added in FP32 in short independent chains.
-template <int NT, bool REV = false>
-__device__ __forceinline__ double2 ds_stencil(const float4 (&T)[NT], int u, const float2 (&A)[NT],
+template <int NT, bool REV = false, int NS>
+__device__ __forceinline__ double2 ds_stencil(const float4 (&T)[NS], int u, const float2 (&A)[NT],
                                               const float2 (&B)[NT]) {
     static_assert(NT == 4 || NT == 6, "4 or 6 taps");
+    static_assert(NS >= NT, "a ring of at least NT taps");
     float2 p[NT], e[NT], La, Lb;
 #pragma unroll
     for (int k = 0; k < NT; ++k) {
-        const float4 v = T[(u + (REV ? NT - 1 - k : k)) % NT];
+        const float4 v = T[(u + (REV ? NT - 1 - k : k)) % NS];
         const float2 h = make_float2(v.x, v.y), l = make_float2(v.z, v.w);
         p[k] = __fmul2_rn(h, A[k]);
         e[k] = __ffma2_rn(h, A[k], neg2(p[k]));  // exact error of the product

@@ -3,7 +3,7 @@ through the C ABI.
 
 The streamed form computes every cell with the same operations as the staged
 column-pair kernel (path 4), so the two give the same bits wherever both
-apply, walking up the rows or, for lines shifted 2 npts or more rows down,
+apply, walking up the rows or, for lines shifted npts + 2 or more rows down,
 down them; it is the default for column pairs the staged form cannot take
 (lines too tall for a shared-memory strip, rows 1 MB or more apart). Tolerances as
 in test_adv_ds_gpu.py: 2e-13 max|f| per step against the FP64 staged kernel,
@@ -186,7 +186,7 @@ def test_stream_ds_misaligned_field_runs_fp64(bkma, cuda):
 
 # per-line velocities whose shifts run from -12.6 to +26.6 cells (n1 = 1024,
 # dt = 0.001): tap-0 offsets d from about +10 down to -29; each 64-column group
-# is one line (n2 = 64), and the lines with d <= -2 npts walk down their rows
+# is one line (n2 = 64), and the lines with d <= -(npts + 2) walk down their rows
 FAR_VEL = np.array([-12.3, -6.0, 0.3, 5.0, 9.0, 13.0, 20.0, 26.0])
 
 
