@@ -19,7 +19,7 @@
 //    row stays in its register until its last window's FP64 fallback could
 //    read it, so the ring's length sets the registers it holds (2 npts rows:
 //    e2 251, e8 256 GCells/s; npts + 4: 258 / 265; npts + 2: 266 / 277;
-//    npts + 1: 257 / 268);
+//    npts + 1: 257 / 268; npts, one row of loads ahead: 226 / 236);
 //  * a window holding a tap the split cannot carry runs the staged kernel's
 //    FP64 arithmetic from the raw ring (the same bits as the staged kernel);
 //  * in place: a lane loads every row before it overwrites it. Walking up
