@@ -32,6 +32,16 @@
 // against the staged FP64 kernel the result differs by at most ~2e-13 max|f|
 // per step. One step reads and writes each cell once (16 B per cell-step); the
 // tile is read completely before the first store, so in place is legal.
+//
+// The same arithmetic per cell (ds_arith.cuh), so the same bits, in the other
+// staged forms of this file (path 5): contiguous lines (n2 = 1) as 4-cell
+// groups (adv_ds_rows, one per thread; adv_ds_qruns, runs of them with
+// sliding register rings; adv_ds_lineq, lines of 16-128 cells shared by a
+// warp's lanes through shuffles), as runs along two sections (adv_ds_runs),
+// as half lines in 2-CTA clusters (adv_ds_halves, adv_ds_halves_q), k fused
+// steps (adv_ds_rows_fused); and whole slabs of short lines with an even n2
+// (adv_ds_slabs). Each stages its lines by bulk copies completed on an
+// mbarrier with a bounded wait (stage_block2).
 #include <cuda.h>
 
 #include <algorithm>
