@@ -5,8 +5,9 @@
 // of what HBM allows at 16 B per cell-step. This kernel keeps the field in
 // FP64 in HBM and forms each cell's sum_k w_k f_k from FP32 pieces:
 //
-//  * staging: one CTA = one slab i0 x 8 columns (64-byte rows) x all n1 rows,
-//    copied by TMA (cp.async.bulk.tensor, FP64 tensor map) into shared memory;
+//  * staging: one CTA = one slab i0 x 4 or 8 columns (32- or 64-byte rows; 4
+//    by default, six CTAs of 128 threads per SM) x all n1 rows, copied by TMA
+//    (cp.async.bulk.tensor, FP64 tensor map) into shared memory;
 //  * split: a thread walks a run of consecutive rows of one column pair and
 //    splits every tap it loads once, into a register ring of npts pairs:
 //    x = h + l, h = x's leading 24 bits (truncated; integer operations on the
