@@ -530,6 +530,32 @@ def test_ds_lineq_exception_lines_and_unsplittable(bkma, cuda, oracle):
     assert np.abs(c.cpu().numpy() - want).max() <= 1e-11 * np.abs(want).max()
 
 
+def test_ds_lineq_timeout_reported(bkma, cuda):
+    """A staging wait that gives up: every lane still leaves through the same
+    path (no shuffle left waiting), the status reports the timeout and the
+    field is untouched."""
+    import torch
+    p = AdvParams(40, 64, 1, 0.003, 0.0, 1.0, -2.0, 2.0)
+    g, _ = _rows_plans(bkma, p)
+    g.set_tile(5, 8, 256, 5)
+    f0 = torch.tensor(_init(p, 57), device=cuda)
+    a = f0.clone()
+    g.set_wait_limit(0)
+    g.step(a)
+    with pytest.raises(bkma.BkmaError) as e:
+        g.status()
+    assert e.value.status == 4
+    assert torch.equal(a, f0)
+    g.set_wait_limit(1 << 22)
+    g.step(a)
+    g.status()
+    q, _ = _rows_plans(bkma, p)
+    q.set_tile(1, 8, 256, 5)
+    b = f0.clone()
+    q.step(b)
+    assert torch.equal(a, b)
+
+
 # ---- lines of 8192 cells and more: half lines in 2-CTA clusters (W = 3)
 
 
